@@ -1,0 +1,320 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 render path: traced rays per second.
+
+Workload (default): the response-matrix configuration, a 12 m Davies-Cotton
+dish (380 hex facets, f = 15 m, 0.5 mrad tilt errors, 4 mast cylinders and a
+camera box) with a 2048-pixel hexagonal camera, 4096 point sources on a
+64 x 64 grid within +-3 deg and 256 Monte-Carlo samples per facet: one step
+renders the dense 4096 x 2048 response matrix (3.99e8 rays). Inputs are
+seeded synthetic scenes (iactrace_gb300.workloads), resident on the device.
+
+  value     rays/s of the render step (device time, CUDA events, L2 flushed
+            before every timed step by a 256 MiB write outside the events)
+  e2e       rays/s through the public API with host buffers: pinned
+            sources/values copied in, the matrix copied back, every step
+  roofline  the render kernel's algorithmic FP32 flops per launch over its
+            event-timed duration, against an FP32 FMA peak measured live on
+            the same GPU by a probe kernel of the library
+  cpu_baseline  the C++ FP32 restatement of the reference (OpenMP, all host
+            cores) on a bounded sample of the same workload
+
+`--impl reference` times the reference algorithm's CPU restatement instead
+(the reference itself is JAX and cannot be installed here).
+Multi-GPU: one process per GPU, each renders its own full workload
+(replicas, weak scaling); rank 0 prints the max-over-ranks timing.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import torch
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "traced rays/s: fwd and fwd+adjoint vs plain fwd kernel, img err<=1e-5 vs FP64"
+# algorithmic FP32 flops per ray (FMA = 2), reference evaluation without early-out:
+# point primary 26 + 4 cylinders x 98 + box 29 + sensor plane 34 + hex bin 56
+F_RAY = {"response": 537, "plain": 503, "cassegrain": 894}
+
+
+def _env_rank():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, ValueError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax = float(p[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def build_workload(name: str):
+    from iactrace_gb300 import workloads as W
+    if name == "response":
+        return W.response_matrix(), "response"
+    if name == "plain":
+        return W.plain_forward(), "image"
+    if name == "cassegrain":
+        return W.cassegrain(), "image"
+    raise SystemExit(f"unknown workload {name}")
+
+
+def workload_config(name, tel, S, mode, flush):
+    F = sum(len(g) for g in tel.mirror_groups if g.optical_stage == 0)
+    M = tel.mirror_groups[0].n_samples
+    cfg = {"workload": {"response": "response_matrix_dc380_hex2048", "plain": "plain_forward_dc380_square960",
+                        "cassegrain": "cassegrain_61seg_square1024"}[name],
+           "facets": F, "samples_per_facet": M, "sources": S,
+           "pixels": int(math.prod(tel.sensors[0].get_accumulator_shape())),
+           "output": "response matrix (S, P) fp32" if mode == "response" else "image fp32",
+           "rays_per_step": F * M * S, "l2": flush}
+    return cfg, F * M * S
+
+
+def fp32_peak_tflops(dev) -> float:
+    """FP32 throughput of an FMA-chain probe kernel on this GPU (TFLOP/s)."""
+    from iactrace_gb300 import _native as N
+    lib = N.load()
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    blocks, iters = sms * 16, 4096
+    out = torch.empty(blocks * 256, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(3):
+        N.check(lib.iact_probe_fma(out.data_ptr(), blocks, iters, stream.cuda_stream))
+    best = float("inf")
+    for _ in range(5):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        N.check(lib.iact_probe_fma(out.data_ptr(), blocks, iters, stream.cuda_stream))
+        b.record(stream)
+        b.synchronize()
+        best = min(best, a.elapsed_time(b) / 1e3)
+    flops = blocks * 256 * iters * 8 * 2
+    return flops / best / 1e12
+
+
+def cpu_baseline(name, tel, src, val, stype, mode, target_s=12.0):
+    """C++ FP32 restatement on all host cores, bounded sample of the workload."""
+    import oracle.oracle as O
+    threads = os.cpu_count() or 1
+    F = sum(len(g) for g in tel.mirror_groups if g.optical_stage == 0)
+    M = tel.mirror_groups[0].n_samples
+    omode = "response" if mode == "response" else "image"
+    n = max(1, min(src.shape[0], threads))
+    t = time.perf_counter()
+    O.render(tel, src[:n], val[:n], stype, 0, mode=omode, dtype="f32", threads=threads)
+    dt = time.perf_counter() - t
+    rate = n * F * M / max(dt, 1e-9)
+    n2 = int(max(n, min(src.shape[0], rate * target_s / (F * M))))
+    t = time.perf_counter()
+    O.render(tel, src[:n2], val[:n2], stype, 0, mode=omode, dtype="f32", threads=threads)
+    dt = time.perf_counter() - t
+    rays = n2 * F * M
+    return {"value": rays / dt, "unit": "rays/s", "cores": threads, "kind": "port",
+            "sample": f"{n2} of {src.shape[0]} sources x {F} facets x {M} samples ({rays:.3g} rays, {dt:.1f} s)"}
+
+
+def run_reference(args, rank, world):
+    """CPU restatement of the reference algorithm, all host threads, bounded steps."""
+    if rank != 0:
+        return
+    import oracle.oracle as O
+    (tel, src, val, stype), mode = build_workload(args.workload)
+    cfg, rays_full = workload_config(args.workload, tel, src.shape[0], mode, "n/a (CPU)")
+    threads = os.cpu_count() or 1
+    F = cfg["facets"]
+    M = cfg["samples_per_facet"]
+    omode = "response" if mode == "response" else "image"
+    n = max(1, min(src.shape[0], threads))
+    t = time.perf_counter()
+    O.render(tel, src[:n], val[:n], stype, 0, mode=omode, dtype="f32", threads=threads)
+    rate = n * F * M / max(time.perf_counter() - t, 1e-9)
+    budget = 150.0 / max(1, args.steps + args.warmup)
+    ns = int(max(1, min(src.shape[0], rate * budget / (F * M))))
+    for _ in range(args.warmup):
+        O.render(tel, src[:ns], val[:ns], stype, 0, mode=omode, dtype="f32", threads=threads)
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        O.render(tel, src[:ns], val[:ns], stype, 0, mode=omode, dtype="f32", threads=threads)
+    dt = time.perf_counter() - t
+    rays = ns * F * M * args.steps
+    value = rays / dt
+    sample = f"{ns} of {src.shape[0]} sources x {F} facets x {M} samples per step"
+    print(json.dumps({
+        "metric": METRIC, "value": value, "unit": "rays/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": cfg, "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": "rays/s", "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "rays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "reference is JAX (not installable here); timed its C++ FP32 restatement (oracle/) on host cores",
+    }), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="response", choices=["response", "plain", "cassegrain"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    rank, world, local = _env_rank()
+    dist = world > 1
+    if dist:
+        import torch.distributed as tdist
+        tdist.init_process_group("nccl" if args.impl == "ours" else "gloo")
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        if dist:
+            tdist.destroy_process_group()
+        return
+
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    import iactrace_gb300 as it
+    from iactrace_gb300 import _native as N
+    N.load(build_if_missing=True)
+    (tel, src_h, val_h, stype), mode = build_workload(args.workload)
+    S = src_h.shape[0]
+    flush_buf = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    cfg, rays = workload_config(args.workload, tel, S, mode, "flushed before each step (256 MiB write)")
+    fn = it.render_response_matrix if mode == "response" else it.render
+    src = src_h.to(dev)
+    val = val_h.to(dev)
+    stream = torch.cuda.current_stream(dev)
+
+    opts = N.IactOpts()
+    kev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+
+    for _ in range(args.warmup):
+        out = fn(tel, src, val, stype)
+    torch.cuda.synchronize(dev)
+
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    time.sleep(0.3)
+    if dist:
+        tdist.barrier()
+    torch.cuda.synchronize(dev)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for k in range(args.steps):
+        flush_buf.fill_(float(k))
+        opts.kernel_events[0] = kev[k][0].cuda_event
+        opts.kernel_events[1] = kev[k][1].cuda_event
+        ev[k][0].record(stream)
+        out = fn(tel, src, val, stype, opts=opts)
+        ev[k][1].record(stream)
+    torch.cuda.synchronize(dev)
+    if dist:
+        tdist.barrier()
+    step_s = sum(a.elapsed_time(b) for a, b in ev) / 1e3 / args.steps
+    kern_s = sum(a.elapsed_time(b) for a, b in kev) / 1e3 / args.steps
+
+    # e2e through the public API with host buffers
+    src_pin = src_h.pin_memory()
+    val_pin = val_h.pin_memory()
+    out_pin = torch.empty(out.shape, dtype=torch.float32).pin_memory()
+    for _ in range(2):
+        o = fn(tel, src_pin.to(dev, non_blocking=True), val_pin.to(dev, non_blocking=True), stype)
+        out_pin.copy_(o, non_blocking=True)
+    torch.cuda.synchronize(dev)
+    e2e_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for k in range(args.steps):
+        flush_buf.fill_(float(k))
+        e2e_ev[k][0].record(stream)
+        o = fn(tel, src_pin.to(dev, non_blocking=True), val_pin.to(dev, non_blocking=True), stype)
+        out_pin.copy_(o, non_blocking=True)
+        e2e_ev[k][1].record(stream)
+    torch.cuda.synchronize(dev)
+    e2e_s = sum(a.elapsed_time(b) for a, b in e2e_ev) / 1e3 / args.steps
+    clk = clocks.stop()
+
+    t = torch.tensor([step_s, kern_s, e2e_s], device=dev, dtype=torch.float64)
+    if dist:
+        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+    step_s, kern_s, e2e_s = t.tolist()
+
+    peak = fp32_peak_tflops(dev)
+    achieved = F_RAY[args.workload] * rays / kern_s / 1e12
+    h2d = src_h.numel() * 4 + val_h.numel() * 4
+    d2h = out.numel() * 4
+    line = {
+        "metric": METRIC, "value": rays * world / step_s, "unit": "rays/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scenes and sources)", "config": cfg,
+        "e2e": {"value": rays * world / e2e_s, "unit": "rays/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3},
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                     "traffic": None, "kernel": "k_render", "kernel_ms": kern_s * 1e3,
+                     "flops_per_ray": F_RAY[args.workload],
+                     "peak_source": "measured live: FP32 FMA-chain probe kernel (iact_probe_fma)"},
+        "gpu_launches": 2 * args.steps,
+        "clocks": clk,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(args.workload, tel, src_h, val_h, stype, mode)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        tdist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

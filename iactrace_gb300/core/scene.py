@@ -1,0 +1,141 @@
+"""Packing of a Telescope into the device tables of the C ABI.
+
+Stage-0 groups are concatenated in list order (core/render.py:202-205);
+stage >= 1 mirrors are flattened in (stage, group, mirror) order, so the
+kernels' "first strict minimum" equals the reference's argmin over mirrors
+and strict ``<`` over groups (core/render.py:62-71, :110). Obstruction groups
+are concatenated per kind: the shadow mask only asks whether any member of
+any group is hit (core/render.py:38-40).
+"""
+from __future__ import annotations
+
+import ctypes
+from collections import defaultdict
+
+import numpy as np
+import torch
+
+from .. import _native as N
+
+
+def stages_of(tel):
+    """core/render.py:12-18 _get_stages."""
+    by = defaultdict(list)
+    for g in tel.mirror_groups:
+        by[g.optical_stage].append(g)
+    return dict(sorted(by.items()))
+
+
+def _f32(t, device):
+    return t.detach().to(device=device, dtype=torch.float32).contiguous()
+
+
+def _mirror_records(stage_groups) -> np.ndarray:
+    recs = []
+    for stage, groups in stage_groups:
+        for g in groups:
+            asph = g.aspheric.detach().cpu().float().tolist()
+            if len(asph) > N.IACT_MAX_ASPH:
+                raise ValueError(f"at most {N.IACT_MAX_ASPH} aspheric coefficients are supported")
+            polygon = hasattr(g, "vertices")
+            for i in range(len(g)):
+                m = N.IactMirror()
+                m.stage = int(stage)
+                m.aperture = N.APERTURE_POLYGON if polygon else N.APERTURE_DISK
+                m.n_asph = len(asph)
+                m.pos[:] = g.positions[i].detach().cpu().tolist()
+                m.rot[:] = g.rotations[i].detach().cpu().tolist()
+                m.offset[:] = g.offsets[i].detach().cpu().tolist()
+                m.curvature, m.conic = g.curvature, g.conic
+                for k, a in enumerate(asph):
+                    m.asph[k] = a
+                if polygon:
+                    v = g.vertices[i].detach().cpu().tolist()
+                    if len(v) > N.IACT_MAX_POLY:
+                        raise ValueError(f"at most {N.IACT_MAX_POLY} polygon vertices are supported")
+                    m.n_vert = len(v)
+                    for k, (x, y) in enumerate(v):
+                        m.vert[k][0], m.vert[k][1] = x, y
+                else:
+                    m.radius = float(g.radii[i])
+                recs.append(bytes(m))
+    if len(recs) > N.IACT_MAX_STAGE_MIRRORS:
+        raise ValueError(f"at most {N.IACT_MAX_STAGE_MIRRORS} mirrors over all stages >= 1 are supported")
+    return np.frombuffer(b"".join(recs), dtype=np.uint8) if recs else np.zeros(0, np.uint8)
+
+
+class PackedScene:
+    """Device-resident tables + the iact_scene_t that points at them."""
+
+    def __init__(self, tel, device):
+        device = torch.device(device)
+        st = stages_of(tel)
+        prim = st.get(0, [])
+        self.has_primary = len(prim) > 0
+        self.F = sum(len(g) for g in prim)
+        ms = {g.n_samples for g in prim}
+        if len(ms) > 1:
+            raise ValueError(f"all primary groups must have the same sample count, got {sorted(ms)}")
+        self.M = ms.pop() if ms else 0
+        d = N.IactScene()
+        d.n_facets, d.n_samples = self.F, self.M
+        if self.F and self.M:
+            cat = lambda name: torch.cat([getattr(g, name).detach().float() for g in prim])
+            self.facet_pos = _f32(cat("positions"), device)
+            self.facet_rot = _f32(cat("rotations"), device)
+            self.facet_scale = _f32(cat("perturbation_scale"), device)
+            self.points = _f32(cat("points"), device)
+            self.normals = _f32(cat("normals"), device)
+            self.delta = _f32(cat("perturbation_delta"), device)
+            self.weights = _f32(cat("weights").reshape(self.F, self.M), device)
+            for name in ("facet_pos", "facet_rot", "facet_scale", "points", "normals", "delta", "weights"):
+                setattr(d, name, getattr(self, name).data_ptr())
+        later = [(s, gs) for s, gs in st.items() if s != 0]
+        recs = _mirror_records(later)
+        self.n_mirrors = len(recs) // ctypes.sizeof(N.IactMirror)
+        self.mirrors = torch.from_numpy(recs.copy()).to(device) if self.n_mirrors else None
+        d.n_mirrors = self.n_mirrors
+        d.mirrors = self.mirrors.data_ptr() if self.n_mirrors else None
+        kinds = defaultdict(list)
+        for g in (tel.obstruction_groups or []):
+            kinds[g.kind].append(g.table().float())
+        self.obst = {}
+        for kind in ("cyl", "box", "sph", "obox", "tri"):
+            if kinds[kind]:
+                t = _f32(torch.cat(kinds[kind]), device)
+                self.obst[kind] = t
+                setattr(d, "n_" + kind, int(t.shape[0]))
+                setattr(d, kind, t.data_ptr())
+        self.desc = d
+        self.device = device
+        size = ctypes.c_size_t(0)
+        lib = N.load()
+        N.check(lib.iact_workspace_size(ctypes.byref(d), ctypes.byref(size)))
+        self.ws_bytes = int(size.value)
+
+
+def _fingerprint(tel):
+    fp = [id(tel)]
+    for g in tel.mirror_groups:
+        for name in ("positions", "rotations", "perturbation_scale", "points", "normals", "perturbation_delta",
+                     "weights", "offsets", "aspheric"):
+            t = getattr(g, name, None)
+            if t is not None:
+                fp.append((id(t), t._version))
+        fp.append((g.optical_stage, g.curvature, g.conic))
+    for g in (tel.obstruction_groups or []):
+        fp.append(id(g))
+    return tuple(fp)
+
+
+def pack_scene(tel, device) -> PackedScene:
+    """Packed tables of `tel` on `device`, cached until a tensor changes."""
+    cache = tel.__dict__.setdefault("_packed", {})
+    key = str(torch.device(device))
+    fp = _fingerprint(tel)
+    hit = cache.get(key)
+    if hit is not None and hit[0] == fp:
+        return hit[1]
+    ps = PackedScene(tel, device)
+    cache[key] = (fp, ps)
+    return ps

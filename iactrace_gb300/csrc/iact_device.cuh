@@ -1,0 +1,394 @@
+// Per-ray device math of the render path (sm_103a).
+//
+// Each function states the reference expression it evaluates
+// (GerritRo/iactrace v0.4.0). The per-primitive and per-mirror constants the
+// reference recomputes on every ray (cylinder axis and height, triangle
+// edges, mirror rotation matrices, z0) are computed once per launch, with
+// the same float32 operations, into compact shared-memory records.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/iactrace_gb300.h"
+
+namespace iact {
+
+constexpr float kBig = 1e10f;  // the reference's miss / shadow sentinel
+constexpr float kEps = 1e-8f;
+constexpr unsigned kFull = 0xffffffffu;
+
+// ------------------------------------------------------------ table records
+// Sizes in floats; records are packed back to back in shared memory.
+constexpr int kCylF = 8;    // p1(3) axis(3) height r*r
+constexpr int kBoxF = 6;    // min(3) max(3)
+constexpr int kSphF = 4;    // center(3) r*r
+constexpr int kOboxF = 15;  // center(3) half(3) R(9) row-major local->world
+constexpr int kTriF = 9;    // v0(3) e1(3) e2(3)
+constexpr int kMirF = 48;   // see MirRec
+
+// One stage >= 1 mirror, as laid out in shared memory (floats).
+struct MirRec {
+  float R[9];       // 0..8  local->world rotation
+  float pos[3];     // 9..11
+  float off[2];     // 12..13
+  float unused14;   // 14
+  float c;          // 15  curvature
+  float kp1;        // 16  1 + conic (float32)
+  float alpha;      // 17  (1+k) c c (float32)
+  float r2ap;       // 18  disk radius^2
+  float n_asph;     // 19
+  float aperture;   // 20
+  float n_vert;     // 21
+  float stage;      // 22
+  float k;          // 23  conic constant
+  float asph[8];    // 24..31
+  float vert[16];   // 32..47
+};
+static_assert(sizeof(MirRec) == kMirF * sizeof(float), "MirRec layout");
+
+struct V3 {
+  float x, y, z;
+};
+__device__ __forceinline__ V3 mk(float x, float y, float z) { return {x, y, z}; }
+__device__ __forceinline__ V3 operator-(V3 a, V3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ V3 operator+(V3 a, V3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ V3 operator*(float s, V3 a) { return {s * a.x, s * a.y, s * a.z}; }
+__device__ __forceinline__ float dot(V3 a, V3 b) { return fmaf(a.z, b.z, fmaf(a.y, b.y, a.x * b.x)); }
+
+// core/transforms.py:72-107 euler_to_matrix: R = (Rz @ Ry) @ Rx, degrees.
+__device__ __forceinline__ void euler_to_matrix(float tip, float tilt, float rot, float* R) {
+  const float k = 0.017453292519943295f;  // pi / 180
+  float sx, cx, sy, cy, sz, cz;
+  sincosf(tip * k, &sx, &cx);
+  sincosf(tilt * k, &sy, &cy);
+  sincosf(rot * k, &sz, &cz);
+  // Rz @ Ry = [[cz*cy, -sz, cz*sy], [sz*cy, cz, sz*sy], [-sy, 0, cy]]
+  float a00 = cz * cy, a01 = -sz, a02 = cz * sy;
+  float a10 = sz * cy, a11 = cz, a12 = sz * sy;
+  float a20 = -sy, a21 = 0.f, a22 = cy;
+  // (Rz @ Ry) @ Rx, Rx = [[1,0,0],[0,cx,-sx],[0,sx,cx]]
+  R[0] = a00; R[1] = a01 * cx + a02 * sx; R[2] = a02 * cx - a01 * sx;
+  R[3] = a10; R[4] = a11 * cx + a12 * sx; R[5] = a12 * cx - a11 * sx;
+  R[6] = a20; R[7] = a21 * cx + a22 * sx; R[8] = a22 * cx - a21 * sx;
+}
+
+__device__ __forceinline__ V3 rmul(const float* R, V3 v) {
+  return {fmaf(R[2], v.z, fmaf(R[1], v.y, R[0] * v.x)), fmaf(R[5], v.z, fmaf(R[4], v.y, R[3] * v.x)),
+          fmaf(R[8], v.z, fmaf(R[7], v.y, R[6] * v.x))};
+}
+__device__ __forceinline__ V3 rtmul(const float* R, V3 v) {
+  return {fmaf(R[6], v.z, fmaf(R[3], v.y, R[0] * v.x)), fmaf(R[7], v.z, fmaf(R[4], v.y, R[1] * v.x)),
+          fmaf(R[8], v.z, fmaf(R[5], v.y, R[2] * v.x))};
+}
+
+// ------------------------------------------------------------- primitives
+// Each returns true when the primitive's t (as the reference computes it)
+// is < 1e10, i.e. when it shadows the ray (core/render.py:40). The group
+// minimum of the reference is never NaN (every t passes a jnp.where that
+// maps NaN to inf), so "some member's t < 1e10" is the same test.
+
+// core/intersections.py:44-87 intersect_cylinder
+__device__ __forceinline__ bool cyl_shadows(const float* c, V3 o, V3 d) {
+  V3 p1 = mk(c[0], c[1], c[2]), ax = mk(c[3], c[4], c[5]);
+  float h = c[6], r2 = c[7];
+  V3 oc = o - p1;
+  float oca = dot(oc, ax), rda = dot(d, ax);
+  V3 ocp = oc - oca * ax;
+  V3 rdp = d - rda * ax;
+  float a = dot(rdp, rdp);
+  float b = 2.f * dot(ocp, rdp);
+  float cc = dot(ocp, ocp) - r2;
+  float disc = b * b - 4.f * a * cc;
+  float sq = sqrtf(fmaxf(disc, 0.f));
+  float inv2a = __frcp_rn(2.f * a + kEps);
+  float t1 = (-b - sq) * inv2a;
+  float t2 = (-b + sq) * inv2a;
+  float y1 = fmaf(t1, rda, oca), y2 = fmaf(t2, rda, oca);
+  bool hit = (disc >= 0.f) && (((t1 > kEps) && (y1 >= 0.f) && (y1 <= h) && (t1 < kBig)) ||
+                               ((t2 > kEps) && (y2 >= 0.f) && (y2 <= h) && (t2 < kBig)));
+  float invr = __frcp_rn(rda + kEps);
+  float tb = -oca * invr;
+  float tt = (h - oca) * invr;
+  V3 pb = ocp + tb * rdp, pt = ocp + tt * rdp;
+  hit = hit || ((tb > kEps) && (dot(pb, pb) <= r2) && (tb < kBig));
+  hit = hit || ((tt > kEps) && (dot(pt, pt) <= r2) && (tt < kBig));
+  return hit;
+}
+
+// core/intersections.py:90-110 intersect_box; jnp.minimum/maximum propagate
+// NaN, so a NaN slab value means no hit.
+__device__ __forceinline__ bool box_shadows(const float* bx, V3 o, V3 d) {
+  float ix = __frcp_rn(d.x + kEps), iy = __frcp_rn(d.y + kEps), iz = __frcp_rn(d.z + kEps);
+  float x1 = (bx[0] - o.x) * ix, x2 = (bx[3] - o.x) * ix;
+  float y1 = (bx[1] - o.y) * iy, y2 = (bx[4] - o.y) * iy;
+  float z1 = (bx[2] - o.z) * iz, z2 = (bx[5] - o.z) * iz;
+  bool nan = isnan(x1) || isnan(x2) || isnan(y1) || isnan(y2) || isnan(z1) || isnan(z2);
+  float tmin = fmaxf(fmaxf(fminf(x1, x2), fminf(y1, y2)), fminf(z1, z2));
+  float tmax = fminf(fminf(fmaxf(x1, x2), fmaxf(y1, y2)), fmaxf(z1, z2));
+  bool hit = (tmax >= tmin) && (tmax > kEps) && !nan;
+  float tr = (tmin > kEps) ? tmin : tmax;
+  return hit && (tr < kBig);
+}
+
+// core/intersections.py:195-226 intersect_sphere
+__device__ __forceinline__ bool sph_shadows(const float* s, V3 o, V3 d) {
+  V3 oc = o - mk(s[0], s[1], s[2]);
+  float a = dot(d, d);
+  float b = 2.f * dot(oc, d);
+  float c = dot(oc, oc) - s[3];
+  float disc = b * b - 4.f * a * c;
+  float sq = sqrtf(fmaxf(disc, 0.f));
+  float inv2a = __frcp_rn(2.f * a + kEps);
+  float t1 = (-b - sq) * inv2a, t2 = (-b + sq) * inv2a;
+  return (disc >= 0.f) && (((t1 > kEps) && (t1 < kBig)) || ((t2 > kEps) && (t2 < kBig)));
+}
+
+__device__ __forceinline__ float sgnf(float v) { return v > 0.f ? 1.f : (v < 0.f ? -1.f : 0.f); }
+
+// core/intersections.py:113-149 intersect_oriented_box
+__device__ __forceinline__ bool obox_shadows(const float* b, V3 o, V3 d) {
+  const float* R = b + 6;
+  V3 lo = rtmul(R, o - mk(b[0], b[1], b[2]));
+  V3 ld = rtmul(R, d);
+  float ix = __frcp_rn(ld.x + kEps * sgnf(ld.x + kEps));
+  float iy = __frcp_rn(ld.y + kEps * sgnf(ld.y + kEps));
+  float iz = __frcp_rn(ld.z + kEps * sgnf(ld.z + kEps));
+  float x1 = (-b[3] - lo.x) * ix, x2 = (b[3] - lo.x) * ix;
+  float y1 = (-b[4] - lo.y) * iy, y2 = (b[4] - lo.y) * iy;
+  float z1 = (-b[5] - lo.z) * iz, z2 = (b[5] - lo.z) * iz;
+  bool nan = isnan(x1) || isnan(x2) || isnan(y1) || isnan(y2) || isnan(z1) || isnan(z2);
+  float tmin = fmaxf(fmaxf(fminf(x1, x2), fminf(y1, y2)), fminf(z1, z2));
+  float tmax = fminf(fminf(fmaxf(x1, x2), fmaxf(y1, y2)), fmaxf(z1, z2));
+  bool hit = (tmax >= tmin) && (tmax > kEps) && !nan;
+  float tr = (tmin > kEps) ? tmin : tmax;
+  return hit && (tr > kEps) && (tr < kBig);
+}
+
+// core/intersections.py:152-192 intersect_triangle (Moller-Trumbore)
+__device__ __forceinline__ bool tri_shadows(const float* t, V3 o, V3 d) {
+  V3 v0 = mk(t[0], t[1], t[2]), e1 = mk(t[3], t[4], t[5]), e2 = mk(t[6], t[7], t[8]);
+  V3 h = mk(d.y * e2.z - d.z * e2.y, d.z * e2.x - d.x * e2.z, d.x * e2.y - d.y * e2.x);
+  float a = dot(e1, h);
+  bool parallel = fabsf(a) < kEps;
+  float f = __frcp_rn(a + kEps * sgnf(a + kEps));
+  V3 s = o - v0;
+  float u = f * dot(s, h);
+  V3 q = mk(s.y * e1.z - s.z * e1.y, s.z * e1.x - s.x * e1.z, s.x * e1.y - s.y * e1.x);
+  float v = f * dot(d, q);
+  float tt = f * dot(e2, q);
+  return !parallel && (u >= 0.f) && (u <= 1.f) && (v >= 0.f) && (u + v <= 1.f) && (tt > kEps) &&
+         (tt < kBig);
+}
+
+// Shadow-table view (shared memory). Counts are CTA-uniform.
+struct Obst {
+  const float* cyl;
+  const float* box;
+  const float* sph;
+  const float* obox;
+  const float* tri;
+  int n_cyl, n_box, n_sph, n_obox, n_tri;
+};
+
+// core/render.py:21-41 _check_occlusions, for one ray: true = shadowed.
+__device__ __forceinline__ bool occluded(const Obst& ob, V3 o, V3 d) {
+  bool s = false;
+#pragma unroll 1
+  for (int i = 0; i < ob.n_cyl; ++i) s |= cyl_shadows(ob.cyl + i * kCylF, o, d);
+#pragma unroll 1
+  for (int i = 0; i < ob.n_box; ++i) s |= box_shadows(ob.box + i * kBoxF, o, d);
+#pragma unroll 1
+  for (int i = 0; i < ob.n_sph; ++i) s |= sph_shadows(ob.sph + i * kSphF, o, d);
+#pragma unroll 1
+  for (int i = 0; i < ob.n_obox; ++i) s |= obox_shadows(ob.obox + i * kOboxF, o, d);
+#pragma unroll 1
+  for (int i = 0; i < ob.n_tri; ++i) s |= tri_shadows(ob.tri + i * kTriF, o, d);
+  return s;
+}
+
+// ----------------------------------------------------------------- sensor
+struct SensorK {
+  int type, n_pixels, width, height;
+  float R[9];
+  float pos[3];
+  float x0, y0, dx, dy, edge_width;
+  float hex_size, inradius, gc, gs, off_x, off_y, hex_sx, hex_sy, edge_threshold;
+  int q_min, r_min, table_q, table_r;
+  float sigma;
+  int kernel_size;
+};
+
+// core/intersections.py:6-41 intersect_plane -> local (x, y) or (1e10, 1e10)
+__device__ __forceinline__ void plane_hit(const SensorK& s, V3 o, V3 d, float& x, float& y) {
+  V3 u1 = mk(s.R[0], s.R[3], s.R[6]), u2 = mk(s.R[1], s.R[4], s.R[7]), n = mk(s.R[2], s.R[5], s.R[8]);
+  V3 c = mk(s.pos[0], s.pos[1], s.pos[2]);
+  float ndotd = dot(d, n), ndoto = dot(o, n), ndotp = dot(n, c);
+  bool parallel = fabsf(ndotd) < 1e-10f;
+  float t = __fdiv_rn(ndotp - ndoto, parallel ? 1.f : ndotd);
+  V3 op = (o + t * d) - c;
+  bool invalid = parallel || (t <= 0.f);
+  x = invalid ? kBig : dot(op, u1);
+  y = invalid ? kBig : dot(op, u2);
+}
+
+// sensors/square.py:66-91 SquareSensor.accumulate: pixel id or -1
+__device__ __forceinline__ int bin_square(const SensorK& s, float x, float y) {
+  float xc = __fdiv_rn(x - s.x0, s.dx), yc = __fdiv_rn(y - s.y0, s.dy);
+  float xf = floorf(xc), yf = floorf(yc);
+  // compare in float: out-of-range and NaN fail, as the int32 cast would
+  bool valid = (xf >= 0.f) && (xf < (float)s.width) && (yf >= 0.f) && (yf < (float)s.height);
+  float fx = xc - xf, fy = yc - yf;
+  float dist = fminf(fminf(fx, 1.f - fx) * s.dx, fminf(fy, 1.f - fy) * s.dy);
+  valid = valid && !(dist < s.edge_width);
+  return valid ? (int)yf * s.width + (int)xf : -1;
+}
+
+// sensors/hexagonal.py:16-23 _rotate and :26-29 _cartesian_to_axial, :32-39 _axial_round
+__device__ __forceinline__ void hex_axial(const SensorK& s, float x, float y, float& xg, float& yg,
+                                          float& qi, float& ri) {
+  const float SQRT3_3 = 0.5773502691896257f;
+  float xs = x - s.off_x, ys = y - s.off_y;
+  xg = s.gc * xs - s.gs * ys;
+  yg = s.gs * xs + s.gc * ys;
+  float q = __fdiv_rn(SQRT3_3 * xg - __fdiv_rn(yg, 3.f), s.hex_size);
+  float r = __fdiv_rn(__fdiv_rn(2.f * yg, 3.f), s.hex_size);
+  float sv = -q - r;
+  qi = rintf(q);
+  ri = rintf(r);
+  float si = rintf(sv);
+  float dq = fabsf(qi - q), dr = fabsf(ri - r), ds = fabsf(si - sv);
+  if ((dq > dr) && (dq > ds)) qi = -ri - si;
+  if ((dr > dq) && (dr > ds)) ri = -qi - si;
+}
+
+// sensors/hexagonal.py:155-172 _lookup_pixels over a table in shared memory
+__device__ __forceinline__ int hex_lookup(const SensorK& s, const int* table, float qi, float ri) {
+  float qx = qi - (float)s.q_min, rx = ri - (float)s.r_min;
+  if (!((qx >= 0.f) && (qx < (float)s.table_q) && (rx >= 0.f) && (rx < (float)s.table_r))) return -1;
+  int p = table[(int)qx * s.table_r + (int)rx];
+  return p >= 0 ? p : -1;
+}
+
+// sensors/hexagonal.py:42-47 _hex_norm
+__device__ __forceinline__ float hex_norm(float x, float y, float inr) {
+  float ax = fabsf(x), ay = fabsf(y);
+  return __fdiv_rn(fmaxf(ax, 0.5f * ax + 0.8660254037844386f * ay), inr);
+}
+
+// sensors/hexagonal.py:174-194 HexagonalSensor.accumulate: pixel id or -1
+__device__ __forceinline__ int bin_hex(const SensorK& s, const int* table, float x, float y) {
+  float xg, yg, qi, ri;
+  hex_axial(s, x, y, xg, yg, qi, ri);
+  int p = hex_lookup(s, table, qi, ri);
+  float hcx = s.hex_sx * (qi + 0.5f * ri);
+  float hcy = s.hex_sy * ri;
+  float hd = hex_norm(xg - hcx, yg - hcy, s.inradius);
+  return (hd > s.edge_threshold) ? -1 : p;
+}
+
+// ------------------------------------------------------- stage >= 1 mirrors
+// core/surfaces.py:25-39 _sag_raw and its r2-derivative, in FP64: the sag
+// root is the one place where the float32 chain cancels (ray origins several
+// metres from the surface against a 1e-6 residual tolerance).
+__device__ __forceinline__ double sag_raw_d(const float* m, double r2) {
+  double c = m[15], alpha = (1.0 + (double)m[23]) * c * c;
+  double den = 1.0 + sqrt(1.0 - alpha * r2);
+  double z = r2 * c / den;
+  int na = (int)m[19];
+  if (na > 0) {
+    double r4 = r2 * r2, p = r4, sacc = 0.0;
+    for (int i = 0; i < na; ++i) {  // a_i * r2^(2(i+1))
+      sacc += (double)m[24 + i] * p;
+      p *= r4;
+    }
+    z += sacc;
+  }
+  return z;
+}
+__device__ __forceinline__ double sag_raw_dr2_d(const float* m, double r2) {
+  double c = m[15], alpha = (1.0 + (double)m[23]) * c * c;
+  double s = sqrt(1.0 - alpha * r2);
+  double den = 1.0 + s;
+  double dz = c / den + (r2 * c) * alpha / (2.0 * s * den * den);
+  int na = (int)m[19];
+  if (na > 0) {
+    double r4 = r2 * r2, pm1 = r2, sacc = 0.0;  // p*r2^(p-1), p = 2(i+1)
+    for (int i = 0; i < na; ++i) {
+      sacc += (double)m[24 + i] * (double)(2 * (i + 1)) * pm1;
+      pm1 *= r4;
+    }
+    dz += sacc;
+  }
+  return dz;
+}
+
+// core/intersections.py:229-285 intersect_conic (on the raw-frame origin)
+__device__ __forceinline__ double conic_t(const float* m, double ox, double oy, double oz, double dx,
+                                          double dy, double dz) {
+  double c = m[15], kp = 1.0 + (double)m[23];
+  double A = c * (dx * dx + dy * dy + kp * dz * dz);
+  double B = 2.0 * (c * (ox * dx + oy * dy + kp * oz * dz) - dz);
+  double C = c * (ox * ox + oy * oy + kp * oz * oz) - 2.0 * oz;
+  const double inf = __longlong_as_double(0x7ff0000000000000ll);
+  if (fabs(c) < 1e-12) return (fabs(dz) > 1e-10) ? -oz / dz : inf;
+  double disc = B * B - 4.0 * A * C;
+  if (disc < 0.0) return inf;
+  double sq = sqrt(disc);
+  double t1 = (-B - sq) / (2.0 * A + 1e-30), t2 = (-B + sq) / (2.0 * A + 1e-30);
+  bool v1 = t1 > 1e-8, v2 = t2 > 1e-8;
+  return (v1 && v2) ? fmin(t1, t2) : (v1 ? t1 : (v2 ? t2 : inf));
+}
+
+// core/surfaces.py:67-108 AsphericSurface.intersect + core/intersections.py:290-367
+// newton_raphson_intersect (10 steps, tol 1e-8, valid if t > 1e-8 and
+// |g| < 1e-6). Local frame in, local point and unit normal out; returns t or
+// +inf when invalid or outside the aperture (core/render.py:100-101).
+__device__ __forceinline__ float mirror_hit(const float* m, V3 o, V3 d, V3& pl, V3& nl) {
+  const float inf = __int_as_float(0x7f800000);
+  double x0 = m[12], y0 = m[13];
+  double z0 = sag_raw_d(m, x0 * x0 + y0 * y0);
+  double ox = o.x, oy = o.y, oz = o.z, dx = d.x, dy = d.y, dz = d.z;
+  double t = conic_t(m, ox + x0, oy + y0, oz + z0, dx, dy, dz);
+  bool conv = false;
+  for (int it = 0; it < 10; ++it) {
+    if (!conv) {
+      double xs = ox + t * dx + x0, ys = oy + t * dy + y0;
+      double r2 = xs * xs + ys * ys;
+      double g = (oz + t * dz) - (sag_raw_d(m, r2) - z0);
+      double gd = sag_raw_dr2_d(m, r2);
+      double gp = dz - (gd * (2.0 * xs) * dx + gd * (2.0 * ys) * dy);
+      double gs = (fabs(gp) > 1e-12) ? gp : 1e-12;
+      conv = fabs(g) < 1e-8;
+      t = t - g / gs;
+    }
+  }
+  double xh = ox + t * dx, yh = oy + t * dy;
+  double xs = xh + x0, ys = yh + y0;
+  double r2 = xs * xs + ys * ys;
+  double zs = sag_raw_d(m, r2) - z0;
+  double res = fabs((oz + t * dz) - zs);
+  bool valid = (t > 1e-8) && (res < 1e-6);
+  double gd = sag_raw_dr2_d(m, r2);
+  double nx = -(gd * 2.0 * xs), ny = -(gd * 2.0 * ys);
+  double nn = sqrt(nx * nx + ny * ny + 1.0);
+  pl = mk((float)xh, (float)yh, (float)zs);
+  nl = mk((float)(nx / nn), (float)(ny / nn), (float)(1.0 / nn));
+  // telescope/mirrors.py:147-149 disk, :209-220 polygon check_aperture
+  bool in_ap;
+  if ((int)m[20] == IACT_APERTURE_DISK) {
+    in_ap = pl.x * pl.x + pl.y * pl.y <= m[18];
+  } else {
+    in_ap = true;
+    int n = (int)m[21];
+    for (int i = 0; i < n; ++i) {
+      int j = (i + 1 == n) ? 0 : i + 1;
+      float ax = m[32 + 2 * i], ay = m[33 + 2 * i], bx = m[32 + 2 * j], by = m[33 + 2 * j];
+      float cr = (bx - ax) * (pl.y - ay) - (by - ay) * (pl.x - ax);
+      in_ap = in_ap && (cr >= 0.f);
+    }
+  }
+  return (valid && in_ap) ? (float)t : inf;
+}
+
+}  // namespace iact

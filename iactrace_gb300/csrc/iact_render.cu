@@ -1,0 +1,706 @@
+// Forward render kernels of the GB300 render path.
+//
+//   k_prep    : telescope/mirrors.py:64-79 transform_to_world for every
+//               (facet, sample) once per call, into float4 world samples,
+//               plus the per-launch constant tables (obstruction records,
+//               stage-mirror records) the render kernel stages in shared
+//               memory.
+//   k_render  : core/render.py:118-171 for every ray (source, facet, sample):
+//               one lane owns one ray through the fused chain (direction,
+//               shadow, reflect, later stages, sensor plane, pixel bin).
+//               Persistent CTAs pull (source block, facet chunk, sample
+//               chunk) tiles from an atomic queue. Pixel hits are run-length
+//               merged per lane in registers, then added into shared-memory
+//               histogram rows (one row for an image, one row per source of
+//               the block for a response matrix) that are flushed to global
+//               memory with one atomic per non-zero bin.
+//   k_debug   : core/render.py:223-268 render_debug, one thread per ray.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+
+#include "iact_device.cuh"
+#include "iact_internal.h"
+
+namespace iact {
+
+// Offsets (floats) of the record groups inside the table region.
+struct TableOffsets {
+  int cyl, box, sph, obox, tri, mir, total;
+};
+__host__ __device__ inline TableOffsets table_offsets(int n_cyl, int n_box, int n_sph, int n_obox,
+                                                      int n_tri, int n_mir) {
+  TableOffsets t;
+  t.cyl = 0;
+  t.box = t.cyl + n_cyl * kCylF;
+  t.sph = t.box + n_box * kBoxF;
+  t.obox = t.sph + n_sph * kSphF;
+  t.tri = t.obox + n_obox * kOboxF;
+  t.mir = (t.tri + n_tri * kTriF + 3) & ~3;
+  t.total = t.mir + n_mir * kMirF;
+  return t;
+}
+
+struct PrepK {
+  int F, M;
+  const float* facet_pos;
+  const float* facet_rot;
+  const float* facet_scale;
+  const float* points;
+  const float* normals;
+  const float* delta;
+  const float* weights;
+  float4* P4;
+  float4* N4;
+  float* tables;
+  const float* cyl;
+  const float* box;
+  const float* sph;
+  const float* obox;
+  const float* tri;
+  const iact_mirror_t* mirrors;
+  int n_cyl, n_box, n_sph, n_obox, n_tri, n_mir;
+};
+
+__global__ void __launch_bounds__(256) k_prep(const PrepK p) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (blockIdx.x == 0) {
+    TableOffsets to = table_offsets(p.n_cyl, p.n_box, p.n_sph, p.n_obox, p.n_tri, p.n_mir);
+    for (int k = threadIdx.x; k < p.n_cyl; k += blockDim.x) {
+      const float* c = p.cyl + 7 * k;
+      float* o = p.tables + to.cyl + kCylF * k;
+      // core/intersections.py:46-48 axis, height
+      float ax = c[3] - c[0], ay = c[4] - c[1], az = c[5] - c[2];
+      float h = sqrtf(ax * ax + ay * ay + az * az);
+      o[0] = c[0]; o[1] = c[1]; o[2] = c[2];
+      o[3] = ax / h; o[4] = ay / h; o[5] = az / h;
+      o[6] = h;
+      o[7] = c[6] * c[6];
+    }
+    for (int k = threadIdx.x; k < p.n_box; k += blockDim.x) {
+      const float* b = p.box + 6 * k;
+      float* o = p.tables + to.box + kBoxF * k;
+      for (int a = 0; a < 3; ++a) {  // core/intersections.py:94-95
+        o[a] = fminf(b[a], b[3 + a]);
+        o[3 + a] = fmaxf(b[a], b[3 + a]);
+      }
+    }
+    for (int k = threadIdx.x; k < p.n_sph; k += blockDim.x) {
+      const float* s = p.sph + 4 * k;
+      float* o = p.tables + to.sph + kSphF * k;
+      o[0] = s[0]; o[1] = s[1]; o[2] = s[2];
+      o[3] = s[3] * s[3];
+    }
+    for (int k = threadIdx.x; k < p.n_obox * kOboxF; k += blockDim.x) p.tables[to.obox + k] = p.obox[k];
+    for (int k = threadIdx.x; k < p.n_tri; k += blockDim.x) {
+      const float* t = p.tri + 9 * k;
+      float* o = p.tables + to.tri + kTriF * k;
+      o[0] = t[0]; o[1] = t[1]; o[2] = t[2];
+      for (int a = 0; a < 3; ++a) {  // core/intersections.py:166-167 edges
+        o[3 + a] = t[3 + a] - t[a];
+        o[6 + a] = t[6 + a] - t[a];
+      }
+    }
+    for (int k = threadIdx.x; k < p.n_mir; k += blockDim.x) {
+      const iact_mirror_t& m = p.mirrors[k];
+      float* o = p.tables + to.mir + kMirF * k;
+      euler_to_matrix(m.rot[0], m.rot[1], m.rot[2], o);
+      o[9] = m.pos[0]; o[10] = m.pos[1]; o[11] = m.pos[2];
+      o[12] = m.offset[0]; o[13] = m.offset[1];
+      o[14] = 0.f;
+      o[15] = m.curvature;
+      o[16] = 1.f + m.conic;
+      o[17] = (1.f + m.conic) * m.curvature * m.curvature;
+      o[18] = m.radius * m.radius;
+      o[19] = (float)m.n_asph;
+      o[20] = (float)m.aperture;
+      o[21] = (float)m.n_vert;
+      o[22] = (float)m.stage;
+      o[23] = m.conic;
+      for (int a = 0; a < 8; ++a) o[24 + a] = a < m.n_asph ? m.asph[a] : 0.f;
+      for (int a = 0; a < 8; ++a) {
+        o[32 + 2 * a] = a < m.n_vert ? m.vert[a][0] : 0.f;
+        o[33 + 2 * a] = a < m.n_vert ? m.vert[a][1] : 0.f;
+      }
+    }
+  }
+  const long long n = (long long)p.F * p.M;
+  if (i >= n) return;
+  const int f = (int)(i / p.M);
+  float R[9];
+  euler_to_matrix(p.facet_rot[3 * f], p.facet_rot[3 * f + 1], p.facet_rot[3 * f + 2], R);
+  V3 pl = mk(p.points[3 * i], p.points[3 * i + 1], p.points[3 * i + 2]);
+  V3 nl = mk(p.normals[3 * i], p.normals[3 * i + 1], p.normals[3 * i + 2]);
+  V3 dl = mk(p.delta[3 * i], p.delta[3 * i + 1], p.delta[3 * i + 2]);
+  V3 pw = rmul(R, pl) + mk(p.facet_pos[3 * f], p.facet_pos[3 * f + 1], p.facet_pos[3 * f + 2]);
+  V3 nw = rmul(R, nl), dw = rmul(R, dl);
+  float sc = p.facet_scale[f];
+  V3 pe = nw + sc * dw;  // perturbed = normals_world + scale * delta_world
+  float nn = sqrtf(dot(pe, pe));
+  p.P4[i] = make_float4(pw.x, pw.y, pw.z, 1.f / p.weights[i]);
+  p.N4[i] = make_float4(pe.x / nn, pe.y / nn, pe.z / nn, 0.f);
+}
+
+struct RenderK {
+  int F, M, S, P;
+  const float4* P4;
+  const float4* N4;
+  const float* sources;
+  const float* values;
+  const float* tables;
+  int n_table_floats;
+  int n_cyl, n_box, n_sph, n_obox, n_tri, n_mir;
+  const int* hex_table;
+  int hex_in_smem;
+  SensorK sn;
+  float* out;
+  int rows_in_smem;  // histogram rows held in shared memory, 0 = add to `out` directly
+  int SB, FC, CC;    // tile: sources, facets, 32-sample chunks
+  int n_fchunk, n_cchunk, n_tiles;
+  int* counter;
+};
+
+// all 32 lanes call; key < 0 or v == 0 means nothing to add for this lane
+__device__ __forceinline__ void warp_add(float* hist, int key, float v) {
+  const int k0 = __shfl_sync(kFull, key, 0);
+  if (__all_sync(kFull, key == k0)) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+    if ((threadIdx.x & 31) == 0 && k0 >= 0 && v != 0.f) atomicAdd(hist + k0, v);
+  } else if (key >= 0 && v != 0.f) {
+    atomicAdd(hist + key, v);
+  }
+}
+
+// sensors/square.py:144-172 DifferentiableSquareSensor.accumulate, one ray
+// (all lanes call; inactive lanes pass ok = false). Rays whose plane hit is
+// the 1e10 sentinel deposit nothing.
+__device__ __forceinline__ void splat_square(const SensorK& s, float* hist, int rowbase, bool ok,
+                                             float x, float y, float v) {
+  ok = ok && (x < 1e9f) && (y < 1e9f);
+  float xp = __fdiv_rn(x - s.x0, s.dx), yp = __fdiv_rn(y - s.y0, s.dy);
+  float xb = floorf(xp), yb = floorf(yp);
+  float xf = xp - xb, yf = yp - yb;
+  const int K = s.kernel_size, n = 2 * K + 1;
+  const float inv2s = __fdiv_rn(-0.5f, s.sigma * s.sigma);
+  float tot = 0.f;
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) {
+      float ddx = xf - (float)(j - K), ddy = yf - (float)(i - K);
+      tot += expf(inv2s * (ddx * ddx + ddy * ddy));
+    }
+  const float scale = ok ? v / tot : 0.f;
+  const int xi0 = ok ? (int)xb : 0, yi0 = ok ? (int)yb : 0;
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) {
+      float ddx = xf - (float)(j - K), ddy = yf - (float)(i - K);
+      float w = expf(inv2s * (ddx * ddx + ddy * ddy)) * scale;
+      int xi = xi0 + j - K, yi = yi0 + i - K;
+      bool in = ok && xi >= 0 && xi < s.width && yi >= 0 && yi < s.height;
+      warp_add(hist, in ? rowbase + yi * s.width + xi : -1, w);
+    }
+}
+
+// sensors/hexagonal.py:264-315 DifferentiableHexagonalSensor.accumulate
+__device__ __forceinline__ void splat_hex(const SensorK& s, const int* table, float* hist,
+                                          int rowbase, bool ok, float x, float y, float v) {
+  ok = ok && (x < 1e9f) && (y < 1e9f);
+  float xg, yg, qi, ri;
+  hex_axial(s, ok ? x : 0.f, ok ? y : 0.f, xg, yg, qi, ri);
+  float ddx = xg - s.hex_sx * (qi + 0.5f * ri), ddy = yg - s.hex_sy * ri;
+  const int K = s.kernel_size;
+  float tot = 0.f;
+  for (int q = -K; q <= K; ++q)
+    for (int r = -K; r <= K; ++r) {
+      if (max(max(abs(q), abs(r)), abs(q + r)) > K) continue;
+      float a = __fdiv_rn(hex_norm(ddx - s.hex_sx * ((float)q + 0.5f * (float)r), ddy - s.hex_sy * (float)r,
+                                   s.inradius),
+                          s.sigma);
+      tot += expf(-0.5f * (a * a));
+    }
+  const float scale = ok ? v / tot : 0.f;
+  for (int q = -K; q <= K; ++q)
+    for (int r = -K; r <= K; ++r) {
+      if (max(max(abs(q), abs(r)), abs(q + r)) > K) continue;
+      float a = __fdiv_rn(hex_norm(ddx - s.hex_sx * ((float)q + 0.5f * (float)r), ddy - s.hex_sy * (float)r,
+                                   s.inradius),
+                          s.sigma);
+      float w = expf(-0.5f * (a * a)) * scale;
+      int p = ok ? hex_lookup(s, table, qi + (float)q, ri + (float)r) : -1;
+      warp_add(hist, p >= 0 ? rowbase + p : -1, w);
+    }
+}
+
+// core/render.py:118-157 for one ray; returns sensor-plane (x, y), value and
+// the index of the last stage mirror hit (-1 if none).
+template <int SRC, bool STAGES>
+__device__ __forceinline__ void trace_ray(const RenderK& p, const Obst& ob, const float* mir, float4 P,
+                                          float4 N, V3 src, float v, float& x, float& y, float& val,
+                                          int& hit_mirror) {
+  V3 tp = mk(P.x, P.y, P.z), tn = mk(N.x, N.y, N.z);
+  V3 d;
+  if (SRC == IACT_SRC_POINT) {
+    V3 dd = tp - src;  // dirs = normalize(tp - src)
+    d = rsqrtf(dot(dd, dd)) * dd;
+  } else {
+    d = src;  // parallel: the source entry is the direction, as given
+  }
+  const bool sh = occluded(ob, tp, mk(-d.x, -d.y, -d.z));
+  const float c = dot(d, tn);  // core/reflection.py:5-20
+  V3 r = d - (2.f * c) * tn;
+  val = (v * -c * P.w) * (sh ? 0.f : 1.f);  // values * cos / tw * shadow
+  V3 o = tp;
+  hit_mirror = -1;
+  if (STAGES) {
+    // core/render.py:44-79 _reflect_at_stage, one pass per stage
+    int mi = 0;
+    while (mi < p.n_mir) {
+      const int stg = (int)mir[mi * kMirF + 22];
+      float best_t = __int_as_float(0x7f800000);
+      V3 bp = mk(0.f, 0.f, 0.f), bn = mk(0.f, 0.f, 0.f);
+      int bi = -1;
+      int mj = mi;
+      for (; mj < p.n_mir && (int)mir[mj * kMirF + 22] == stg; ++mj) {
+        const float* m = mir + mj * kMirF;
+        V3 pos = mk(m[9], m[10], m[11]);
+        V3 pl, nl;
+        float t = mirror_hit(m, rtmul(m, o - pos), rtmul(m, r), pl, nl);
+        if (t < best_t) {  // closest hit, first index on ties (argmin)
+          best_t = t;
+          bp = rmul(m, pl) + pos;
+          bn = rmul(m, nl);
+          bi = mj;
+        }
+      }
+      const float c2 = dot(r, bn);
+      V3 rr = r - (2.f * c2) * bn;
+      const bool sh2 = occluded(ob, o, r);
+      val = val * (best_t < kBig ? 1.f : 0.f) * (sh2 ? 0.f : 1.f) * fabsf(c2);
+      o = bp;
+      r = rr;
+      hit_mirror = bi;
+      mi = mj;
+    }
+  }
+  plane_hit(p.sn, o, r, x, y);
+}
+
+template <int SRC, bool SOFT, int MODE, bool STAGES>
+__global__ void __launch_bounds__(256) k_render(const RenderK p) {
+  extern __shared__ __align__(16) float smem[];
+  __shared__ int s_tile;
+  const int tab_n = (p.n_table_floats + 3) & ~3;
+  const int htab_n = p.hex_in_smem ? ((p.sn.table_q * p.sn.table_r + 3) & ~3) : 0;
+  float* tab = smem;
+  int* htab = reinterpret_cast<int*>(smem + tab_n);
+  float* sh_hist = smem + tab_n + htab_n;
+  const int hist_n = p.rows_in_smem * p.P;
+  const int nthr = blockDim.x;
+
+  for (int i = threadIdx.x; i < p.n_table_floats; i += nthr) tab[i] = p.tables[i];
+  for (int i = threadIdx.x; i < htab_n; i += nthr)
+    htab[i] = i < p.sn.table_q * p.sn.table_r ? p.hex_table[i] : -1;
+  for (int i = threadIdx.x; i < hist_n; i += nthr) sh_hist[i] = 0.f;
+
+  const TableOffsets to = table_offsets(p.n_cyl, p.n_box, p.n_sph, p.n_obox, p.n_tri, p.n_mir);
+  Obst ob;
+  ob.cyl = tab + to.cyl; ob.box = tab + to.box; ob.sph = tab + to.sph;
+  ob.obox = tab + to.obox; ob.tri = tab + to.tri;
+  ob.n_cyl = p.n_cyl; ob.n_box = p.n_box; ob.n_sph = p.n_sph; ob.n_obox = p.n_obox; ob.n_tri = p.n_tri;
+  const float* mir = tab + to.mir;
+  const int* table = p.hex_in_smem ? htab : p.hex_table;
+  float* hist = p.rows_in_smem ? sh_hist : p.out;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = nthr >> 5;
+  const int nch = (p.M + 31) >> 5;
+  int cur_sblk = -1;
+  int rl_key = -1;  // run-length merged hit of this lane (hard sensors)
+  float rl_val = 0.f;
+
+  __syncthreads();
+  for (;;) {
+    if (threadIdx.x == 0) s_tile = atomicAdd(p.counter, 1);
+    __syncthreads();
+    const int tile = s_tile;
+    if (tile >= p.n_tiles) break;
+    const int per_s = p.n_fchunk * p.n_cchunk;
+    const int sblk = tile / per_s;
+    const int fc = (tile - sblk * per_s) / p.n_cchunk;
+    const int cc = tile - sblk * per_s - fc * p.n_cchunk;
+    const int s0 = sblk * p.SB, f0 = fc * p.FC, c0 = cc * p.CC;
+    const int SBc = min(p.SB, p.S - s0), FCc = min(p.FC, p.F - f0), CCc = min(p.CC, nch - c0);
+
+    if (MODE == IACT_MODE_RESPONSE && p.rows_in_smem && sblk != cur_sblk) {
+      // rows of the previous source block -> global, then clear
+      if (cur_sblk >= 0) {
+        const int cs0 = cur_sblk * p.SB, csb = min(p.SB, p.S - cs0);
+        for (int i = threadIdx.x; i < csb * p.P; i += nthr) {
+          float h = sh_hist[i];
+          if (h != 0.f) {
+            atomicAdd(p.out + (size_t)cs0 * p.P + i, h);
+            sh_hist[i] = 0.f;
+          }
+        }
+      }
+      cur_sblk = sblk;
+      __syncthreads();
+    }
+
+    const int T = SBc * FCc * CCc;
+    const int tb = (warp * T) / nw, te = ((warp + 1) * T) / nw;
+    for (int t = tb; t < te; ++t) {
+      const int sl = t / (FCc * CCc);
+      const int rem = t - sl * FCc * CCc;
+      const int fl = rem / CCc;
+      const int m = (c0 + rem - fl * CCc) * 32 + lane;
+      const int s = s0 + sl, f = f0 + fl;
+      const bool act = m < p.M;
+      const V3 src = mk(__ldg(p.sources + 3 * s), __ldg(p.sources + 3 * s + 1), __ldg(p.sources + 3 * s + 2));
+      const float v = __ldg(p.values + s);
+      float x = 0.f, y = 0.f, val = 0.f;
+      int hm;
+      if (act) {
+        const size_t si = (size_t)f * p.M + m;
+        trace_ray<SRC, STAGES>(p, ob, mir, __ldg(p.P4 + si), __ldg(p.N4 + si), src, v, x, y, val, hm);
+      }
+      int rowbase;
+      if (MODE == IACT_MODE_RESPONSE) rowbase = (p.rows_in_smem ? sl : s) * p.P;
+      else rowbase = 0;
+      if (SOFT) {
+        if (p.sn.type == IACT_SENSOR_SOFT_SQUARE) splat_square(p.sn, hist, rowbase, act, x, y, val);
+        else splat_hex(p.sn, table, hist, rowbase, act, x, y, val);
+      } else if (act) {
+        const int pix = (p.sn.type == IACT_SENSOR_SQUARE) ? bin_square(p.sn, x, y) : bin_hex(p.sn, table, x, y);
+        if (pix >= 0 && val != 0.f) {
+          const int key = rowbase + pix;
+          if (key == rl_key) {
+            rl_val += val;
+          } else {
+            if (rl_key >= 0) atomicAdd(hist + rl_key, rl_val);
+            rl_key = key;
+            rl_val = val;
+          }
+        }
+      }
+    }
+    if (!SOFT && rl_key >= 0) {
+      atomicAdd(hist + rl_key, rl_val);
+      rl_key = -1;
+      rl_val = 0.f;
+    }
+    __syncthreads();
+  }
+  // final flush of the shared rows
+  if (p.rows_in_smem) {
+    int base = 0, nrows = 1;
+    if (MODE == IACT_MODE_RESPONSE) {
+      if (cur_sblk < 0) return;
+      base = cur_sblk * p.SB;
+      nrows = min(p.SB, p.S - base);
+    }
+    for (int i = threadIdx.x; i < nrows * p.P; i += nthr) {
+      float h = sh_hist[i];
+      if (h != 0.f) atomicAdd(p.out + (size_t)base * p.P + i, h);
+    }
+  }
+}
+
+template <int SRC, bool STAGES>
+__global__ void __launch_bounds__(256) k_debug(const RenderK p, float* pts, float* vals, int32_t* pix,
+                                               int32_t* hit_mirror) {
+  extern __shared__ __align__(16) float smem[];
+  const int tab_n = (p.n_table_floats + 3) & ~3;
+  for (int i = threadIdx.x; i < p.n_table_floats; i += blockDim.x) smem[i] = p.tables[i];
+  (void)tab_n;
+  __syncthreads();
+  const TableOffsets to = table_offsets(p.n_cyl, p.n_box, p.n_sph, p.n_obox, p.n_tri, p.n_mir);
+  Obst ob;
+  ob.cyl = smem + to.cyl; ob.box = smem + to.box; ob.sph = smem + to.sph;
+  ob.obox = smem + to.obox; ob.tri = smem + to.tri;
+  ob.n_cyl = p.n_cyl; ob.n_box = p.n_box; ob.n_sph = p.n_sph; ob.n_obox = p.n_obox; ob.n_tri = p.n_tri;
+  const float* mir = smem + to.mir;
+  const long long n = (long long)p.F * p.S * p.M;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int m = (int)(i % p.M);
+    const long long fs = i / p.M;
+    const int s = (int)(fs % p.S), f = (int)(fs / p.S);
+    const size_t si = (size_t)f * p.M + m;
+    float x, y, val;
+    int hm;
+    trace_ray<SRC, STAGES>(p, ob, mir, p.P4[si], p.N4[si], mk(p.sources[3 * s], p.sources[3 * s + 1], p.sources[3 * s + 2]),
+                           p.values[s], x, y, val, hm);
+    pts[2 * i] = x;
+    pts[2 * i + 1] = y;
+    vals[i] = val;
+    if (pix) {
+      int q;
+      if (p.sn.type == IACT_SENSOR_SQUARE || p.sn.type == IACT_SENSOR_SOFT_SQUARE) q = bin_square(p.sn, x, y);
+      else q = bin_hex(p.sn, p.hex_table, x, y);
+      pix[i] = q;
+    }
+    if (hit_mirror) hit_mirror[i] = hm;
+  }
+}
+
+// ------------------------------------------------------------------ host side
+
+namespace {
+
+inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+struct DevInfo {
+  int sm_count = 0;
+  int smem_optin = 0;
+};
+
+DevInfo device_info() {
+  static std::mutex mu;
+  static DevInfo cache[64];
+  static bool have[64] = {false};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> g(mu);
+  if (dev < 0 || dev >= 64) dev = 0;
+  if (!have[dev]) {
+    cudaDeviceGetAttribute(&cache[dev].sm_count, cudaDevAttrMultiProcessorCount, dev);
+    cudaDeviceGetAttribute(&cache[dev].smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    have[dev] = true;
+  }
+  return cache[dev];
+}
+
+void host_euler(const float* deg, float* R) {
+  const double k = M_PI / 180.0;
+  double cx = cos(deg[0] * k), sx = sin(deg[0] * k);
+  double cy = cos(deg[1] * k), sy = sin(deg[1] * k);
+  double cz = cos(deg[2] * k), sz = sin(deg[2] * k);
+  double a00 = cz * cy, a01 = -sz, a02 = cz * sy, a10 = sz * cy, a11 = cz, a12 = sz * sy, a20 = -sy, a21 = 0,
+         a22 = cy;
+  double r[9] = {a00, a01 * cx + a02 * sx, a02 * cx - a01 * sx, a10, a11 * cx + a12 * sx, a12 * cx - a11 * sx,
+                 a20, a21 * cx + a22 * sx, a22 * cx - a21 * sx};
+  for (int i = 0; i < 9; ++i) R[i] = (float)r[i];
+}
+
+SensorK make_sensor(const iact_sensor_t* s) {
+  SensorK k;
+  memset(&k, 0, sizeof(k));
+  k.type = s->type;
+  k.n_pixels = s->n_pixels;
+  k.width = s->width;
+  k.height = s->height;
+  host_euler(s->rot, k.R);
+  for (int i = 0; i < 3; ++i) k.pos[i] = s->pos[i];
+  k.x0 = s->x0; k.y0 = s->y0; k.dx = s->dx; k.dy = s->dy; k.edge_width = s->edge_width;
+  k.hex_size = s->hex_size; k.inradius = s->inradius; k.gc = s->grid_cos; k.gs = s->grid_sin;
+  k.off_x = s->off_x; k.off_y = s->off_y; k.hex_sx = s->hex_sx; k.hex_sy = s->hex_sy;
+  k.edge_threshold = s->edge_threshold;
+  k.q_min = s->q_min; k.r_min = s->r_min; k.table_q = s->table_q; k.table_r = s->table_r;
+  k.sigma = s->sigma;
+  k.kernel_size = s->kernel_size;
+  return k;
+}
+
+int launch_prep(const iact_scene_t* sc, const WsLayout& L, char* ws, cudaStream_t st) {
+  PrepK p;
+  p.F = sc->n_facets; p.M = sc->n_samples;
+  p.facet_pos = sc->facet_pos; p.facet_rot = sc->facet_rot; p.facet_scale = sc->facet_scale;
+  p.points = sc->points; p.normals = sc->normals; p.delta = sc->delta; p.weights = sc->weights;
+  p.P4 = reinterpret_cast<float4*>(ws + L.p4);
+  p.N4 = reinterpret_cast<float4*>(ws + L.n4);
+  p.tables = reinterpret_cast<float*>(ws + L.tables);
+  p.cyl = sc->cyl; p.box = sc->box; p.sph = sc->sph; p.obox = sc->obox; p.tri = sc->tri;
+  p.mirrors = sc->mirrors;
+  p.n_cyl = sc->n_cyl; p.n_box = sc->n_box; p.n_sph = sc->n_sph; p.n_obox = sc->n_obox; p.n_tri = sc->n_tri;
+  p.n_mir = sc->n_mirrors;
+  long long n = (long long)p.F * p.M;
+  int blocks = (int)std::max<long long>(1, (n + 255) / 256);
+  k_prep<<<blocks, 256, 0, st>>>(p);
+  return check_cuda(cudaGetLastError(), "k_prep launch");
+}
+
+RenderK base_params(const iact_scene_t* sc, const iact_sensor_t* sn, const WsLayout& L, char* ws,
+                    const float* sources, const float* values, int S) {
+  RenderK p;
+  memset(&p, 0, sizeof(p));
+  p.F = sc->n_facets; p.M = sc->n_samples; p.S = S; p.P = sn->n_pixels;
+  p.P4 = reinterpret_cast<const float4*>(ws + L.p4);
+  p.N4 = reinterpret_cast<const float4*>(ws + L.n4);
+  p.sources = sources; p.values = values;
+  p.tables = reinterpret_cast<const float*>(ws + L.tables);
+  p.n_table_floats = L.n_table_floats;
+  p.n_cyl = sc->n_cyl; p.n_box = sc->n_box; p.n_sph = sc->n_sph; p.n_obox = sc->n_obox; p.n_tri = sc->n_tri;
+  p.n_mir = sc->n_mirrors;
+  p.hex_table = sn->table;
+  p.sn = make_sensor(sn);
+  p.counter = reinterpret_cast<int*>(ws + L.counter);
+  return p;
+}
+
+template <int SRC, bool SOFT, int MODE, bool STAGES>
+int run_render(RenderK p, int block, size_t smem, cudaStream_t st, void* const* ev) {
+  auto kern = k_render<SRC, SOFT, MODE, STAGES>;
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return check_cuda(e, "cudaFuncSetAttribute(k_render smem)");
+  }
+  int per_sm = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, smem);
+  if (e != cudaSuccess) return check_cuda(e, "occupancy query");
+  if (per_sm < 1) return set_error(IACT_E_UNSUPPORTED, "render kernel does not fit on an SM with this configuration");
+  DevInfo di = device_info();
+  int grid = std::min(p.n_tiles, per_sm * di.sm_count);
+  grid = std::max(grid, 1);
+  if (ev && ev[0]) cudaEventRecord(static_cast<cudaEvent_t>(ev[0]), st);
+  kern<<<grid, block, smem, st>>>(p);
+  int rc = check_cuda(cudaGetLastError(), "k_render launch");
+  if (ev && ev[1]) cudaEventRecord(static_cast<cudaEvent_t>(ev[1]), st);
+  return rc;
+}
+
+template <int SRC, bool SOFT, int MODE>
+int dispatch_stages(bool stages, RenderK p, int block, size_t smem, cudaStream_t st, void* const* ev) {
+  return stages ? run_render<SRC, SOFT, MODE, true>(p, block, smem, st, ev)
+                : run_render<SRC, SOFT, MODE, false>(p, block, smem, st, ev);
+}
+template <int SRC, bool SOFT>
+int dispatch_mode(int mode, bool stages, RenderK p, int block, size_t smem, cudaStream_t st, void* const* ev) {
+  return mode == IACT_MODE_RESPONSE ? dispatch_stages<SRC, SOFT, IACT_MODE_RESPONSE>(stages, p, block, smem, st, ev)
+                                    : dispatch_stages<SRC, SOFT, IACT_MODE_IMAGE>(stages, p, block, smem, st, ev);
+}
+template <int SRC>
+int dispatch_soft(bool soft, int mode, bool stages, RenderK p, int block, size_t smem, cudaStream_t st,
+                  void* const* ev) {
+  return soft ? dispatch_mode<SRC, true>(mode, stages, p, block, smem, st, ev)
+              : dispatch_mode<SRC, false>(mode, stages, p, block, smem, st, ev);
+}
+
+}  // namespace
+
+WsLayout workspace_layout(const iact_scene_t* sc) {
+  WsLayout L;
+  TableOffsets to = table_offsets(sc->n_cyl, sc->n_box, sc->n_sph, sc->n_obox, sc->n_tri, sc->n_mirrors);
+  L.n_table_floats = to.total;
+  size_t off = 0;
+  L.counter = off;
+  off = align256(off + 64);
+  L.tables = off;
+  off = align256(off + sizeof(float) * (size_t)std::max(to.total, 1));
+  size_t n = (size_t)std::max(sc->n_facets, 0) * (size_t)std::max(sc->n_samples, 0);
+  L.p4 = off;
+  off = align256(off + sizeof(float4) * n);
+  L.n4 = off;
+  off = align256(off + sizeof(float4) * n);
+  L.total = off;
+  return L;
+}
+
+int launch_render(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type, const float* sources,
+                  const float* values, int S, int mode, float* out, void* ws, size_t ws_bytes,
+                  const iact_opts_t* opts, cudaStream_t st) {
+  const WsLayout L = workspace_layout(sc);
+  char* w = static_cast<char*>(ws);
+  const size_t P = (size_t)sn->n_pixels;
+  const size_t out_n = (mode == IACT_MODE_RESPONSE) ? (size_t)S * P : P;
+  int rc = check_cuda(cudaMemsetAsync(out, 0, out_n * sizeof(float), st), "zero output");
+  if (rc) return rc;
+  if (S == 0 || sc->n_facets == 0 || sc->n_samples == 0) return IACT_OK;
+  rc = check_cuda(cudaMemsetAsync(w + L.counter, 0, 64, st), "reset tile counter");
+  if (rc) return rc;
+  rc = launch_prep(sc, L, w, st);
+  if (rc) return rc;
+
+  RenderK p = base_params(sc, sn, L, w, sources, values, S);
+  p.out = out;
+  int block = (opts && opts->block_threads > 0) ? opts->block_threads : 256;
+  if (block % 32 || block > 256) return set_error(IACT_E_INVALID, "opts.block_threads must be a multiple of 32, <= 256");
+  const int nw = block / 32;
+  const int nch = (p.M + 31) / 32;
+  int SB = (opts && opts->sources_per_cta > 0) ? opts->sources_per_cta : std::min(S, nw);
+  SB = std::min(SB, S);
+  const int target = nw * 48;  // warp tasks (32 rays each) per tile
+  int CC = std::min(nch, std::max(1, target / SB));
+  int FC = (opts && opts->facets_per_tile > 0) ? opts->facets_per_tile : std::max(1, target / (SB * CC));
+  FC = std::min(FC, p.F);
+  p.SB = SB; p.FC = FC; p.CC = CC;
+  p.n_fchunk = (p.F + FC - 1) / FC;
+  p.n_cchunk = (nch + CC - 1) / CC;
+  const long long tiles = (long long)((S + SB - 1) / SB) * p.n_fchunk * p.n_cchunk;
+  if (tiles > 0x7fffffffLL) return set_error(IACT_E_UNSUPPORTED, "too many work tiles");
+  p.n_tiles = (int)tiles;
+
+  DevInfo di = device_info();
+  const size_t budget = (size_t)std::min(di.smem_optin > 0 ? di.smem_optin : 49152, 200 * 1024);
+  const size_t tab_bytes = sizeof(float) * (size_t)((L.n_table_floats + 3) & ~3);
+  const bool hex = (sn->type == IACT_SENSOR_HEX || sn->type == IACT_SENSOR_SOFT_HEX);
+  const size_t htab_elems = hex ? (size_t)sn->table_q * sn->table_r : 0;
+  size_t htab_bytes = sizeof(int) * ((htab_elems + 3) & ~(size_t)3);
+  p.hex_in_smem = (hex && tab_bytes + htab_bytes <= budget / 2) ? 1 : 0;
+  if (!p.hex_in_smem) htab_bytes = 0;
+  if (tab_bytes + htab_bytes > budget) return set_error(IACT_E_UNSUPPORTED, "scene tables exceed shared memory");
+  const int rows = (mode == IACT_MODE_RESPONSE) ? SB : 1;
+  const size_t hist_bytes = sizeof(float) * (size_t)rows * P;
+  const int hist_mode = opts ? opts->hist_mode : 0;
+  bool use_smem = (hist_mode != 2) && (tab_bytes + htab_bytes + hist_bytes <= budget);
+  if (hist_mode == 1 && !use_smem) return set_error(IACT_E_UNSUPPORTED, "histogram rows do not fit in shared memory");
+  p.rows_in_smem = use_smem ? rows : 0;
+  const size_t smem = tab_bytes + htab_bytes + (use_smem ? hist_bytes : 0);
+
+  const bool soft = (sn->type == IACT_SENSOR_SOFT_SQUARE || sn->type == IACT_SENSOR_SOFT_HEX);
+  const bool stages = sc->n_mirrors > 0;
+  void* const* ev = opts ? opts->kernel_events : nullptr;
+  return src_type == IACT_SRC_POINT ? dispatch_soft<IACT_SRC_POINT>(soft, mode, stages, p, block, smem, st, ev)
+                                    : dispatch_soft<IACT_SRC_PARALLEL>(soft, mode, stages, p, block, smem, st, ev);
+}
+
+int launch_debug(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type, const float* sources,
+                 const float* values, int S, float* pts, float* vals, int32_t* pix, int32_t* hit_mirror,
+                 void* ws, size_t ws_bytes, cudaStream_t st) {
+  (void)ws_bytes;
+  if (S == 0 || sc->n_facets == 0 || sc->n_samples == 0) return IACT_OK;
+  const WsLayout L = workspace_layout(sc);
+  char* w = static_cast<char*>(ws);
+  int rc = launch_prep(sc, L, w, st);
+  if (rc) return rc;
+  RenderK p = base_params(sc, sn, L, w, sources, values, S);
+  const size_t smem = sizeof(float) * (size_t)((L.n_table_floats + 3) & ~3);
+  const long long n = (long long)p.F * p.S * p.M;
+  const int block = 256;
+  const int grid = (int)std::min<long long>((n + block - 1) / block, 1 << 20);
+  const bool stages = sc->n_mirrors > 0;
+  if (smem > 48 * 1024) return set_error(IACT_E_UNSUPPORTED, "scene tables too large for the debug kernel");
+  if (src_type == IACT_SRC_POINT) {
+    if (stages) k_debug<IACT_SRC_POINT, true><<<grid, block, smem, st>>>(p, pts, vals, pix, hit_mirror);
+    else k_debug<IACT_SRC_POINT, false><<<grid, block, smem, st>>>(p, pts, vals, pix, hit_mirror);
+  } else {
+    if (stages) k_debug<IACT_SRC_PARALLEL, true><<<grid, block, smem, st>>>(p, pts, vals, pix, hit_mirror);
+    else k_debug<IACT_SRC_PARALLEL, false><<<grid, block, smem, st>>>(p, pts, vals, pix, hit_mirror);
+  }
+  return check_cuda(cudaGetLastError(), "k_debug launch");
+}
+
+__global__ void __launch_bounds__(256) k_probe_fma(float* out, int iters) {
+  // 8 independent FMA chains per thread keep the FP32 pipe saturated
+  float a[8];
+  const float m = 1.0000001f, c = 1e-7f;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) a[j] = threadIdx.x * 1e-3f + j;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) a[j] = fmaf(a[j], m, c);
+  }
+  float s = 0.f;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) s += a[j];
+  out[(size_t)blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+int launch_probe_fma(float* out, int blocks, int iters, cudaStream_t st) {
+  k_probe_fma<<<blocks, 256, 0, st>>>(out, iters);
+  return check_cuda(cudaGetLastError(), "k_probe_fma launch");
+}
+
+}  // namespace iact

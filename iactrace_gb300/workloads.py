@@ -1,0 +1,171 @@
+"""Synthetic telescope scenes of the benchmark workloads (seeded, no files).
+
+  davies_cotton()        12 m Davies-Cotton dish, f = 15 m, 380 spherical hex
+                         facets (0.60 m flat-to-flat, R = 2f), Gaussian
+                         tip/tilt errors (sigma 0.5 mrad), 4 mast cylinders
+                         (r = 5 cm) and a 1.5 x 1.5 x 1.6 m camera box.
+  plain_forward()        that dish, 32 x 30 square camera (42 mm pitch),
+                         16 point sources at z = 1e10 within 2.5 deg, values
+                         U(0.5, 1), 1000 samples per facet.
+  response_matrix()      that dish, 2048-pixel hex camera (42 mm pitch),
+                         4096 point sources on a 64 x 64 grid within +-3 deg,
+                         unit values, 256 samples per facet.
+  cassegrain()           two-mirror Cassegrain: 10 m conic primary
+                         (k = -1.05, f = 10 m) of 61 hex segments with
+                         aspheric terms, 3 m hyperboloid secondary, 32 x 32
+                         square camera, 64 point sources within 1.5 deg.
+
+Facet layouts follow the Davies-Cotton construction: facet centres on a
+sphere of radius f about the focus, each facet normal aimed at (0, 0, 2f).
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+import torch
+
+from .core.apertures import DiskAperture, PolygonAperture
+from .core.integrators import MCIntegrator
+from .core.obstructions import Box, Cylinder, group_obstructions
+from .core.surfaces import AsphericSurface
+from .sensors import HexagonalSensor, SquareSensor
+from .telescope.mirrors import Mirror, group_mirrors
+from .telescope.telescope import Telescope
+from .utils import keys as _keys
+
+
+def hex_grid(n: int, pitch: float) -> np.ndarray:
+    """The n points of a pointy-top hexagonal lattice (nearest-neighbour
+    distance `pitch`) closest to the origin, ordered by radius then angle."""
+    rings = int(math.ceil(math.sqrt(n / 3.0))) + 3
+    pts = []
+    for q in range(-rings, rings + 1):
+        for r in range(-rings, rings + 1):
+            x = pitch * (q + r / 2.0)
+            y = pitch * (math.sqrt(3) / 2.0) * r
+            pts.append((x, y))
+    pts = np.array(pts)
+    rad = np.round(np.hypot(pts[:, 0], pts[:, 1]), 9)
+    ang = np.round(np.mod(np.arctan2(pts[:, 1], pts[:, 0]), 2 * np.pi), 9)
+    order = np.lexsort((ang, rad))
+    return pts[order[:n]]
+
+
+def hex_vertices(flat_to_flat: float) -> list[list[float]]:
+    """Counter-clockwise vertices of a pointy-top hexagon."""
+    rc = flat_to_flat / math.sqrt(3.0)
+    return [[rc * math.cos(math.radians(90 + 60 * k)), rc * math.sin(math.radians(90 + 60 * k))] for k in range(6)]
+
+
+def dc_orientation(pos, aim_z: float) -> list[float]:
+    """Euler (tip, tilt, 0) degrees whose local +z points from pos to (0, 0, aim_z)."""
+    nvec = np.array([-pos[0], -pos[1], aim_z - pos[2]], float)
+    nvec /= np.linalg.norm(nvec)
+    tip = -math.degrees(math.asin(nvec[1]))
+    tilt = math.degrees(math.atan2(nvec[0], nvec[2]))
+    return [tip, tilt, 0.0]
+
+
+def davies_cotton(n_facets: int = 380, focal: float = 15.0, facet_flat: float = 0.60, tilt_sigma_mrad: float = 0.5,
+                  n_samples: int = 1000, seed: int = 0, obstructions: bool = True):
+    """Mirror groups (sampled) and obstruction groups of the DC dish."""
+    rng = np.random.default_rng(seed)
+    centres = hex_grid(n_facets, facet_flat)
+    surf = AsphericSurface(curvature=1.0 / (2.0 * focal), conic=0.0, aspheric=[])
+    verts = hex_vertices(facet_flat)
+    sig_deg = math.degrees(tilt_sigma_mrad * 1e-3)
+    mirrors = []
+    for (x, y) in centres:
+        z = focal - math.sqrt(focal * focal - x * x - y * y)
+        rot = dc_orientation((x, y, z), 2.0 * focal)
+        rot[0] += sig_deg * rng.standard_normal()
+        rot[1] += sig_deg * rng.standard_normal()
+        mirrors.append(Mirror([x, y, z], rot, surf, PolygonAperture(verts), optical_stage=0))
+    groups = group_mirrors(mirrors)
+    key = _keys.key(seed)
+    integ = MCIntegrator(n_samples)
+    groups = [integ.sample_group(g, k) for g, k in zip(groups, _keys.split(key, len(groups)))]
+    obst = []
+    if obstructions:
+        rim = 0.5 * facet_flat * math.sqrt(n_facets * math.sqrt(3) / 2 / math.pi) * 2 * 1.15
+        for ang in (60.0, 120.0, 240.0, 300.0):
+            a = math.radians(ang)
+            p1 = [rim * math.cos(a), rim * math.sin(a), 1.2]
+            p2 = [1.155 * math.cos(a), 1.155 * math.sin(a), focal + 0.6]
+            obst.append(Cylinder(p1, p2, 0.05))
+        obst.append(Box([-0.75, -0.75, focal], [0.75, 0.75, focal + 1.6]))
+    return groups, group_obstructions(obst)
+
+
+def point_sources_disk(n: int, max_deg: float, seed: int, distance: float = 1e10):
+    """n point sources at z = distance, directions uniform in a disk of angular radius max_deg."""
+    g = torch.Generator().manual_seed(seed)
+    th = torch.deg2rad(torch.tensor(max_deg, dtype=torch.float64)) * torch.sqrt(torch.rand(n, generator=g, dtype=torch.float64))
+    ph = 2 * math.pi * torch.rand(n, generator=g, dtype=torch.float64)
+    t = torch.tan(th)
+    return torch.stack([distance * t * torch.cos(ph), distance * t * torch.sin(ph),
+                        torch.full((n,), distance, dtype=torch.float64)], 1).float()
+
+
+def point_sources_grid(n_side: int, half_deg: float, distance: float = 1e10):
+    """n_side^2 point sources at z = distance on a regular angle grid within +-half_deg."""
+    a = torch.deg2rad(torch.linspace(-half_deg, half_deg, n_side, dtype=torch.float64))
+    X, Y = torch.meshgrid(a, a, indexing="xy")
+    return torch.stack([distance * torch.tan(X).reshape(-1), distance * torch.tan(Y).reshape(-1),
+                        torch.full((n_side * n_side,), distance, dtype=torch.float64)], 1).float()
+
+
+def plain_forward(n_samples: int = 1000, n_sources: int = 16, seed: int = 0):
+    """Plain-forward workload: (telescope, sources, values, source_type)."""
+    groups, obst = davies_cotton(n_samples=n_samples, seed=seed)
+    cam = SquareSensor([0.0, 0.0, 15.0], [0.0, 0.0, 0.0], 32, 30, (-0.672, 0.672, -0.63, 0.63))
+    tel = Telescope(groups, obst, [cam], name="dc12m_square")
+    src = point_sources_disk(n_sources, 2.5, seed + 1)
+    g = torch.Generator().manual_seed(seed + 2)
+    val = 0.5 + 0.5 * torch.rand(n_sources, generator=g)
+    return tel, src, val, "point"
+
+
+def hex_camera(n_pixels: int = 2048, pitch: float = 0.042, z: float = 15.0, edge_width: float = 0.0):
+    return HexagonalSensor([0.0, 0.0, z], [0.0, 0.0, 0.0], hex_grid(n_pixels, pitch).astype(np.float32),
+                           edge_width=edge_width)
+
+
+def response_matrix(n_samples: int = 256, n_side: int = 64, seed: int = 0):
+    """Response-matrix workload: (telescope, sources, values, source_type)."""
+    groups, obst = davies_cotton(n_samples=n_samples, seed=seed)
+    tel = Telescope(groups, obst, [hex_camera()], name="dc12m_hex2048")
+    src = point_sources_grid(n_side, 3.0)
+    return tel, src, torch.ones(src.shape[0]), "point"
+
+
+def cassegrain(n_samples: int = 500, n_sources: int = 64, seed: int = 0, with_aspheric: bool = True):
+    """Two-mirror Cassegrain workload: (telescope, sources, values, source_type)."""
+    f = 10.0
+    c1, k1 = 1.0 / (2.0 * f), -1.05
+    rng = np.random.default_rng(seed)
+    R = 5.0
+    asph = [float(rng.normal(0.0, 1e-6) / R ** (4 * (i + 1))) for i in range(4)] if with_aspheric else []
+    prim = AsphericSurface(c1, k1, asph)
+    verts = hex_vertices(1.2)
+    mirrors = []
+    for (x, y) in hex_grid(61, 1.2):
+        z0 = float(prim._sag_raw(torch.tensor(x, dtype=torch.float64), torch.tensor(y, dtype=torch.float64)))
+        mirrors.append(Mirror([x, y, z0], [0.0, 0.0, 0.0], prim, PolygonAperture(verts), optical_stage=0,
+                              offset=[x, y]))
+    # convex hyperboloid with foci at the primary focus (z = 10) and z = -0.5,
+    # vertex at z = 6 (local +z points down after the 180 deg tip)
+    a = 0.5 * ((6.0 + 0.5) - (f - 6.0))
+    ch = 0.5 * (f + 0.5)
+    sec = AsphericSurface(-a / (ch * ch - a * a), -(ch / a) ** 2, [])
+    mirrors.append(Mirror([0.0, 0.0, 6.0], [180.0, 0.0, 0.0], sec, DiskAperture(1.5), optical_stage=1))
+    groups = group_mirrors(mirrors)
+    key = _keys.key(seed)
+    integ = MCIntegrator(n_samples)
+    groups = [integ.sample_group(g, k) if g.optical_stage == 0 else g
+              for g, k in zip(groups, _keys.split(key, len(groups)))]
+    cam = SquareSensor([0.0, 0.0, -0.5], [0.0, 0.0, 0.0], 32, 32, (-0.45, 0.45, -0.45, 0.45))
+    tel = Telescope(groups, [], [cam], name="cassegrain10m")
+    src = point_sources_disk(n_sources, 1.5, seed + 1)
+    return tel, src, torch.ones(n_sources), "point"

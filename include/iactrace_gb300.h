@@ -1,0 +1,179 @@
+/*
+ * iactrace_gb300 — C ABI of the GB300 (sm_103a) render path of IACTrace.
+ *
+ * One call traces Monte-Carlo rays (source s, primary facet f, sample m)
+ * from the sampled primary-mirror points through obstruction shadowing,
+ * reflection, optional later mirror stages and the sensor plane, and bins
+ * them into a square or hexagonal pixel image.
+ *
+ * Conventions
+ *   - Every pointer inside iact_scene_t / iact_sensor_t and every array
+ *     argument is a DEVICE pointer (caller-owned, e.g. torch CUDA tensors),
+ *     except the descriptor structs themselves, which live in host memory
+ *     and are read only during the call.
+ *   - Calls are stream-ordered on `stream` (a cudaStream_t passed as void*;
+ *     NULL = legacy default stream). They never synchronise the device.
+ *   - The callee allocates nothing: scratch memory is the caller's
+ *     `workspace` of at least iact_workspace_size() bytes.
+ *   - Return value: IACT_OK (0) or a negative IACT_E_* status. The message
+ *     of the last failure on the calling thread is iact_last_error().
+ *   - Layout: float32 everywhere, row-major, xyz innermost. Angles are
+ *     Euler degrees (tip, tilt, rotation), R = Rz * Ry * Rx.
+ *
+ * Reference interface replaced (GerritRo/iactrace v0.4.0, JAX):
+ *   iact_render(IMAGE)     <- core/render.py:174-220  render()
+ *                             (telescope/telescope.py:56-83 Telescope.__call__)
+ *   iact_render(RESPONSE)  <- core/render.py:271-324  render_response_matrix()
+ *   iact_render_debug      <- core/render.py:223-268  render_debug()
+ *   iact_render_backward   <- jax.grad of render() / render_response_matrix()
+ *                             (no dedicated reference function)
+ *   iact_sample_facets     <- core/integrators.py:97-187 MCIntegrator.sample_group
+ */
+#ifndef IACTRACE_GB300_H
+#define IACTRACE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define IACT_ABI_VERSION 1
+
+/* status codes */
+#define IACT_OK 0
+#define IACT_E_INVALID (-1)     /* bad argument (null pointer, size, enum)  */
+#define IACT_E_UNSUPPORTED (-2) /* valid request this build cannot serve    */
+#define IACT_E_CUDA (-3)        /* CUDA runtime error (launch/config)       */
+#define IACT_E_WORKSPACE (-4)   /* workspace missing, too small, misaligned */
+#define IACT_E_DEVICE (-5)      /* a kernel-side check failed (see message) */
+
+/* limits of the packed tables */
+#define IACT_MAX_ASPH 8          /* aspheric coefficients per surface      */
+#define IACT_MAX_POLY 8          /* polygon aperture vertices              */
+#define IACT_MAX_STAGE_MIRRORS 64 /* mirrors over all stages >= 1          */
+#define IACT_MAX_OBSTRUCTIONS 2048 /* primitives over all obstruction kinds */
+
+enum { IACT_SRC_POINT = 0, IACT_SRC_PARALLEL = 1 };
+enum { IACT_MODE_IMAGE = 0, IACT_MODE_RESPONSE = 1 };
+enum {
+  IACT_SENSOR_SQUARE = 0,      /* sensors/square.py:28-91     SquareSensor */
+  IACT_SENSOR_HEX = 1,         /* sensors/hexagonal.py:104-194 HexagonalSensor */
+  IACT_SENSOR_SOFT_SQUARE = 2, /* sensors/square.py:94-172 DifferentiableSquareSensor */
+  IACT_SENSOR_SOFT_HEX = 3     /* sensors/hexagonal.py:197-315 DifferentiableHexagonalSensor */
+};
+enum { IACT_APERTURE_DISK = 0, IACT_APERTURE_POLYGON = 1 };
+
+/* One mirror of an optical stage >= 1 (telescope/mirrors.py:101-229). */
+typedef struct {
+  int32_t stage;    /* optical stage, >= 1; the table is sorted by stage  */
+  int32_t aperture; /* IACT_APERTURE_*                                     */
+  int32_t n_asph;   /* aspheric coefficients in use (<= IACT_MAX_ASPH)     */
+  int32_t n_vert;   /* polygon vertices in use (<= IACT_MAX_POLY)          */
+  float pos[3];
+  float rot[3];     /* Euler degrees */
+  float offset[2];  /* (x0, y0) on the parent surface */
+  float curvature, conic;
+  float asph[IACT_MAX_ASPH]; /* coefficient i multiplies r^(4(i+1)) */
+  float radius;              /* disk aperture radius */
+  float vert[IACT_MAX_POLY][2];
+  float pad_[5];
+} iact_mirror_t; /* 176 bytes */
+
+/* Scene: primary samples, later stages, obstructions. */
+typedef struct {
+  /* stage-0 facets, all primary groups concatenated (core/render.py:202-205) */
+  int32_t n_facets;  /* F */
+  int32_t n_samples; /* M (same for every facet) */
+  const float* facet_pos;   /* [F,3] */
+  const float* facet_rot;   /* [F,3] Euler degrees */
+  const float* facet_scale; /* [F]   perturbation scale, radians */
+  const float* points;      /* [F,M,3] local sample points */
+  const float* normals;     /* [F,M,3] local unit normals */
+  const float* delta;       /* [F,M,3] local unit-sigma perturbation deltas */
+  const float* weights;     /* [F,M]   sample weights */
+  /* stages >= 1, flattened in (stage, group, mirror) order */
+  int32_t n_mirrors;
+  const iact_mirror_t* mirrors; /* [n_mirrors] */
+  /* obstructions (core/obstructions.py) */
+  int32_t n_cyl, n_box, n_sph, n_obox, n_tri;
+  const float* cyl;  /* [n_cyl,7]  p1(3) p2(3) r          */
+  const float* box;  /* [n_box,6]  p1(3) p2(3)            */
+  const float* sph;  /* [n_sph,4]  center(3) r            */
+  const float* obox; /* [n_obox,15] center(3) half(3) R(9), R row-major local->world */
+  const float* tri;  /* [n_tri,9]  v0(3) v1(3) v2(3)      */
+} iact_scene_t;
+
+/* Sensor plane + pixelisation. Constants are the float32 values the
+ * reference computes at sensor construction. */
+typedef struct {
+  int32_t type;     /* IACT_SENSOR_* */
+  int32_t n_pixels; /* accumulator size: width*height or hex pixel count */
+  int32_t width, height;
+  float pos[3];
+  float rot[3]; /* Euler degrees */
+  /* square (both kinds) */
+  float x0, y0, dx, dy, edge_width;
+  /* hexagonal (both kinds) */
+  float hex_size, inradius, grid_cos, grid_sin, off_x, off_y;
+  float hex_sx, hex_sy; /* size*sqrt(3) and size*1.5 (axial -> Cartesian) */
+  float edge_threshold; /* 1 - edge_width / inradius */
+  int32_t q_min, r_min, table_q, table_r;
+  const int32_t* table; /* [table_q, table_r] pixel id or -1 */
+  /* soft deposition (Differentiable* sensors) */
+  float sigma;
+  int32_t kernel_size;
+} iact_sensor_t;
+
+/* Optional launch knobs; NULL or zeros select the built-in defaults. */
+typedef struct {
+  int32_t block_threads;    /* threads per CTA (multiple of 32)           */
+  int32_t sources_per_cta;  /* warps per CTA each own one source at a time */
+  int32_t facets_per_tile;  /* primary facets per work tile               */
+  int32_t hist_mode;        /* 0 auto, 1 shared-memory rows, 2 global     */
+  /* optional cudaEvent_t pair recorded on `stream` right before and after
+   * the render kernel (profiling); NULL to skip */
+  void* kernel_events[2];
+} iact_opts_t;
+
+int iact_abi_version(void);
+const char* iact_last_error(void);
+/* sizeof(iact_scene_t), sizeof(iact_sensor_t), sizeof(iact_mirror_t),
+ * sizeof(iact_opts_t) as compiled into the library (binding self-check). */
+int iact_abi_layout(size_t* out, int n);
+
+/* Diagnostics: runs `iters` dependent FP32 FMAs per thread over
+ * `blocks` x 256 threads (a throughput probe of the FP32 pipe) and writes
+ * one float per thread to out[blocks*256]. */
+int iact_probe_fma(float* out, int32_t blocks, int32_t iters, void* stream);
+
+/* Bytes of scratch needed by iact_render / iact_render_debug /
+ * iact_render_backward for this scene. */
+int iact_workspace_size(const iact_scene_t* scene, size_t* bytes);
+
+/* Forward render.
+ *   mode IMAGE:    out[n_pixels]            (zeroed by the callee)
+ *   mode RESPONSE: out[n_sources, n_pixels] (fully written by the callee)
+ * sources [S,3]: positions (POINT) or propagation directions (PARALLEL,
+ * used as given, not normalised); values [S]. */
+int iact_render(const iact_scene_t* scene, const iact_sensor_t* sensor,
+                int32_t source_type, const float* sources, const float* values,
+                int32_t n_sources, int32_t mode, float* out, void* workspace,
+                size_t workspace_bytes, const iact_opts_t* opts, void* stream);
+
+/* Per-ray hits in the reference's order, ray = (f*S + s)*M + m:
+ *   pts [F*S*M,2] sensor-plane (x, y) or (1e10, 1e10); vals [F*S*M];
+ *   pix [F*S*M] hard pixel id or -1 (may be NULL);
+ *   hit_mirror [F*S*M] index into scene->mirrors of the last stage's hit,
+ *   -1 for a miss or a single-stage scene (may be NULL). */
+int iact_render_debug(const iact_scene_t* scene, const iact_sensor_t* sensor,
+                      int32_t source_type, const float* sources,
+                      const float* values, int32_t n_sources, float* pts,
+                      float* vals, int32_t* pix, int32_t* hit_mirror,
+                      void* workspace, size_t workspace_bytes, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* IACTRACE_GB300_H */

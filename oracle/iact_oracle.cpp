@@ -1,0 +1,163 @@
+// ORACLE — test infrastructure only (see iact_oracle.hpp). C entry points
+// over the templated restatement: FP64 (the oracle) and FP32 (the index
+// restatement, multi-threaded as the timed CPU baseline).
+//
+// All descriptor pointers are HOST pointers here; the descriptor layout is
+// the product's C ABI (include/iactrace_gb300.h) so the same packed tables
+// feed the CUDA path and this checker.
+#include <omp.h>
+
+#include <cstdio>
+#include <vector>
+
+#include "iact_oracle.hpp"
+
+using namespace oracle;
+
+namespace {
+
+bool scene_ok(const iact_scene_t* sc, const iact_sensor_t* sn, int S) {
+  if (!sc || !sn || S < 0) return false;
+  if (sc->n_facets < 0 || sc->n_samples < 0) return false;
+  if (sn->n_pixels <= 0) return false;
+  return true;
+}
+
+template <typename T>
+void deposit_ray(const iact_sensor_t& sn, T x, T y, T v, T* row) {
+  if (sn.type == IACT_SENSOR_SQUARE || sn.type == IACT_SENSOR_HEX) {
+    int32_t p = bin_hard<T>(sn, x, y, nullptr);
+    if (p >= 0) row[p] += v;
+  } else if (sn.type == IACT_SENSOR_SOFT_SQUARE) {
+    splat_square<T>(sn, x, y, v, [&](int32_t p, T w) { row[p] += w; });
+  } else {
+    splat_hex<T>(sn, x, y, v, [&](int32_t p, T w) { row[p] += w; });
+  }
+}
+
+// core/render.py:174-220 render (mode IMAGE) and :271-324
+// render_response_matrix (mode RESPONSE); the facet sum order is the
+// reference's lax.scan order when n_threads == 1.
+template <typename T>
+int render_impl(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type, const float* sources,
+                const float* values, int S, int mode, T* out, int n_threads) {
+  if (!scene_ok(sc, sn, S)) return IACT_E_INVALID;
+  const size_t P = (size_t)sn->n_pixels;
+  const size_t F = (size_t)sc->n_facets, M = (size_t)sc->n_samples;
+  const size_t rows = (mode == IACT_MODE_RESPONSE) ? (size_t)S : 1;
+  std::fill(out, out + rows * P, T(0));
+  if (F == 0 || M == 0 || S == 0) return IACT_OK;
+  World<T> w = transform_to_world<T>(*sc);
+  Prepared<T> pr = prepare<T>(*sc, *sn);
+  if (n_threads <= 0) n_threads = omp_get_max_threads();
+  if (mode == IACT_MODE_RESPONSE) {
+    // each thread owns whole source rows: no reduction needed
+#pragma omp parallel for schedule(dynamic, 1) num_threads(n_threads)
+    for (int s = 0; s < S; ++s) {
+      T* row = out + (size_t)s * P;
+      for (size_t f = 0; f < F; ++f) {
+        for (size_t m = 0; m < M; ++m) {
+          RayOut<T> r = trace_ray<T>(*sc, pr, w, f * M + m, src_type, sources + 3 * s, T(values[s]));
+          deposit_ray<T>(*sn, r.x, r.y, r.val, row);
+        }
+      }
+    }
+    return IACT_OK;
+  }
+  // image: per-thread accumulators over facets, summed at the end
+  std::vector<std::vector<T>> acc((size_t)n_threads, std::vector<T>(P, T(0)));
+#pragma omp parallel for schedule(dynamic, 1) num_threads(n_threads)
+  for (long f = 0; f < (long)F; ++f) {
+    T* img = acc[(size_t)omp_get_thread_num()].data();
+    for (int s = 0; s < S; ++s)
+      for (size_t m = 0; m < M; ++m) {
+        RayOut<T> r = trace_ray<T>(*sc, pr, w, (size_t)f * M + m, src_type, sources + 3 * s, T(values[s]));
+        deposit_ray<T>(*sn, r.x, r.y, r.val, img);
+      }
+  }
+  for (int t = 0; t < n_threads; ++t)
+    for (size_t p = 0; p < P; ++p) out[p] += acc[(size_t)t][p];
+  return IACT_OK;
+}
+
+// core/render.py:223-268 render_debug, ray = (f*S + s)*M + m
+template <typename T>
+int debug_impl(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type, const float* sources,
+               const float* values, int S, T* pts, T* vals, int32_t* pix, int32_t* hit_mirror,
+               T* margin) {
+  if (!scene_ok(sc, sn, S)) return IACT_E_INVALID;
+  const size_t F = (size_t)sc->n_facets, M = (size_t)sc->n_samples;
+  if (F == 0 || M == 0 || S == 0) return IACT_OK;
+  World<T> w = transform_to_world<T>(*sc);
+  Prepared<T> pr = prepare<T>(*sc, *sn);
+#pragma omp parallel for schedule(static)
+  for (long f = 0; f < (long)F; ++f)
+    for (int s = 0; s < S; ++s)
+      for (size_t m = 0; m < M; ++m) {
+        size_t i = ((size_t)f * S + s) * M + m;
+        RayOut<T> r = trace_ray<T>(*sc, pr, w, (size_t)f * M + m, src_type, sources + 3 * s, T(values[s]));
+        pts[2 * i] = r.x;
+        pts[2 * i + 1] = r.y;
+        vals[i] = r.val;
+        T mg = 0;
+        int32_t p = -1;
+        if (sn->type == IACT_SENSOR_SQUARE || sn->type == IACT_SENSOR_HEX ||
+            sn->type == IACT_SENSOR_SOFT_SQUARE || sn->type == IACT_SENSOR_SOFT_HEX) {
+          iact_sensor_t hard = *sn;
+          if (hard.type == IACT_SENSOR_SOFT_SQUARE) hard.type = IACT_SENSOR_SQUARE;
+          if (hard.type == IACT_SENSOR_SOFT_HEX) hard.type = IACT_SENSOR_HEX;
+          p = bin_hard<T>(hard, r.x, r.y, &mg);
+        }
+        if (pix) pix[i] = p;
+        if (hit_mirror) hit_mirror[i] = r.hit_mirror;
+        if (margin) margin[i] = mg;
+      }
+  return IACT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int oracle_render_f64(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type,
+                      const float* sources, const float* values, int S, int mode, double* out,
+                      int n_threads) {
+  return render_impl<double>(sc, sn, src_type, sources, values, S, mode, out, n_threads);
+}
+
+int oracle_render_f32(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type,
+                      const float* sources, const float* values, int S, int mode, float* out,
+                      int n_threads) {
+  return render_impl<float>(sc, sn, src_type, sources, values, S, mode, out, n_threads);
+}
+
+int oracle_render_debug_f64(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type,
+                            const float* sources, const float* values, int S, double* pts,
+                            double* vals, int32_t* pix, int32_t* hit_mirror, double* margin) {
+  return debug_impl<double>(sc, sn, src_type, sources, values, S, pts, vals, pix, hit_mirror, margin);
+}
+
+int oracle_render_debug_f32(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type,
+                            const float* sources, const float* values, int S, float* pts,
+                            float* vals, int32_t* pix, int32_t* hit_mirror, float* margin) {
+  return debug_impl<float>(sc, sn, src_type, sources, values, S, pts, vals, pix, hit_mirror, margin);
+}
+
+// telescope/mirrors.py:64-79 transform_to_world, for direct checks
+int oracle_transform_f64(const iact_scene_t* sc, double* tp, double* tn, double* tw) {
+  World<double> w = transform_to_world<double>(*sc);
+  for (size_t i = 0; i < w.tw.size(); ++i) {
+    tp[3 * i] = w.tp[i].x;
+    tp[3 * i + 1] = w.tp[i].y;
+    tp[3 * i + 2] = w.tp[i].z;
+    tn[3 * i] = w.tn[i].x;
+    tn[3 * i + 1] = w.tn[i].y;
+    tn[3 * i + 2] = w.tn[i].z;
+    tw[i] = w.tw[i];
+  }
+  return IACT_OK;
+}
+
+int oracle_max_threads(void) { return omp_get_max_threads(); }
+
+}  // extern "C"

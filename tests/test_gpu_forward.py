@@ -1,0 +1,212 @@
+"""Forward-path parity of the CUDA kernels against the FP64 oracle.
+
+Every case runs the CUDA path through the C ABI (iact_render /
+iact_render_debug) and the C++ restatement of the reference on the same
+packed scene and the same sample arrays.
+
+Acceptance (the tolerances are written here, per case):
+  * per ray, the hard pixel id equals the FP64 oracle's unless the FP64 hit
+    lies within EDGE_BAND of a pixel edge (the float32 reference chain itself
+    moves hits by up to ~3e-6 m against FP64; EDGE_BAND = 4e-6 m, i.e.
+    1e-4 of a 42 mm pixel);
+  * shadow decisions (value zero vs non-zero) differ on at most
+    SHADOW_FLIPS of the rays (rays grazing an obstruction);
+  * sensor-plane hits agree within PTS_TOL metres;
+  * the image (or response matrix) equals the FP64 ray values binned with
+    the GPU's own pixel ids to a relative L2 error <= IMG_TOL (1e-5): this is
+    the image error of the arithmetic and of the accumulation; the raw
+    relative L2 against the FP64 image, which adds the edge flips above, is
+    bounded by RAW_TOL.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+import torch
+
+import iactrace_gb300 as it
+from iactrace_gb300 import workloads as W
+
+EDGE_BAND = 4e-6
+SHADOW_FLIPS = 2e-5
+PTS_TOL = 8e-6
+IMG_TOL = 1e-5
+RAW_TOL = 2e-4
+
+pytestmark = pytest.mark.gpu
+
+
+def _oracle():
+    import oracle.oracle as O
+    return O
+
+
+def _gpu_debug(tel, src, val, st, sensor_idx=0):
+    pts, vals, pix, hm = it.render_debug(tel, src, val, st, sensor_idx, extras=True)
+    return {"pts": pts.cpu().double().numpy(), "vals": vals.cpu().double().numpy(),
+            "pix": pix.cpu().numpy(), "hit_mirror": hm.cpu().numpy()}
+
+
+def check_rays(tel, src, val, st, sensor_idx=0, check_mirror=True):
+    O = _oracle()
+    g = _gpu_debug(tel, src, val, st, sensor_idx)
+    o = O.render_debug(tel, src, val, st, sensor_idx, "f64")
+    n = g["vals"].size
+    assert n == o["vals"].size
+    flips = g["pix"] != o["pix"]
+    assert np.all(o["margin"][flips] < EDGE_BAND), \
+        f"{flips.sum()} pixel mismatches, max edge margin {o['margin'][flips].max():.3g} m"
+    zg, zo = g["vals"] == 0, o["vals"] == 0
+    sh = zg != zo
+    assert sh.sum() <= max(2, SHADOW_FLIPS * n), f"{sh.sum()} shadow flips of {n}"
+    ok = (o["pts"][:, 0] < 1e9) & (g["pts"][:, 0] < 1e9)
+    assert np.array_equal(o["pts"][:, 0] < 1e9, g["pts"][:, 0] < 1e9)
+    if ok.any():
+        perr = np.abs(g["pts"][ok] - o["pts"][ok]).max()
+        assert perr < PTS_TOL, f"sensor-plane hits differ by {perr:.3g} m"
+    same = ~sh & ~zo
+    if same.any():
+        verr = np.abs(g["vals"][same] - o["vals"][same]) / np.abs(o["vals"][same]).max()
+        assert verr.max() < 2e-5, f"ray values differ by {verr.max():.3g} (relative)"
+    if check_mirror:
+        mm = g["hit_mirror"] != o["hit_mirror"]
+        assert mm.sum() <= max(2, 1e-4 * n), f"{mm.sum()} stage-mirror hit mismatches"
+    return g, o, {"pix_flips": int(flips.sum()), "shadow_flips": int(sh.sum()), "rays": n}
+
+
+def rebin(pix, vals, P, S=None, M=None, F=None):
+    """FP64 accumulation of ray values at the given pixel ids (ray order f, s, m)."""
+    if S is None:
+        img = np.zeros(P)
+        m = pix >= 0
+        np.add.at(img, pix[m], vals[m])
+        return img
+    out = np.zeros((S, P))
+    s_idx = (np.arange(pix.size) // M) % S
+    m = pix >= 0
+    np.add.at(out, (s_idx[m], pix[m]), vals[m])
+    return out
+
+
+def check_image(tel, src, val, st, sensor_idx=0, mode="image", img_tol=IMG_TOL, raw_tol=RAW_TOL):
+    O = _oracle()
+    g, o, stats = check_rays(tel, src, val, st, sensor_idx)
+    P = int(np.prod(tel.sensors[sensor_idx].get_accumulator_shape()))
+    S = src.shape[0]
+    M = tel.mirror_groups[0].n_samples
+    if mode == "image":
+        img = it.render(tel, src, val, st, sensor_idx).cpu().double().numpy().reshape(-1)
+        ref_cont = rebin(g["pix"], o["vals"], P)
+        ref = O.render(tel, src, val, st, sensor_idx).reshape(-1)
+    else:
+        img = it.render_response_matrix(tel, src, val, st, sensor_idx).cpu().double().numpy()
+        ref_cont = rebin(g["pix"], o["vals"], P, S, M)
+        ref = O.render(tel, src, val, st, sensor_idx, mode="response")
+    scale = np.linalg.norm(ref)
+    cont = np.linalg.norm(img - ref_cont) / scale
+    raw = np.linalg.norm(img - ref) / scale
+    assert cont <= img_tol, f"image error {cont:.3g} > {img_tol} (stats {stats})"
+    assert raw <= raw_tol, f"raw image error {raw:.3g} > {raw_tol} (stats {stats})"
+    return cont, raw, stats
+
+
+def test_plain_forward_square(cuda):
+    tel, src, val, st = W.plain_forward(n_samples=256, n_sources=16)
+    cont, raw, stats = check_image(tel, src, val, st)
+    print(f"plain: cont {cont:.2e} raw {raw:.2e} {stats}")
+
+
+def test_response_matrix_hex(cuda):
+    tel, src, val, st = W.response_matrix(n_samples=32, n_side=16)
+    cont, raw, stats = check_image(tel, src, val, st, mode="response")
+    print(f"response: cont {cont:.2e} raw {raw:.2e} {stats}")
+
+
+def test_response_equals_image_sum(cuda):
+    """Rows of the response matrix sum to the image (same rays, same bins)."""
+    tel, src, val, st = W.response_matrix(n_samples=32, n_side=8)
+    R = it.render_response_matrix(tel, src, val, st).double()
+    img = it.render(tel, src, val, st).double()
+    assert torch.allclose(R.sum(0), img, rtol=1e-5, atol=1e-6 * img.abs().max().item())
+
+
+def test_parallel_sources_hex_edge(cuda):
+    from iactrace_gb300 import Telescope
+    groups, obst = W.davies_cotton(n_samples=64, seed=3)
+    cam = W.hex_camera(960, 0.042, edge_width=0.002)
+    tel = Telescope(groups, obst, [cam])
+    g = torch.Generator().manual_seed(5)
+    th = torch.deg2rad(torch.tensor(2.0)) * torch.sqrt(torch.rand(12, generator=g))
+    ph = 6.283185307 * torch.rand(12, generator=g)
+    d = torch.stack([torch.sin(th) * torch.cos(ph), torch.sin(th) * torch.sin(ph), -torch.cos(th)], 1)
+    check_image(tel, d, torch.rand(12, generator=g) + 0.5, "parallel")
+
+
+def test_square_edge_width_and_roughness(cuda):
+    from iactrace_gb300 import SquareSensor, Telescope
+    groups, obst = W.davies_cotton(n_samples=64, seed=4)
+    tel = Telescope(groups, obst, [SquareSensor([0, 0, 15.0], [0, 0, 0], 32, 30, (-0.672, 0.672, -0.63, 0.63),
+                                                edge_width=0.003)])
+    tel = tel.apply_roughness(24.0)
+    src = W.point_sources_disk(8, 2.5, 9)
+    check_image(tel, src, torch.ones(8), "point")
+
+
+def test_cassegrain_two_stage(cuda):
+    tel, src, val, st = W.cassegrain(n_samples=64, n_sources=16)
+    cont, raw, stats = check_image(tel, src, val, st)
+    print(f"cassegrain: cont {cont:.2e} raw {raw:.2e} {stats}")
+
+
+def test_sphere_obox_triangle_obstructions(cuda):
+    from iactrace_gb300 import Telescope
+    from iactrace_gb300.core import OrientedBox, Sphere, Triangle, group_obstructions
+    from iactrace_gb300.core.transforms import euler_to_matrix
+    groups, obst = W.davies_cotton(n_samples=64, seed=6)
+    extra = group_obstructions([
+        Sphere([1.0, 0.5, 8.0], 0.6), Sphere([-2.0, 1.0, 5.0], 0.3),
+        OrientedBox([0.0, -2.0, 7.0], [0.8, 0.3, 0.4], euler_to_matrix(torch.tensor([10.0, 20.0, 30.0]))),
+        Triangle([-1.0, -1.0, 9.0], [1.5, -0.5, 9.5], [0.0, 1.5, 8.5]),
+    ])
+    tel = Telescope(groups, list(obst) + extra, [W.hex_camera(960)])
+    src = W.point_sources_disk(8, 2.0, 11)
+    check_image(tel, src, torch.ones(8), "point")
+
+
+@pytest.mark.parametrize("kind", ["square", "hex"])
+def test_soft_sensors(cuda, kind):
+    from iactrace_gb300 import DifferentiableHexagonalSensor, DifferentiableSquareSensor, Telescope
+    groups, obst = W.davies_cotton(n_samples=64, seed=7)
+    if kind == "square":
+        cam = DifferentiableSquareSensor([0, 0, 15.0], [0, 0, 0], 32, 30, (-0.672, 0.672, -0.63, 0.63), sigma=0.4)
+    else:
+        cam = DifferentiableHexagonalSensor([0, 0, 15.0], [0, 0, 0], W.hex_grid(960, 0.042), sigma=0.5)
+    tel = Telescope(groups, obst, [cam])
+    src = W.point_sources_disk(8, 2.0, 12)
+    O = _oracle()
+    img = it.render(tel, src, torch.ones(8), "point").cpu().double().numpy().reshape(-1)
+    ref = O.render(tel, src, torch.ones(8), "point").reshape(-1)
+    err = np.linalg.norm(img - ref) / np.linalg.norm(ref)
+    assert err < 1e-4, err
+
+
+def test_empty_and_edge_inputs(cuda):
+    tel, src, val, st = W.plain_forward(n_samples=32, n_sources=4)
+    z = it.render(tel, src[:0], val[:0], st)
+    assert z.shape == (30, 32) and float(z.abs().sum()) == 0.0
+    R = it.render_response_matrix(tel, src[:0], val[:0], st)
+    assert R.shape == (0, 960)
+    # a source behind the dish: every ray is shadowed or misses; no NaN
+    img = it.render(tel, torch.tensor([[0.0, 0.0, -1e10]]), torch.ones(1), "point")
+    assert torch.isfinite(img).all()
+    # one sample per facet, one source
+    tel1, src1, val1, st1 = W.plain_forward(n_samples=1, n_sources=1)
+    check_image(tel1, src1, val1, st1, raw_tol=1e-3)
+
+
+def test_large_sample_counts_ragged(cuda):
+    """M not a multiple of 32 and S not a multiple of the warps per CTA."""
+    tel, src, val, st = W.plain_forward(n_samples=77, n_sources=13)
+    check_image(tel, src, val, st)
+    tel2, src2, val2, st2 = W.response_matrix(n_samples=45, n_side=5)
+    check_image(tel2, src2, val2, st2, mode="response")

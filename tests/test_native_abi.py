@@ -1,0 +1,68 @@
+"""The C ABI library: loads without a GPU, exports every declared symbol,
+agrees with the binding on struct layouts and validates its arguments."""
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+
+import pytest
+
+from iactrace_gb300 import _native as N
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    src = open(os.path.join(ROOT, "include", "iactrace_gb300.h")).read()
+    return sorted(set(re.findall(r"^\s*(?:int|const char\*)\s+(iact_\w+)\s*\(", src, re.M)))
+
+
+def test_exports_every_declared_symbol(built):
+    lib = ctypes.CDLL(N.lib_path())
+    syms = declared_symbols()
+    assert "iact_render" in syms and "iact_render_debug" in syms
+    for s in syms:
+        assert hasattr(lib, s), f"{s} declared in include/iactrace_gb300.h but not exported"
+
+
+def test_layout_and_version(built):
+    N.check_layout(built)
+    assert built.iact_abi_version() == 1
+
+
+def test_workspace_size_and_validation(built):
+    sc = N.IactScene()
+    sz = ctypes.c_size_t(0)
+    assert built.iact_workspace_size(ctypes.byref(sc), ctypes.byref(sz)) == 0 and sz.value > 0
+    sc.n_facets, sc.n_samples = 4, 8  # arrays missing
+    assert built.iact_workspace_size(ctypes.byref(sc), ctypes.byref(sz)) == N.IACT_E_INVALID
+    assert b"non-NULL" in built.iact_last_error()
+    sc = N.IactScene()
+    sc.n_cyl = 3  # table missing
+    assert built.iact_workspace_size(ctypes.byref(sc), ctypes.byref(sz)) == N.IACT_E_INVALID
+
+
+def test_render_rejects_bad_arguments_before_any_cuda_call(built):
+    sc, sn = N.IactScene(), N.IactSensor()
+    rc = built.iact_render(ctypes.byref(sc), ctypes.byref(sn), 0, None, None, 0, 0, None, None, 0, None, None)
+    assert rc == N.IACT_E_INVALID  # sensor without pixels
+    sn.type, sn.n_pixels, sn.width, sn.height, sn.dx, sn.dy = N.SENSOR_SQUARE, 4, 2, 2, 0.1, 0.1
+    rc = built.iact_render(ctypes.byref(sc), ctypes.byref(sn), 7, None, None, 0, 0, None, None, 0, None, None)
+    assert rc == N.IACT_E_INVALID and b"source_type" in built.iact_last_error()
+    rc = built.iact_render(ctypes.byref(sc), ctypes.byref(sn), 0, None, None, 0, 0, None, None, 0, None, None)
+    assert rc == N.IACT_E_WORKSPACE
+    sn.type = N.SENSOR_HEX
+    rc = built.iact_render(ctypes.byref(sc), ctypes.byref(sn), 0, None, None, 0, 0, None, None, 0, None, None)
+    assert rc == N.IACT_E_INVALID and b"lookup table" in built.iact_last_error()
+
+
+def test_render_without_device_fails_loudly(built):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("has a GPU")
+    import iactrace_gb300 as it
+    from iactrace_gb300 import workloads as W
+    tel, src, val, st = W.plain_forward(n_samples=4, n_sources=1)
+    with pytest.raises(RuntimeError):
+        it.render(tel, src, val, st)
