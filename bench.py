@@ -242,6 +242,9 @@ def main():
 
     opts = N.IactOpts()
     kev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for a, b in kev:  # torch creates the CUDA event at its first record()
+        a.record(stream)
+        b.record(stream)
 
     for _ in range(args.warmup):
         out = fn(tel, src, val, stype)
@@ -305,7 +308,7 @@ def main():
                      "traffic": None, "kernel": "k_render", "kernel_ms": kern_s * 1e3,
                      "flops_per_ray": F_RAY[args.workload],
                      "peak_source": "measured live: FP32 FMA-chain probe kernel (iact_probe_fma)"},
-        "gpu_launches": 2 * args.steps,
+        "gpu_launches": 3 * args.steps,  # k_prep, k_render, k_finish per step
         "clocks": clk,
     }
     if rank == 0 and not args.no_cpu_baseline:

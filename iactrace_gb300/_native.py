@@ -30,6 +30,7 @@ SRC_POINT = 0
 SRC_PARALLEL = 1
 MODE_IMAGE = 0
 MODE_RESPONSE = 1
+MODE_DEBUG = 2
 SENSOR_SQUARE = 0
 SENSOR_HEX = 1
 SENSOR_SOFT_SQUARE = 2
@@ -100,7 +101,8 @@ _SIGS = {
     "iact_abi_version": ([], ctypes.c_int),
     "iact_last_error": ([], ctypes.c_char_p),
     "iact_abi_layout": ([ctypes.POINTER(ctypes.c_size_t), ctypes.c_int], ctypes.c_int),
-    "iact_workspace_size": ([ctypes.POINTER(IactScene), ctypes.POINTER(ctypes.c_size_t)], ctypes.c_int),
+    "iact_workspace_size": ([ctypes.POINTER(IactScene), ctypes.POINTER(IactSensor), _i, _i,
+                             ctypes.POINTER(ctypes.c_size_t)], ctypes.c_int),
     "iact_render": ([ctypes.POINTER(IactScene), ctypes.POINTER(IactSensor), _i, ctypes.c_void_p, ctypes.c_void_p,
                      _i, _i, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(IactOpts),
                      ctypes.c_void_p], ctypes.c_int),

@@ -35,8 +35,9 @@ def _inputs(sources, values, device):
     return src, val
 
 
-def _workspace(ps, device):
-    return torch.empty(max(ps.ws_bytes, 256), dtype=torch.uint8, device=device)
+def _workspace(ps, sdesc, S, mode, device):
+    """Per-call scratch from torch's stream-ordered caching allocator."""
+    return torch.empty(max(ps.workspace_bytes(sdesc, S, mode), 256), dtype=torch.uint8, device=device)
 
 
 def _launch(tel, sources, values, source_type, sensor_idx, mode, opts=None):
@@ -52,7 +53,7 @@ def _launch(tel, sources, values, source_type, sensor_idx, mode, opts=None):
     ps = pack_scene(tel, device)
     sdesc, keep = sensor.pack(device)
     out = torch.empty(shape, dtype=torch.float32, device=device)
-    ws = _workspace(ps, device)
+    ws = _workspace(ps, sdesc, S, mode, device)
     stream = torch.cuda.current_stream(device).cuda_stream
     N.check(lib.iact_render(ctypes.byref(ps.desc), ctypes.byref(sdesc), source_code(source_type),
                             src.data_ptr(), val.data_ptr(), S, mode, out.data_ptr(), ws.data_ptr(),
@@ -90,7 +91,7 @@ def render_debug(tel, sources, values, source_type="point", sensor_idx=0, extras
     vals = torch.empty((n,), dtype=torch.float32, device=device)
     pix = torch.empty((n,), dtype=torch.int32, device=device) if extras else None
     hm = torch.empty((n,), dtype=torch.int32, device=device) if extras else None
-    ws = _workspace(ps, device)
+    ws = _workspace(ps, sdesc, S, N.MODE_DEBUG, device)
     stream = torch.cuda.current_stream(device).cuda_stream
     N.check(lib.iact_render_debug(ctypes.byref(ps.desc), ctypes.byref(sdesc), source_code(source_type),
                                   src.data_ptr(), val.data_ptr(), S, pts.data_ptr(), vals.data_ptr(),

@@ -108,10 +108,12 @@ class PackedScene:
                 setattr(d, kind, t.data_ptr())
         self.desc = d
         self.device = device
+
+    def workspace_bytes(self, sensor_desc, n_sources: int, mode: int) -> int:
         size = ctypes.c_size_t(0)
-        lib = N.load()
-        N.check(lib.iact_workspace_size(ctypes.byref(d), ctypes.byref(size)))
-        self.ws_bytes = int(size.value)
+        N.check(N.load().iact_workspace_size(ctypes.byref(self.desc), ctypes.byref(sensor_desc), int(n_sources),
+                                             int(mode), ctypes.byref(size)))
+        return int(size.value)
 
 
 def _fingerprint(tel):

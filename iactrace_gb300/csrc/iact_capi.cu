@@ -77,7 +77,7 @@ int validate_sensor(const iact_sensor_t* sn) {
 namespace {
 
 int check_common(const iact_scene_t* sc, const iact_sensor_t* sn, int32_t src_type, const float* sources,
-                 const float* values, int32_t S, void* ws, size_t ws_bytes) {
+                 const float* values, int32_t S, int mode, void* ws, size_t ws_bytes) {
   int rc = validate_scene(sc);
   if (rc) return rc;
   rc = validate_sensor(sn);
@@ -86,7 +86,7 @@ int check_common(const iact_scene_t* sc, const iact_sensor_t* sn, int32_t src_ty
     return set_error(IACT_E_INVALID, "source_type must be IACT_SRC_POINT or IACT_SRC_PARALLEL");
   if (S < 0) return set_error(IACT_E_INVALID, "negative source count");
   if (S > 0 && (!sources || !values)) return set_error(IACT_E_INVALID, "sources/values are NULL");
-  const WsLayout L = workspace_layout(sc);
+  const WsLayout L = workspace_layout(sc, acc_elems(sn, S, mode));
   if (!ws) return set_error(IACT_E_WORKSPACE, "workspace is NULL");
   if (reinterpret_cast<uintptr_t>(ws) % 256) return set_error(IACT_E_WORKSPACE, "workspace must be 256-byte aligned");
   if (ws_bytes < L.total)
@@ -120,22 +120,28 @@ int iact_probe_fma(float* out, int32_t blocks, int32_t iters, void* stream) {
   return launch_probe_fma(out, blocks, iters, static_cast<cudaStream_t>(stream));
 }
 
-int iact_workspace_size(const iact_scene_t* scene, size_t* bytes) {
+int iact_workspace_size(const iact_scene_t* scene, const iact_sensor_t* sensor, int32_t n_sources, int32_t mode,
+                        size_t* bytes) {
   int rc = validate_scene(scene);
   if (rc) return rc;
+  rc = validate_sensor(sensor);
+  if (rc) return rc;
   if (!bytes) return set_error(IACT_E_INVALID, "bytes is NULL");
-  *bytes = workspace_layout(scene).total;
+  if (n_sources < 0) return set_error(IACT_E_INVALID, "negative source count");
+  if (mode != IACT_MODE_IMAGE && mode != IACT_MODE_RESPONSE && mode != IACT_MODE_DEBUG)
+    return set_error(IACT_E_INVALID, "unknown mode");
+  *bytes = workspace_layout(scene, acc_elems(sensor, n_sources, mode)).total;
   return IACT_OK;
 }
 
 int iact_render(const iact_scene_t* scene, const iact_sensor_t* sensor, int32_t source_type,
                 const float* sources, const float* values, int32_t n_sources, int32_t mode, float* out,
                 void* workspace, size_t workspace_bytes, const iact_opts_t* opts, void* stream) {
-  int rc = check_common(scene, sensor, source_type, sources, values, n_sources, workspace, workspace_bytes);
-  if (rc) return rc;
   if (mode != IACT_MODE_IMAGE && mode != IACT_MODE_RESPONSE)
     return set_error(IACT_E_INVALID, "mode must be IACT_MODE_IMAGE or IACT_MODE_RESPONSE");
-  if (!out) return set_error(IACT_E_INVALID, "out is NULL");
+  int rc = check_common(scene, sensor, source_type, sources, values, n_sources, mode, workspace, workspace_bytes);
+  if (rc) return rc;
+  if (!out && acc_elems(sensor, n_sources, mode) > 0) return set_error(IACT_E_INVALID, "out is NULL");
   if (mode == IACT_MODE_RESPONSE && (long long)n_sources * sensor->n_pixels > 0x7fffffffLL)
     return set_error(IACT_E_UNSUPPORTED, "response matrix larger than 2^31 entries");
   return launch_render(scene, sensor, source_type, sources, values, n_sources, mode, out, workspace,
@@ -145,7 +151,8 @@ int iact_render(const iact_scene_t* scene, const iact_sensor_t* sensor, int32_t 
 int iact_render_debug(const iact_scene_t* scene, const iact_sensor_t* sensor, int32_t source_type,
                       const float* sources, const float* values, int32_t n_sources, float* pts, float* vals,
                       int32_t* pix, int32_t* hit_mirror, void* workspace, size_t workspace_bytes, void* stream) {
-  int rc = check_common(scene, sensor, source_type, sources, values, n_sources, workspace, workspace_bytes);
+  int rc = check_common(scene, sensor, source_type, sources, values, n_sources, IACT_MODE_DEBUG, workspace,
+                        workspace_bytes);
   if (rc) return rc;
   const long long n = (long long)scene->n_facets * n_sources * scene->n_samples;
   if (n > 0 && (!pts || !vals)) return set_error(IACT_E_INVALID, "pts/vals are NULL");

@@ -25,10 +25,12 @@ struct WsLayout {
   size_t tables;   // processed obstruction/mirror/sensor records (floats)
   size_t p4;       // float4 [F*M] world point, 1/weight
   size_t n4;       // float4 [F*M] perturbed world normal
+  size_t acc;      // double [rows * P] FP64 accumulator of the render
   size_t total;
   int n_table_floats;
 };
-WsLayout workspace_layout(const iact_scene_t* sc);
+WsLayout workspace_layout(const iact_scene_t* sc, size_t acc_elems);
+size_t acc_elems(const iact_sensor_t* sn, int S, int mode);  // mode < 0: debug (none)
 
 int launch_render(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type,
                   const float* sources, const float* values, int S, int mode, float* out,

@@ -156,29 +156,40 @@ struct RenderK {
   const int* hex_table;
   int hex_in_smem;
   SensorK sn;
-  float* out;
-  int rows_in_smem;  // histogram rows held in shared memory, 0 = add to `out` directly
+  double* acc;       // FP64 accumulator [rows_total * P] in the workspace
+  int rows_in_smem;  // FP32 histogram rows held in shared memory per tile, 0 = add to `acc` directly
   int SB, FC, CC;    // tile: sources, facets, 32-sample chunks
   int n_fchunk, n_cchunk, n_tiles;
   int* counter;
 };
 
+// Where hits go: FP32 shared-memory rows of the current tile, or the FP64
+// global accumulator. The choice is uniform over the CTA.
+struct Sink {
+  float* sh;
+  double* g;
+  __device__ __forceinline__ void add(int key, float v) const {
+    if (sh) atomicAdd(sh + key, v);
+    else atomicAdd(g + key, (double)v);
+  }
+};
+
 // all 32 lanes call; key < 0 or v == 0 means nothing to add for this lane
-__device__ __forceinline__ void warp_add(float* hist, int key, float v) {
+__device__ __forceinline__ void warp_add(const Sink& sink, int key, float v) {
   const int k0 = __shfl_sync(kFull, key, 0);
   if (__all_sync(kFull, key == k0)) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
-    if ((threadIdx.x & 31) == 0 && k0 >= 0 && v != 0.f) atomicAdd(hist + k0, v);
+    if ((threadIdx.x & 31) == 0 && k0 >= 0 && v != 0.f) sink.add(k0, v);
   } else if (key >= 0 && v != 0.f) {
-    atomicAdd(hist + key, v);
+    sink.add(key, v);
   }
 }
 
 // sensors/square.py:144-172 DifferentiableSquareSensor.accumulate, one ray
 // (all lanes call; inactive lanes pass ok = false). Rays whose plane hit is
 // the 1e10 sentinel deposit nothing.
-__device__ __forceinline__ void splat_square(const SensorK& s, float* hist, int rowbase, bool ok,
+__device__ __forceinline__ void splat_square(const SensorK& s, const Sink& sink, int rowbase, bool ok,
                                              float x, float y, float v) {
   ok = ok && (x < 1e9f) && (y < 1e9f);
   float xp = __fdiv_rn(x - s.x0, s.dx), yp = __fdiv_rn(y - s.y0, s.dy);
@@ -200,12 +211,12 @@ __device__ __forceinline__ void splat_square(const SensorK& s, float* hist, int 
       float w = expf(inv2s * (ddx * ddx + ddy * ddy)) * scale;
       int xi = xi0 + j - K, yi = yi0 + i - K;
       bool in = ok && xi >= 0 && xi < s.width && yi >= 0 && yi < s.height;
-      warp_add(hist, in ? rowbase + yi * s.width + xi : -1, w);
+      warp_add(sink, in ? rowbase + yi * s.width + xi : -1, w);
     }
 }
 
 // sensors/hexagonal.py:264-315 DifferentiableHexagonalSensor.accumulate
-__device__ __forceinline__ void splat_hex(const SensorK& s, const int* table, float* hist,
+__device__ __forceinline__ void splat_hex(const SensorK& s, const int* table, const Sink& sink,
                                           int rowbase, bool ok, float x, float y, float v) {
   ok = ok && (x < 1e9f) && (y < 1e9f);
   float xg, yg, qi, ri;
@@ -230,7 +241,7 @@ __device__ __forceinline__ void splat_hex(const SensorK& s, const int* table, fl
                           s.sigma);
       float w = expf(-0.5f * (a * a)) * scale;
       int p = ok ? hex_lookup(s, table, qi + (float)q, ri + (float)r) : -1;
-      warp_add(hist, p >= 0 ? rowbase + p : -1, w);
+      warp_add(sink, p >= 0 ? rowbase + p : -1, w);
     }
 }
 
@@ -312,13 +323,12 @@ __global__ void __launch_bounds__(256) k_render(const RenderK p) {
   ob.n_cyl = p.n_cyl; ob.n_box = p.n_box; ob.n_sph = p.n_sph; ob.n_obox = p.n_obox; ob.n_tri = p.n_tri;
   const float* mir = tab + to.mir;
   const int* table = p.hex_in_smem ? htab : p.hex_table;
-  float* hist = p.rows_in_smem ? sh_hist : p.out;
+  Sink sink;
+  sink.sh = p.rows_in_smem ? sh_hist : nullptr;
+  sink.g = p.acc;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = nthr >> 5;
   const int nch = (p.M + 31) >> 5;
-  int cur_sblk = -1;
-  int rl_key = -1;  // run-length merged hit of this lane (hard sensors)
-  float rl_val = 0.f;
 
   __syncthreads();
   for (;;) {
@@ -333,22 +343,8 @@ __global__ void __launch_bounds__(256) k_render(const RenderK p) {
     const int s0 = sblk * p.SB, f0 = fc * p.FC, c0 = cc * p.CC;
     const int SBc = min(p.SB, p.S - s0), FCc = min(p.FC, p.F - f0), CCc = min(p.CC, nch - c0);
 
-    if (MODE == IACT_MODE_RESPONSE && p.rows_in_smem && sblk != cur_sblk) {
-      // rows of the previous source block -> global, then clear
-      if (cur_sblk >= 0) {
-        const int cs0 = cur_sblk * p.SB, csb = min(p.SB, p.S - cs0);
-        for (int i = threadIdx.x; i < csb * p.P; i += nthr) {
-          float h = sh_hist[i];
-          if (h != 0.f) {
-            atomicAdd(p.out + (size_t)cs0 * p.P + i, h);
-            sh_hist[i] = 0.f;
-          }
-        }
-      }
-      cur_sblk = sblk;
-      __syncthreads();
-    }
-
+    int rl_key = -1;  // run-length merged hit of this lane (hard sensors)
+    float rl_val = 0.f;
     const int T = SBc * FCc * CCc;
     const int tb = (warp * T) / nw, te = ((warp + 1) * T) / nw;
     for (int t = tb; t < te; ++t) {
@@ -370,8 +366,8 @@ __global__ void __launch_bounds__(256) k_render(const RenderK p) {
       if (MODE == IACT_MODE_RESPONSE) rowbase = (p.rows_in_smem ? sl : s) * p.P;
       else rowbase = 0;
       if (SOFT) {
-        if (p.sn.type == IACT_SENSOR_SOFT_SQUARE) splat_square(p.sn, hist, rowbase, act, x, y, val);
-        else splat_hex(p.sn, table, hist, rowbase, act, x, y, val);
+        if (p.sn.type == IACT_SENSOR_SOFT_SQUARE) splat_square(p.sn, sink, rowbase, act, x, y, val);
+        else splat_hex(p.sn, table, sink, rowbase, act, x, y, val);
       } else if (act) {
         const int pix = (p.sn.type == IACT_SENSOR_SQUARE) ? bin_square(p.sn, x, y) : bin_hex(p.sn, table, x, y);
         if (pix >= 0 && val != 0.f) {
@@ -379,33 +375,34 @@ __global__ void __launch_bounds__(256) k_render(const RenderK p) {
           if (key == rl_key) {
             rl_val += val;
           } else {
-            if (rl_key >= 0) atomicAdd(hist + rl_key, rl_val);
+            if (rl_key >= 0) sink.add(rl_key, rl_val);
             rl_key = key;
             rl_val = val;
           }
         }
       }
     }
-    if (!SOFT && rl_key >= 0) {
-      atomicAdd(hist + rl_key, rl_val);
-      rl_key = -1;
-      rl_val = 0.f;
-    }
+    if (!SOFT && rl_key >= 0) sink.add(rl_key, rl_val);
     __syncthreads();
-  }
-  // final flush of the shared rows
-  if (p.rows_in_smem) {
-    int base = 0, nrows = 1;
-    if (MODE == IACT_MODE_RESPONSE) {
-      if (cur_sblk < 0) return;
-      base = cur_sblk * p.SB;
-      nrows = min(p.SB, p.S - base);
+    if (p.rows_in_smem) {
+      // this tile's FP32 rows -> FP64 accumulator, then clear for the next tile
+      const int base = (MODE == IACT_MODE_RESPONSE) ? s0 : 0;
+      const int nrows = (MODE == IACT_MODE_RESPONSE) ? SBc : 1;
+      for (int i = threadIdx.x; i < nrows * p.P; i += nthr) {
+        const float h = sh_hist[i];
+        if (h != 0.f) {
+          atomicAdd(p.acc + (size_t)base * p.P + i, (double)h);
+          sh_hist[i] = 0.f;
+        }
+      }
     }
-    for (int i = threadIdx.x; i < nrows * p.P; i += nthr) {
-      float h = sh_hist[i];
-      if (h != 0.f) atomicAdd(p.out + (size_t)base * p.P + i, h);
-    }
   }
+}
+
+// FP64 accumulator -> FP32 output
+__global__ void __launch_bounds__(256) k_finish(const double* __restrict__ acc, float* __restrict__ out, size_t n) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    out[i] = (float)acc[i];
 }
 
 template <int SRC, bool STAGES>
@@ -580,7 +577,7 @@ int dispatch_soft(bool soft, int mode, bool stages, RenderK p, int block, size_t
 
 }  // namespace
 
-WsLayout workspace_layout(const iact_scene_t* sc) {
+WsLayout workspace_layout(const iact_scene_t* sc, size_t acc_elems) {
   WsLayout L;
   TableOffsets to = table_offsets(sc->n_cyl, sc->n_box, sc->n_sph, sc->n_obox, sc->n_tri, sc->n_mirrors);
   L.n_table_floats = to.total;
@@ -594,27 +591,40 @@ WsLayout workspace_layout(const iact_scene_t* sc) {
   off = align256(off + sizeof(float4) * n);
   L.n4 = off;
   off = align256(off + sizeof(float4) * n);
+  L.acc = off;
+  off = align256(off + sizeof(double) * acc_elems);
   L.total = off;
   return L;
+}
+
+size_t acc_elems(const iact_sensor_t* sn, int S, int mode) {
+  if (mode == IACT_MODE_RESPONSE) return (size_t)std::max(S, 0) * (size_t)sn->n_pixels;
+  if (mode == IACT_MODE_IMAGE) return (size_t)sn->n_pixels;
+  return 0;
 }
 
 int launch_render(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type, const float* sources,
                   const float* values, int S, int mode, float* out, void* ws, size_t ws_bytes,
                   const iact_opts_t* opts, cudaStream_t st) {
-  const WsLayout L = workspace_layout(sc);
+  (void)ws_bytes;
+  const size_t n_acc = acc_elems(sn, S, mode);
+  const WsLayout L = workspace_layout(sc, n_acc);
   char* w = static_cast<char*>(ws);
   const size_t P = (size_t)sn->n_pixels;
-  const size_t out_n = (mode == IACT_MODE_RESPONSE) ? (size_t)S * P : P;
-  int rc = check_cuda(cudaMemsetAsync(out, 0, out_n * sizeof(float), st), "zero output");
-  if (rc) return rc;
-  if (S == 0 || sc->n_facets == 0 || sc->n_samples == 0) return IACT_OK;
+  int rc;
+  if (S == 0 || sc->n_facets == 0 || sc->n_samples == 0) {
+    if (n_acc) return check_cuda(cudaMemsetAsync(out, 0, n_acc * sizeof(float), st), "zero output");
+    return IACT_OK;
+  }
   rc = check_cuda(cudaMemsetAsync(w + L.counter, 0, 64, st), "reset tile counter");
+  if (rc) return rc;
+  rc = check_cuda(cudaMemsetAsync(w + L.acc, 0, n_acc * sizeof(double), st), "zero accumulator");
   if (rc) return rc;
   rc = launch_prep(sc, L, w, st);
   if (rc) return rc;
 
   RenderK p = base_params(sc, sn, L, w, sources, values, S);
-  p.out = out;
+  p.acc = reinterpret_cast<double*>(w + L.acc);
   int block = (opts && opts->block_threads > 0) ? opts->block_threads : 256;
   if (block % 32 || block > 256) return set_error(IACT_E_INVALID, "opts.block_threads must be a multiple of 32, <= 256");
   const int nw = block / 32;
@@ -652,8 +662,12 @@ int launch_render(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type,
   const bool soft = (sn->type == IACT_SENSOR_SOFT_SQUARE || sn->type == IACT_SENSOR_SOFT_HEX);
   const bool stages = sc->n_mirrors > 0;
   void* const* ev = opts ? opts->kernel_events : nullptr;
-  return src_type == IACT_SRC_POINT ? dispatch_soft<IACT_SRC_POINT>(soft, mode, stages, p, block, smem, st, ev)
-                                    : dispatch_soft<IACT_SRC_PARALLEL>(soft, mode, stages, p, block, smem, st, ev);
+  rc = src_type == IACT_SRC_POINT ? dispatch_soft<IACT_SRC_POINT>(soft, mode, stages, p, block, smem, st, ev)
+                                  : dispatch_soft<IACT_SRC_PARALLEL>(soft, mode, stages, p, block, smem, st, ev);
+  if (rc) return rc;
+  const int fb = (int)std::min<size_t>((n_acc + 255) / 256, 4096);
+  k_finish<<<std::max(fb, 1), 256, 0, st>>>(p.acc, out, n_acc);
+  return check_cuda(cudaGetLastError(), "k_finish launch");
 }
 
 int launch_debug(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type, const float* sources,
@@ -661,7 +675,7 @@ int launch_debug(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type, 
                  void* ws, size_t ws_bytes, cudaStream_t st) {
   (void)ws_bytes;
   if (S == 0 || sc->n_facets == 0 || sc->n_samples == 0) return IACT_OK;
-  const WsLayout L = workspace_layout(sc);
+  const WsLayout L = workspace_layout(sc, 0);
   char* w = static_cast<char*>(ws);
   int rc = launch_prep(sc, L, w, st);
   if (rc) return rc;

@@ -56,7 +56,7 @@ extern "C" {
 #define IACT_MAX_OBSTRUCTIONS 2048 /* primitives over all obstruction kinds */
 
 enum { IACT_SRC_POINT = 0, IACT_SRC_PARALLEL = 1 };
-enum { IACT_MODE_IMAGE = 0, IACT_MODE_RESPONSE = 1 };
+enum { IACT_MODE_IMAGE = 0, IACT_MODE_RESPONSE = 1, IACT_MODE_DEBUG = 2 };
 enum {
   IACT_SENSOR_SQUARE = 0,      /* sensors/square.py:28-91     SquareSensor */
   IACT_SENSOR_HEX = 1,         /* sensors/hexagonal.py:104-194 HexagonalSensor */
@@ -148,13 +148,18 @@ int iact_abi_layout(size_t* out, int n);
  * one float per thread to out[blocks*256]. */
 int iact_probe_fma(float* out, int32_t blocks, int32_t iters, void* stream);
 
-/* Bytes of scratch needed by iact_render / iact_render_debug /
- * iact_render_backward for this scene. */
-int iact_workspace_size(const iact_scene_t* scene, size_t* bytes);
+/* Bytes of scratch needed by a call of the given mode (IMAGE / RESPONSE:
+ * iact_render, DEBUG: iact_render_debug) on this scene, sensor and source
+ * count. Holds the world-space samples, the per-launch tables and the FP64
+ * accumulator of the image or matrix. */
+int iact_workspace_size(const iact_scene_t* scene, const iact_sensor_t* sensor,
+                        int32_t n_sources, int32_t mode, size_t* bytes);
 
 /* Forward render.
- *   mode IMAGE:    out[n_pixels]            (zeroed by the callee)
+ *   mode IMAGE:    out[n_pixels]            (fully written by the callee)
  *   mode RESPONSE: out[n_sources, n_pixels] (fully written by the callee)
+ * Hits are summed per work tile in FP32 shared memory, across tiles in an
+ * FP64 accumulator, and rounded to FP32 once at the end.
  * sources [S,3]: positions (POINT) or propagation directions (PARALLEL,
  * used as given, not normalised); values [S]. */
 int iact_render(const iact_scene_t* scene, const iact_sensor_t* sensor,

@@ -31,16 +31,26 @@ def test_layout_and_version(built):
     assert built.iact_abi_version() == 1
 
 
+def _square(n=4):
+    sn = N.IactSensor()
+    sn.type, sn.n_pixels, sn.width, sn.height, sn.dx, sn.dy = N.SENSOR_SQUARE, n * n, n, n, 0.1, 0.1
+    return sn
+
+
 def test_workspace_size_and_validation(built):
-    sc = N.IactScene()
+    sc, sn = N.IactScene(), _square()
     sz = ctypes.c_size_t(0)
-    assert built.iact_workspace_size(ctypes.byref(sc), ctypes.byref(sz)) == 0 and sz.value > 0
+    ws = lambda S, mode: built.iact_workspace_size(ctypes.byref(sc), ctypes.byref(sn), S, mode, ctypes.byref(sz))
+    assert ws(0, N.MODE_IMAGE) == 0 and sz.value > 0
+    img = sz.value
+    assert ws(100, N.MODE_RESPONSE) == 0 and sz.value >= img + 100 * 16 * 8 - 256
+    assert ws(3, 7) == N.IACT_E_INVALID
     sc.n_facets, sc.n_samples = 4, 8  # arrays missing
-    assert built.iact_workspace_size(ctypes.byref(sc), ctypes.byref(sz)) == N.IACT_E_INVALID
+    assert ws(1, N.MODE_IMAGE) == N.IACT_E_INVALID
     assert b"non-NULL" in built.iact_last_error()
     sc = N.IactScene()
     sc.n_cyl = 3  # table missing
-    assert built.iact_workspace_size(ctypes.byref(sc), ctypes.byref(sz)) == N.IACT_E_INVALID
+    assert ws(1, N.MODE_IMAGE) == N.IACT_E_INVALID
 
 
 def test_render_rejects_bad_arguments_before_any_cuda_call(built):
