@@ -47,6 +47,20 @@ struct MirRec {
 };
 static_assert(sizeof(MirRec) == kMirF * sizeof(float), "MirRec layout");
 
+// Hardware approximations (PTX rcp.approx / sqrt.approx, <= 1 ulp-ish).
+// Used where the value only feeds a hit/miss comparison or a sensor-plane
+// coordinate whose error stays far inside the pixel-edge band.
+__device__ __forceinline__ float rcp_a(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+__device__ __forceinline__ float sqrt_a(float x) {
+  float r;
+  asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
 struct V3 {
   float x, y, z;
 };
@@ -100,35 +114,35 @@ __device__ __forceinline__ bool cyl_shadows(const float* c, V3 o, V3 d) {
   float b = 2.f * dot(ocp, rdp);
   float cc = dot(ocp, ocp) - r2;
   float disc = b * b - 4.f * a * cc;
-  float sq = sqrtf(fmaxf(disc, 0.f));
-  float inv2a = __frcp_rn(2.f * a + kEps);
+  float sq = sqrt_a(fmaxf(disc, 0.f));
+  float inv2a = rcp_a(2.f * a + kEps);
   float t1 = (-b - sq) * inv2a;
   float t2 = (-b + sq) * inv2a;
   float y1 = fmaf(t1, rda, oca), y2 = fmaf(t2, rda, oca);
-  bool hit = (disc >= 0.f) && (((t1 > kEps) && (y1 >= 0.f) && (y1 <= h) && (t1 < kBig)) ||
-                               ((t2 > kEps) && (y2 >= 0.f) && (y2 <= h) && (t2 < kBig)));
-  float invr = __frcp_rn(rda + kEps);
+  bool h1 = (t1 > kEps) & (y1 >= 0.f) & (y1 <= h) & (t1 < kBig);
+  bool h2 = (t2 > kEps) & (y2 >= 0.f) & (y2 <= h) & (t2 < kBig);
+  bool hit = (disc >= 0.f) & (h1 | h2);
+  float invr = rcp_a(rda + kEps);
   float tb = -oca * invr;
   float tt = (h - oca) * invr;
   V3 pb = ocp + tb * rdp, pt = ocp + tt * rdp;
-  hit = hit || ((tb > kEps) && (dot(pb, pb) <= r2) && (tb < kBig));
-  hit = hit || ((tt > kEps) && (dot(pt, pt) <= r2) && (tt < kBig));
+  hit |= (tb > kEps) & (dot(pb, pb) <= r2) & (tb < kBig);
+  hit |= (tt > kEps) & (dot(pt, pt) <= r2) & (tt < kBig);
   return hit;
 }
 
 // core/intersections.py:90-110 intersect_box; jnp.minimum/maximum propagate
 // NaN, so a NaN slab value means no hit.
 __device__ __forceinline__ bool box_shadows(const float* bx, V3 o, V3 d) {
-  float ix = __frcp_rn(d.x + kEps), iy = __frcp_rn(d.y + kEps), iz = __frcp_rn(d.z + kEps);
+  float ix = rcp_a(d.x + kEps), iy = rcp_a(d.y + kEps), iz = rcp_a(d.z + kEps);
   float x1 = (bx[0] - o.x) * ix, x2 = (bx[3] - o.x) * ix;
   float y1 = (bx[1] - o.y) * iy, y2 = (bx[4] - o.y) * iy;
   float z1 = (bx[2] - o.z) * iz, z2 = (bx[5] - o.z) * iz;
-  bool nan = isnan(x1) || isnan(x2) || isnan(y1) || isnan(y2) || isnan(z1) || isnan(z2);
+  bool nan = isnan(x1) | isnan(x2) | isnan(y1) | isnan(y2) | isnan(z1) | isnan(z2);
   float tmin = fmaxf(fmaxf(fminf(x1, x2), fminf(y1, y2)), fminf(z1, z2));
   float tmax = fminf(fminf(fmaxf(x1, x2), fmaxf(y1, y2)), fmaxf(z1, z2));
-  bool hit = (tmax >= tmin) && (tmax > kEps) && !nan;
   float tr = (tmin > kEps) ? tmin : tmax;
-  return hit && (tr < kBig);
+  return (tmax >= tmin) & (tmax > kEps) & !nan & (tr < kBig);
 }
 
 // core/intersections.py:195-226 intersect_sphere
@@ -138,10 +152,10 @@ __device__ __forceinline__ bool sph_shadows(const float* s, V3 o, V3 d) {
   float b = 2.f * dot(oc, d);
   float c = dot(oc, oc) - s[3];
   float disc = b * b - 4.f * a * c;
-  float sq = sqrtf(fmaxf(disc, 0.f));
-  float inv2a = __frcp_rn(2.f * a + kEps);
+  float sq = sqrt_a(fmaxf(disc, 0.f));
+  float inv2a = rcp_a(2.f * a + kEps);
   float t1 = (-b - sq) * inv2a, t2 = (-b + sq) * inv2a;
-  return (disc >= 0.f) && (((t1 > kEps) && (t1 < kBig)) || ((t2 > kEps) && (t2 < kBig)));
+  return (disc >= 0.f) & (((t1 > kEps) & (t1 < kBig)) | ((t2 > kEps) & (t2 < kBig)));
 }
 
 __device__ __forceinline__ float sgnf(float v) { return v > 0.f ? 1.f : (v < 0.f ? -1.f : 0.f); }
@@ -151,18 +165,17 @@ __device__ __forceinline__ bool obox_shadows(const float* b, V3 o, V3 d) {
   const float* R = b + 6;
   V3 lo = rtmul(R, o - mk(b[0], b[1], b[2]));
   V3 ld = rtmul(R, d);
-  float ix = __frcp_rn(ld.x + kEps * sgnf(ld.x + kEps));
-  float iy = __frcp_rn(ld.y + kEps * sgnf(ld.y + kEps));
-  float iz = __frcp_rn(ld.z + kEps * sgnf(ld.z + kEps));
+  float ix = rcp_a(ld.x + kEps * sgnf(ld.x + kEps));
+  float iy = rcp_a(ld.y + kEps * sgnf(ld.y + kEps));
+  float iz = rcp_a(ld.z + kEps * sgnf(ld.z + kEps));
   float x1 = (-b[3] - lo.x) * ix, x2 = (b[3] - lo.x) * ix;
   float y1 = (-b[4] - lo.y) * iy, y2 = (b[4] - lo.y) * iy;
   float z1 = (-b[5] - lo.z) * iz, z2 = (b[5] - lo.z) * iz;
-  bool nan = isnan(x1) || isnan(x2) || isnan(y1) || isnan(y2) || isnan(z1) || isnan(z2);
+  bool nan = isnan(x1) | isnan(x2) | isnan(y1) | isnan(y2) | isnan(z1) | isnan(z2);
   float tmin = fmaxf(fmaxf(fminf(x1, x2), fminf(y1, y2)), fminf(z1, z2));
   float tmax = fminf(fminf(fmaxf(x1, x2), fmaxf(y1, y2)), fmaxf(z1, z2));
-  bool hit = (tmax >= tmin) && (tmax > kEps) && !nan;
   float tr = (tmin > kEps) ? tmin : tmax;
-  return hit && (tr > kEps) && (tr < kBig);
+  return (tmax >= tmin) & (tmax > kEps) & !nan & (tr > kEps) & (tr < kBig);
 }
 
 // core/intersections.py:152-192 intersect_triangle (Moller-Trumbore)
@@ -171,14 +184,13 @@ __device__ __forceinline__ bool tri_shadows(const float* t, V3 o, V3 d) {
   V3 h = mk(d.y * e2.z - d.z * e2.y, d.z * e2.x - d.x * e2.z, d.x * e2.y - d.y * e2.x);
   float a = dot(e1, h);
   bool parallel = fabsf(a) < kEps;
-  float f = __frcp_rn(a + kEps * sgnf(a + kEps));
+  float f = rcp_a(a + kEps * sgnf(a + kEps));
   V3 s = o - v0;
   float u = f * dot(s, h);
   V3 q = mk(s.y * e1.z - s.z * e1.y, s.z * e1.x - s.x * e1.z, s.x * e1.y - s.y * e1.x);
   float v = f * dot(d, q);
   float tt = f * dot(e2, q);
-  return !parallel && (u >= 0.f) && (u <= 1.f) && (v >= 0.f) && (u + v <= 1.f) && (tt > kEps) &&
-         (tt < kBig);
+  return !parallel & (u >= 0.f) & (u <= 1.f) & (v >= 0.f) & (u + v <= 1.f) & (tt > kEps) & (tt < kBig);
 }
 
 // Shadow-table view (shared memory). Counts are CTA-uniform.
@@ -213,6 +225,8 @@ struct SensorK {
   float R[9];
   float pos[3];
   float x0, y0, dx, dy, edge_width;
+  float inv_dx, inv_dy;               // 1/dx, 1/dy
+  float hq_x, hq_y, hr_y, inv_inr;    // sqrt(3)/3/size, 1/(3 size), 2/(3 size), 1/inradius
   float hex_size, inradius, gc, gs, off_x, off_y, hex_sx, hex_sy, edge_threshold;
   int q_min, r_min, table_q, table_r;
   float sigma;
@@ -225,7 +239,7 @@ __device__ __forceinline__ void plane_hit(const SensorK& s, V3 o, V3 d, float& x
   V3 c = mk(s.pos[0], s.pos[1], s.pos[2]);
   float ndotd = dot(d, n), ndoto = dot(o, n), ndotp = dot(n, c);
   bool parallel = fabsf(ndotd) < 1e-10f;
-  float t = __fdiv_rn(ndotp - ndoto, parallel ? 1.f : ndotd);
+  float t = (ndotp - ndoto) * rcp_a(parallel ? 1.f : ndotd);
   V3 op = (o + t * d) - c;
   bool invalid = parallel || (t <= 0.f);
   x = invalid ? kBig : dot(op, u1);
@@ -234,7 +248,7 @@ __device__ __forceinline__ void plane_hit(const SensorK& s, V3 o, V3 d, float& x
 
 // sensors/square.py:66-91 SquareSensor.accumulate: pixel id or -1
 __device__ __forceinline__ int bin_square(const SensorK& s, float x, float y) {
-  float xc = __fdiv_rn(x - s.x0, s.dx), yc = __fdiv_rn(y - s.y0, s.dy);
+  float xc = (x - s.x0) * s.inv_dx, yc = (y - s.y0) * s.inv_dy;
   float xf = floorf(xc), yf = floorf(yc);
   // compare in float: out-of-range and NaN fail, as the int32 cast would
   bool valid = (xf >= 0.f) && (xf < (float)s.width) && (yf >= 0.f) && (yf < (float)s.height);
@@ -251,8 +265,9 @@ __device__ __forceinline__ void hex_axial(const SensorK& s, float x, float y, fl
   float xs = x - s.off_x, ys = y - s.off_y;
   xg = s.gc * xs - s.gs * ys;
   yg = s.gs * xs + s.gc * ys;
-  float q = __fdiv_rn(SQRT3_3 * xg - __fdiv_rn(yg, 3.f), s.hex_size);
-  float r = __fdiv_rn(__fdiv_rn(2.f * yg, 3.f), s.hex_size);
+  (void)SQRT3_3;
+  float q = fmaf(s.hq_x, xg, -s.hq_y * yg);  // (sqrt(3)/3 x - y/3) / size
+  float r = s.hr_y * yg;                      // (2 y / 3) / size
   float sv = -q - r;
   qi = rintf(q);
   ri = rintf(r);
@@ -263,27 +278,29 @@ __device__ __forceinline__ void hex_axial(const SensorK& s, float x, float y, fl
 }
 
 // sensors/hexagonal.py:155-172 _lookup_pixels over a table in shared memory
-__device__ __forceinline__ int hex_lookup(const SensorK& s, const int* table, float qi, float ri) {
+template <typename TT>
+__device__ __forceinline__ int hex_lookup(const SensorK& s, const TT* table, float qi, float ri) {
   float qx = qi - (float)s.q_min, rx = ri - (float)s.r_min;
-  if (!((qx >= 0.f) && (qx < (float)s.table_q) && (rx >= 0.f) && (rx < (float)s.table_r))) return -1;
-  int p = table[(int)qx * s.table_r + (int)rx];
+  bool in = (qx >= 0.f) & (qx < (float)s.table_q) & (rx >= 0.f) & (rx < (float)s.table_r);
+  int p = in ? (int)table[(int)qx * s.table_r + (int)rx] : -1;
   return p >= 0 ? p : -1;
 }
 
 // sensors/hexagonal.py:42-47 _hex_norm
-__device__ __forceinline__ float hex_norm(float x, float y, float inr) {
+__device__ __forceinline__ float hex_norm(float x, float y, float inv_inr) {
   float ax = fabsf(x), ay = fabsf(y);
-  return __fdiv_rn(fmaxf(ax, 0.5f * ax + 0.8660254037844386f * ay), inr);
+  return fmaxf(ax, 0.5f * ax + 0.8660254037844386f * ay) * inv_inr;
 }
 
 // sensors/hexagonal.py:174-194 HexagonalSensor.accumulate: pixel id or -1
-__device__ __forceinline__ int bin_hex(const SensorK& s, const int* table, float x, float y) {
+template <typename TT>
+__device__ __forceinline__ int bin_hex(const SensorK& s, const TT* table, float x, float y) {
   float xg, yg, qi, ri;
   hex_axial(s, x, y, xg, yg, qi, ri);
   int p = hex_lookup(s, table, qi, ri);
   float hcx = s.hex_sx * (qi + 0.5f * ri);
   float hcy = s.hex_sy * ri;
-  float hd = hex_norm(xg - hcx, yg - hcy, s.inradius);
+  float hd = hex_norm(xg - hcx, yg - hcy, s.inv_inr);
   return (hd > s.edge_threshold) ? -1 : p;
 }
 

@@ -192,7 +192,7 @@ __device__ __forceinline__ void warp_add(const Sink& sink, int key, float v) {
 __device__ __forceinline__ void splat_square(const SensorK& s, const Sink& sink, int rowbase, bool ok,
                                              float x, float y, float v) {
   ok = ok && (x < 1e9f) && (y < 1e9f);
-  float xp = __fdiv_rn(x - s.x0, s.dx), yp = __fdiv_rn(y - s.y0, s.dy);
+  float xp = (x - s.x0) * s.inv_dx, yp = (y - s.y0) * s.inv_dy;
   float xb = floorf(xp), yb = floorf(yp);
   float xf = xp - xb, yf = yp - yb;
   const int K = s.kernel_size, n = 2 * K + 1;
@@ -216,29 +216,29 @@ __device__ __forceinline__ void splat_square(const SensorK& s, const Sink& sink,
 }
 
 // sensors/hexagonal.py:264-315 DifferentiableHexagonalSensor.accumulate
-__device__ __forceinline__ void splat_hex(const SensorK& s, const int* table, const Sink& sink,
+template <typename TT>
+__device__ __forceinline__ void splat_hex(const SensorK& s, const TT* table, const Sink& sink,
                                           int rowbase, bool ok, float x, float y, float v) {
   ok = ok && (x < 1e9f) && (y < 1e9f);
   float xg, yg, qi, ri;
   hex_axial(s, ok ? x : 0.f, ok ? y : 0.f, xg, yg, qi, ri);
   float ddx = xg - s.hex_sx * (qi + 0.5f * ri), ddy = yg - s.hex_sy * ri;
   const int K = s.kernel_size;
+  const float inv_sig = 1.f / s.sigma;
   float tot = 0.f;
   for (int q = -K; q <= K; ++q)
     for (int r = -K; r <= K; ++r) {
       if (max(max(abs(q), abs(r)), abs(q + r)) > K) continue;
-      float a = __fdiv_rn(hex_norm(ddx - s.hex_sx * ((float)q + 0.5f * (float)r), ddy - s.hex_sy * (float)r,
-                                   s.inradius),
-                          s.sigma);
+      float a = hex_norm(ddx - s.hex_sx * ((float)q + 0.5f * (float)r), ddy - s.hex_sy * (float)r, s.inv_inr) *
+                inv_sig;
       tot += expf(-0.5f * (a * a));
     }
   const float scale = ok ? v / tot : 0.f;
   for (int q = -K; q <= K; ++q)
     for (int r = -K; r <= K; ++r) {
       if (max(max(abs(q), abs(r)), abs(q + r)) > K) continue;
-      float a = __fdiv_rn(hex_norm(ddx - s.hex_sx * ((float)q + 0.5f * (float)r), ddy - s.hex_sy * (float)r,
-                                   s.inradius),
-                          s.sigma);
+      float a = hex_norm(ddx - s.hex_sx * ((float)q + 0.5f * (float)r), ddy - s.hex_sy * (float)r, s.inv_inr) *
+                inv_sig;
       float w = expf(-0.5f * (a * a)) * scale;
       int p = ok ? hex_lookup(s, table, qi + (float)q, ri + (float)r) : -1;
       warp_add(sink, p >= 0 ? rowbase + p : -1, w);
@@ -304,16 +304,16 @@ __global__ void __launch_bounds__(256) k_render(const RenderK p) {
   extern __shared__ __align__(16) float smem[];
   __shared__ int s_tile;
   const int tab_n = (p.n_table_floats + 3) & ~3;
-  const int htab_n = p.hex_in_smem ? ((p.sn.table_q * p.sn.table_r + 3) & ~3) : 0;
+  const int htab_n = p.hex_in_smem ? ((p.sn.table_q * p.sn.table_r + 7) & ~7) : 0;  // int16 entries
   float* tab = smem;
-  int* htab = reinterpret_cast<int*>(smem + tab_n);
-  float* sh_hist = smem + tab_n + htab_n;
+  short* htab = reinterpret_cast<short*>(smem + tab_n);
+  float* sh_hist = smem + tab_n + htab_n / 2;
   const int hist_n = p.rows_in_smem * p.P;
   const int nthr = blockDim.x;
 
   for (int i = threadIdx.x; i < p.n_table_floats; i += nthr) tab[i] = p.tables[i];
   for (int i = threadIdx.x; i < htab_n; i += nthr)
-    htab[i] = i < p.sn.table_q * p.sn.table_r ? p.hex_table[i] : -1;
+    htab[i] = (short)(i < p.sn.table_q * p.sn.table_r ? p.hex_table[i] : -1);
   for (int i = threadIdx.x; i < hist_n; i += nthr) sh_hist[i] = 0.f;
 
   const TableOffsets to = table_offsets(p.n_cyl, p.n_box, p.n_sph, p.n_obox, p.n_tri, p.n_mir);
@@ -322,7 +322,6 @@ __global__ void __launch_bounds__(256) k_render(const RenderK p) {
   ob.obox = tab + to.obox; ob.tri = tab + to.tri;
   ob.n_cyl = p.n_cyl; ob.n_box = p.n_box; ob.n_sph = p.n_sph; ob.n_obox = p.n_obox; ob.n_tri = p.n_tri;
   const float* mir = tab + to.mir;
-  const int* table = p.hex_in_smem ? htab : p.hex_table;
   Sink sink;
   sink.sh = p.rows_in_smem ? sh_hist : nullptr;
   sink.g = p.acc;
@@ -347,11 +346,12 @@ __global__ void __launch_bounds__(256) k_render(const RenderK p) {
     float rl_val = 0.f;
     const int T = SBc * FCc * CCc;
     const int tb = (warp * T) / nw, te = ((warp + 1) * T) / nw;
+    // task t = (source sl, facet fl, chunk cl), chunk fastest; decoded once
+    int sl = tb / (FCc * CCc);
+    int fl = (tb - sl * FCc * CCc) / CCc;
+    int cl = tb - sl * FCc * CCc - fl * CCc;
     for (int t = tb; t < te; ++t) {
-      const int sl = t / (FCc * CCc);
-      const int rem = t - sl * FCc * CCc;
-      const int fl = rem / CCc;
-      const int m = (c0 + rem - fl * CCc) * 32 + lane;
+      const int m = (c0 + cl) * 32 + lane;
       const int s = s0 + sl, f = f0 + fl;
       const bool act = m < p.M;
       const V3 src = mk(__ldg(p.sources + 3 * s), __ldg(p.sources + 3 * s + 1), __ldg(p.sources + 3 * s + 2));
@@ -367,10 +367,12 @@ __global__ void __launch_bounds__(256) k_render(const RenderK p) {
       else rowbase = 0;
       if (SOFT) {
         if (p.sn.type == IACT_SENSOR_SOFT_SQUARE) splat_square(p.sn, sink, rowbase, act, x, y, val);
-        else splat_hex(p.sn, table, sink, rowbase, act, x, y, val);
+        else if (p.hex_in_smem) splat_hex(p.sn, htab, sink, rowbase, act, x, y, val);
+        else splat_hex(p.sn, p.hex_table, sink, rowbase, act, x, y, val);
       } else if (act) {
-        const int pix = (p.sn.type == IACT_SENSOR_SQUARE) ? bin_square(p.sn, x, y) : bin_hex(p.sn, table, x, y);
-        if (pix >= 0 && val != 0.f) {
+        const int pix = (p.sn.type == IACT_SENSOR_SQUARE) ? bin_square(p.sn, x, y)
+                        : (p.hex_in_smem ? bin_hex(p.sn, htab, x, y) : bin_hex(p.sn, p.hex_table, x, y));
+        if ((pix >= 0) & (val != 0.f)) {
           const int key = rowbase + pix;
           if (key == rl_key) {
             rl_val += val;
@@ -379,6 +381,13 @@ __global__ void __launch_bounds__(256) k_render(const RenderK p) {
             rl_key = key;
             rl_val = val;
           }
+        }
+      }
+      if (++cl == CCc) {
+        cl = 0;
+        if (++fl == FCc) {
+          fl = 0;
+          ++sl;
         }
       }
     }
@@ -498,6 +507,15 @@ SensorK make_sensor(const iact_sensor_t* s) {
   k.q_min = s->q_min; k.r_min = s->r_min; k.table_q = s->table_q; k.table_r = s->table_r;
   k.sigma = s->sigma;
   k.kernel_size = s->kernel_size;
+  k.inv_dx = s->dx > 0.f ? (float)(1.0 / (double)s->dx) : 0.f;
+  k.inv_dy = s->dy > 0.f ? (float)(1.0 / (double)s->dy) : 0.f;
+  if (s->hex_size > 0.f) {
+    const double sz = s->hex_size;
+    k.hq_x = (float)(0.5773502691896257 / sz);
+    k.hq_y = (float)(1.0 / (3.0 * sz));
+    k.hr_y = (float)(2.0 / (3.0 * sz));
+  }
+  k.inv_inr = s->inradius > 0.f ? (float)(1.0 / (double)s->inradius) : 0.f;
   return k;
 }
 
@@ -629,7 +647,10 @@ int launch_render(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type,
   if (block % 32 || block > 256) return set_error(IACT_E_INVALID, "opts.block_threads must be a multiple of 32, <= 256");
   const int nw = block / 32;
   const int nch = (p.M + 31) / 32;
-  int SB = (opts && opts->sources_per_cta > 0) ? opts->sources_per_cta : std::min(S, nw);
+  // a response tile keeps one FP32 shared-memory row per source: two warps per
+  // source halves that footprint and doubles the CTAs an SM holds
+  int SB = (opts && opts->sources_per_cta > 0) ? opts->sources_per_cta
+                                               : std::min(S, mode == IACT_MODE_RESPONSE ? std::max(1, nw / 2) : nw);
   SB = std::min(SB, S);
   const int target = nw * 48;  // warp tasks (32 rays each) per tile
   int CC = std::min(nch, std::max(1, target / SB));
@@ -647,8 +668,8 @@ int launch_render(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type,
   const size_t tab_bytes = sizeof(float) * (size_t)((L.n_table_floats + 3) & ~3);
   const bool hex = (sn->type == IACT_SENSOR_HEX || sn->type == IACT_SENSOR_SOFT_HEX);
   const size_t htab_elems = hex ? (size_t)sn->table_q * sn->table_r : 0;
-  size_t htab_bytes = sizeof(int) * ((htab_elems + 3) & ~(size_t)3);
-  p.hex_in_smem = (hex && tab_bytes + htab_bytes <= budget / 2) ? 1 : 0;
+  size_t htab_bytes = sizeof(short) * ((htab_elems + 7) & ~(size_t)7);
+  p.hex_in_smem = (hex && sn->n_pixels < 32768 && tab_bytes + htab_bytes <= budget / 2) ? 1 : 0;
   if (!p.hex_in_smem) htab_bytes = 0;
   if (tab_bytes + htab_bytes > budget) return set_error(IACT_E_UNSUPPORTED, "scene tables exceed shared memory");
   const int rows = (mode == IACT_MODE_RESPONSE) ? SB : 1;
