@@ -167,6 +167,21 @@ int iact_render(const iact_scene_t* scene, const iact_sensor_t* sensor,
                 int32_t n_sources, int32_t mode, float* out, void* workspace,
                 size_t workspace_bytes, const iact_opts_t* opts, void* stream);
 
+/* Forward render without a caller workspace; it has no counterpart in the
+ * reference (JAX allocates internally). For callers that cannot allocate
+ * device memory (device memory owned by another framework's pool, real-time
+ * acquisition loops that must not allocate): the scratch is a fixed
+ * IACT_NOALLOC_SCRATCH_BYTES array inside the library, held by every GPU
+ * that loads it until exit. Larger requests fail with IACT_E_UNSUPPORTED.
+ * The first call per device resolves the array's address (make it before
+ * any stream capture); calls overlapping on the GPU race on the shared
+ * array. Arguments and results as iact_render. */
+#define IACT_NOALLOC_SCRATCH_BYTES (16u << 20)
+int iact_render_noalloc(const iact_scene_t* scene, const iact_sensor_t* sensor,
+                        int32_t source_type, const float* sources,
+                        const float* values, int32_t n_sources, int32_t mode,
+                        float* out, const iact_opts_t* opts, void* stream);
+
 /* Per-ray hits in the reference's order, ray = (f*S + s)*M + m:
  *   pts [F*S*M,2] sensor-plane (x, y) or (1e10, 1e10); vals [F*S*M];
  *   pix [F*S*M] hard pixel id or -1 (may be NULL);
