@@ -270,6 +270,34 @@ def main():
     step_s = sum(a.elapsed_time(b) for a, b in ev) / 1e3 / args.steps
     kern_s = sum(a.elapsed_time(b) for a, b in kev) / 1e3 / args.steps
 
+    # forward + adjoint through torch.autograd (recompute-based adjoint kernel)
+    grp = tel.mirror_groups[0]
+    rot = grp.rotations.clone().to(dev).requires_grad_(True)
+    pos = grp.positions.clone().to(dev).requires_grad_(True)
+    tel_g = tel.set_mirror_rotations(0, rot).set_mirror_positions(0, pos)
+    src_g = src.clone().requires_grad_(True)
+    val_g = val.clone().requires_grad_(True)
+    gout = torch.randn(out.shape, device=dev, generator=torch.Generator(device=dev).manual_seed(0))
+    fwdadj = None
+    try:
+        for _ in range(2):
+            fn(tel_g, src_g, val_g, stype).backward(gout)
+        torch.cuda.synchronize(dev)
+        fa_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                 for _ in range(args.steps)]
+        for k in range(args.steps):
+            flush_buf.fill_(float(k))
+            fa_ev[k][0].record(stream)
+            fn(tel_g, src_g, val_g, stype).backward(gout)
+            fa_ev[k][1].record(stream)
+        torch.cuda.synchronize(dev)
+        fa_s = sum(a.elapsed_time(b) for a, b in fa_ev) / 1e3 / args.steps
+        fwdadj = {"value": rays / fa_s, "unit": "rays/s", "ms_per_step": fa_s * 1e3,
+                  "time_ratio_vs_fwd": fa_s / step_s,
+                  "grads": "facet rotations and positions, sources, values"}
+    except NotImplementedError as e:
+        fwdadj = {"unavailable": str(e)}
+
     # e2e through the public API with host buffers
     src_pin = src_h.pin_memory()
     val_pin = val_h.pin_memory()
@@ -308,6 +336,7 @@ def main():
                      "traffic": None, "kernel": "k_render", "kernel_ms": kern_s * 1e3,
                      "flops_per_ray": F_RAY[args.workload],
                      "peak_source": "measured live: FP32 FMA-chain probe kernel (iact_probe_fma)"},
+        "fwd_adjoint": fwdadj,
         "gpu_launches": 3 * args.steps,  # k_prep, k_render, k_finish per step
         "clocks": clk,
     }

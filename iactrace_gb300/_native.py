@@ -31,6 +31,7 @@ SRC_PARALLEL = 1
 MODE_IMAGE = 0
 MODE_RESPONSE = 1
 MODE_DEBUG = 2
+MODE_BACKWARD = 3
 SENSOR_SQUARE = 0
 SENSOR_HEX = 1
 SENSOR_SOFT_SQUARE = 2
@@ -107,6 +108,10 @@ _SIGS = {
                      _i, _i, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(IactOpts),
                      ctypes.c_void_p], ctypes.c_int),
     "iact_probe_fma": ([ctypes.c_void_p, _i, _i, ctypes.c_void_p], ctypes.c_int),
+    "iact_render_backward": ([ctypes.POINTER(IactScene), ctypes.POINTER(IactSensor), _i, ctypes.c_void_p,
+                              ctypes.c_void_p, _i, _i, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                              ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                              ctypes.POINTER(IactOpts), ctypes.c_void_p], ctypes.c_int),
     "iact_render_debug": ([ctypes.POINTER(IactScene), ctypes.POINTER(IactSensor), _i, ctypes.c_void_p,
                            ctypes.c_void_p, _i, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                            ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p], ctypes.c_int),

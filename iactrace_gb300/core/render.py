@@ -40,6 +40,82 @@ def _workspace(ps, sdesc, S, mode, device):
     return torch.empty(max(ps.workspace_bytes(sdesc, S, mode), 256), dtype=torch.uint8, device=device)
 
 
+def _forward(ps, desc, sdesc, code, src, val, mode, shape, opts, device):
+    out = torch.empty(shape, dtype=torch.float32, device=device)
+    ws = _workspace(ps, sdesc, src.shape[0], mode, device)
+    stream = torch.cuda.current_stream(device).cuda_stream
+    N.check(N.load().iact_render(ctypes.byref(desc), ctypes.byref(sdesc), code, src.data_ptr(), val.data_ptr(),
+                                 int(src.shape[0]), mode, out.data_ptr(), ws.data_ptr(), ws.numel(),
+                                 ctypes.byref(opts) if opts is not None else None, stream))
+    return out
+
+
+def _desc_with(ps, rot, pos, scale):
+    """The packed scene's descriptor with the facet transforms of these tensors."""
+    d = N.IactScene()
+    ctypes.memmove(ctypes.addressof(d), ctypes.addressof(ps.desc), ctypes.sizeof(d))
+    d.facet_rot, d.facet_pos, d.facet_scale = rot.data_ptr(), pos.data_ptr(), scale.data_ptr()
+    return d
+
+
+class RenderFunction(torch.autograd.Function):
+    """iact_render forward, iact_render_backward (recompute-based adjoint) backward.
+
+    Differentiable inputs: concatenated stage-0 facet rotations (F,3, degrees),
+    positions (F,3), perturbation scales (F,), sources (S,3), values (S,).
+    """
+
+    @staticmethod
+    def forward(ctx, meta, rot, pos, scale, src, val):
+        ps, sensor, code, mode, shape, opts = meta
+        device = src.device
+        sdesc, keep = sensor.pack(device)
+        rot_, pos_, scale_ = (t.detach().contiguous() for t in (rot, pos, scale))
+        src_, val_ = src.detach().contiguous(), val.detach().contiguous()
+        out = _forward(ps, _desc_with(ps, rot_, pos_, scale_), sdesc, code, src_, val_, mode, shape, opts, device)
+        ctx.meta = meta
+        ctx.save_for_backward(rot_, pos_, scale_, src_, val_)
+        del keep
+        return out
+
+    @staticmethod
+    def backward(ctx, gout):
+        ps, sensor, code, mode, shape, opts = ctx.meta
+        rot, pos, scale, src, val = ctx.saved_tensors
+        device = src.device
+        sdesc, keep = sensor.pack(device)
+        need = ctx.needs_input_grad
+        g = [torch.empty_like(t) if need[i + 1] else None for i, t in enumerate((rot, pos, scale, src, val))]
+        ws = torch.empty(max(ps.workspace_bytes(sdesc, src.shape[0], N.MODE_BACKWARD), 256), dtype=torch.uint8,
+                         device=device)
+        gout = gout.detach().to(torch.float32).contiguous()
+        stream = torch.cuda.current_stream(device).cuda_stream
+        ptr = lambda t: t.data_ptr() if t is not None else None
+        N.check(N.load().iact_render_backward(
+            ctypes.byref(_desc_with(ps, rot, pos, scale)), ctypes.byref(sdesc), code, src.data_ptr(),
+            val.data_ptr(), int(src.shape[0]), mode, gout.data_ptr(), ptr(g[0]), ptr(g[1]), ptr(g[2]),
+            ptr(g[3]), ptr(g[4]), ws.data_ptr(), ws.numel(), None, stream))
+        del keep
+        return (None, *g)
+
+
+def _primary_params(tel, device):
+    prim = stages_of(tel).get(0, [])
+    cat = lambda name: torch.cat([getattr(g, name).reshape(len(g), -1) if name != "perturbation_scale"
+                                  else getattr(g, name).reshape(-1) for g in prim]).to(device=device,
+                                                                                      dtype=torch.float32)
+    return cat("rotations"), cat("positions"), cat("perturbation_scale")
+
+
+def _needs_grad(tel, src, val):
+    if not torch.is_grad_enabled():
+        return False
+    if src.requires_grad or val.requires_grad:
+        return True
+    return any(t.requires_grad for g in stages_of(tel).get(0, [])
+               for t in (g.rotations, g.positions, g.perturbation_scale))
+
+
 def _launch(tel, sources, values, source_type, sensor_idx, mode, opts=None):
     device = _device()
     sensor = tel.sensors[sensor_idx]
@@ -49,15 +125,15 @@ def _launch(tel, sources, values, source_type, sensor_idx, mode, opts=None):
     shape = (S, P) if mode == N.MODE_RESPONSE else tuple(sensor.get_accumulator_shape())
     if 0 not in stages_of(tel):  # core/render.py:197-199 empty telescope
         return torch.zeros(shape, device=device)
-    lib = N.load()
     ps = pack_scene(tel, device)
+    code = source_code(source_type)
+    if _needs_grad(tel, src, val):
+        if ps.n_mirrors > 0:
+            raise NotImplementedError("gradients through mirror stages >= 1 are not available yet")
+        rot, pos, scale = _primary_params(tel, device)
+        return RenderFunction.apply((ps, sensor, code, mode, shape, opts), rot, pos, scale, src, val)
     sdesc, keep = sensor.pack(device)
-    out = torch.empty(shape, dtype=torch.float32, device=device)
-    ws = _workspace(ps, sdesc, S, mode, device)
-    stream = torch.cuda.current_stream(device).cuda_stream
-    N.check(lib.iact_render(ctypes.byref(ps.desc), ctypes.byref(sdesc), source_code(source_type),
-                            src.data_ptr(), val.data_ptr(), S, mode, out.data_ptr(), ws.data_ptr(),
-                            ws.numel(), ctypes.byref(opts) if opts is not None else None, stream))
+    out = _forward(ps, ps.desc, sdesc, code, src, val, mode, shape, opts, device)
     del keep
     return out
 

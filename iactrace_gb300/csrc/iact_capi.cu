@@ -86,7 +86,7 @@ int check_common(const iact_scene_t* sc, const iact_sensor_t* sn, int32_t src_ty
     return set_error(IACT_E_INVALID, "source_type must be IACT_SRC_POINT or IACT_SRC_PARALLEL");
   if (S < 0) return set_error(IACT_E_INVALID, "negative source count");
   if (S > 0 && (!sources || !values)) return set_error(IACT_E_INVALID, "sources/values are NULL");
-  const WsLayout L = workspace_layout(sc, acc_elems(sn, S, mode));
+  const WsLayout L = workspace_for(sc, sn, S, mode);
   if (!ws) return set_error(IACT_E_WORKSPACE, "workspace is NULL");
   if (reinterpret_cast<uintptr_t>(ws) % 256) return set_error(IACT_E_WORKSPACE, "workspace must be 256-byte aligned");
   if (ws_bytes < L.total)
@@ -128,9 +128,9 @@ int iact_workspace_size(const iact_scene_t* scene, const iact_sensor_t* sensor, 
   if (rc) return rc;
   if (!bytes) return set_error(IACT_E_INVALID, "bytes is NULL");
   if (n_sources < 0) return set_error(IACT_E_INVALID, "negative source count");
-  if (mode != IACT_MODE_IMAGE && mode != IACT_MODE_RESPONSE && mode != IACT_MODE_DEBUG)
+  if (mode != IACT_MODE_IMAGE && mode != IACT_MODE_RESPONSE && mode != IACT_MODE_DEBUG && mode != IACT_MODE_BACKWARD)
     return set_error(IACT_E_INVALID, "unknown mode");
-  *bytes = workspace_layout(scene, acc_elems(sensor, n_sources, mode)).total;
+  *bytes = workspace_for(scene, sensor, n_sources, mode).total;
   return IACT_OK;
 }
 
@@ -158,6 +158,24 @@ int iact_render_debug(const iact_scene_t* scene, const iact_sensor_t* sensor, in
   if (n > 0 && (!pts || !vals)) return set_error(IACT_E_INVALID, "pts/vals are NULL");
   return launch_debug(scene, sensor, source_type, sources, values, n_sources, pts, vals, pix, hit_mirror,
                       workspace, workspace_bytes, static_cast<cudaStream_t>(stream));
+}
+
+int iact_render_backward(const iact_scene_t* scene, const iact_sensor_t* sensor, int32_t source_type,
+                         const float* sources, const float* values, int32_t n_sources, int32_t mode,
+                         const float* grad_out, float* g_facet_rot, float* g_facet_pos, float* g_facet_scale,
+                         float* g_sources, float* g_values, void* workspace, size_t workspace_bytes,
+                         const iact_opts_t* opts, void* stream) {
+  if (mode != IACT_MODE_IMAGE && mode != IACT_MODE_RESPONSE)
+    return set_error(IACT_E_INVALID, "mode must be IACT_MODE_IMAGE or IACT_MODE_RESPONSE");
+  int rc = check_common(scene, sensor, source_type, sources, values, n_sources, IACT_MODE_BACKWARD, workspace,
+                        workspace_bytes);
+  if (rc) return rc;
+  if (scene->n_mirrors > 0)
+    return set_error(IACT_E_UNSUPPORTED, "iact_render_backward: scenes with mirror stages >= 1 are not supported");
+  if (!grad_out && acc_elems(sensor, n_sources, mode) > 0) return set_error(IACT_E_INVALID, "grad_out is NULL");
+  return launch_backward(scene, sensor, source_type, sources, values, n_sources, mode, grad_out, g_facet_rot,
+                         g_facet_pos, g_facet_scale, g_sources, g_values, workspace, workspace_bytes, opts,
+                         static_cast<cudaStream_t>(stream));
 }
 
 }  // extern "C"

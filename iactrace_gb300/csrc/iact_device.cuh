@@ -408,4 +408,37 @@ __device__ __forceinline__ float mirror_hit(const float* m, V3 o, V3 d, V3& pl, 
   return (valid && in_ap) ? (float)t : inf;
 }
 
+// Offsets (floats) of the record groups inside the table region.
+struct TableOffsets {
+  int cyl, box, sph, obox, tri, mir, total;
+};
+__host__ __device__ inline TableOffsets table_offsets(int n_cyl, int n_box, int n_sph, int n_obox,
+                                                      int n_tri, int n_mir) {
+  TableOffsets t;
+  t.cyl = 0;
+  t.box = t.cyl + n_cyl * kCylF;
+  t.sph = t.box + n_box * kBoxF;
+  t.obox = t.sph + n_sph * kSphF;
+  t.tri = t.obox + n_obox * kOboxF;
+  t.mir = (t.tri + n_tri * kTriF + 3) & ~3;
+  t.total = t.mir + n_mir * kMirF;
+  return t;
+}
+
+
+// Obstruction view over the table region staged in shared memory.
+__device__ __forceinline__ Obst make_obst(const float* tab, int n_cyl, int n_box, int n_sph, int n_obox, int n_tri) {
+  const TableOffsets to = table_offsets(n_cyl, n_box, n_sph, n_obox, n_tri, 0);
+  Obst ob;
+  ob.cyl = tab + to.cyl; ob.box = tab + to.box; ob.sph = tab + to.sph; ob.obox = tab + to.obox; ob.tri = tab + to.tri;
+  ob.n_cyl = n_cyl; ob.n_box = n_box; ob.n_sph = n_sph; ob.n_obox = n_obox; ob.n_tri = n_tri;
+  return ob;
+}
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+  return v;
+}
+
 }  // namespace iact

@@ -8,6 +8,7 @@
 #include <string>
 
 #include "../../include/iactrace_gb300.h"
+#include "iact_device.cuh"
 
 namespace iact {
 
@@ -25,12 +26,24 @@ struct WsLayout {
   size_t tables;   // processed obstruction/mirror/sensor records (floats)
   size_t p4;       // float4 [F*M] world point, 1/weight
   size_t n4;       // float4 [F*M] perturbed world normal
-  size_t acc;      // double [rows * P] FP64 accumulator of the render
+  size_t d4;       // float4 [F*M] world delta / |n + scale delta| (backward only)
+  size_t acc;      // double: [rows * P] render accumulator, or the gradient buckets
   size_t total;
   int n_table_floats;
 };
-WsLayout workspace_layout(const iact_scene_t* sc, size_t acc_elems);
-size_t acc_elems(const iact_sensor_t* sn, int S, int mode);  // mode < 0: debug (none)
+constexpr int kFacetGrad = 13;  // per facet: dL/dR world-frame H (9), dL/dpos (3), dL/dscale (1)
+WsLayout workspace_layout(const iact_scene_t* sc, size_t acc_elems, bool with_delta);
+size_t acc_elems(const iact_sensor_t* sn, int S, int mode);  // 0 for DEBUG
+WsLayout workspace_for(const iact_scene_t* sc, const iact_sensor_t* sn, int S, int mode);
+
+struct DevInfo {
+  int sm_count = 0;
+  int smem_optin = 0;
+};
+DevInfo device_info();
+int launch_prep(const iact_scene_t* sc, const WsLayout& L, char* ws, cudaStream_t st, bool with_delta);
+void host_euler(const float* deg, float* R);
+SensorK make_sensor(const iact_sensor_t* s);
 
 int launch_render(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type,
                   const float* sources, const float* values, int S, int mode, float* out,
@@ -41,5 +54,9 @@ int launch_debug(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type,
                  cudaStream_t stream);
 
 int launch_probe_fma(float* out, int blocks, int iters, cudaStream_t stream);
+int launch_backward(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type, const float* sources,
+                    const float* values, int S, int mode, const float* grad_out, float* g_rot, float* g_pos,
+                    float* g_scale, float* g_src, float* g_val, void* ws, size_t ws_bytes, const iact_opts_t* opts,
+                    cudaStream_t stream);
 
 }  // namespace iact

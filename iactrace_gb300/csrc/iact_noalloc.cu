@@ -73,7 +73,7 @@ extern "C" int iact_render_noalloc(const iact_scene_t* scene, const iact_sensor_
   if (mode != IACT_MODE_IMAGE && mode != IACT_MODE_RESPONSE)
     return set_error(IACT_E_INVALID, "mode must be IACT_MODE_IMAGE or IACT_MODE_RESPONSE");
   if (n_sources < 0) return set_error(IACT_E_INVALID, "negative source count");
-  const size_t need = workspace_layout(scene, acc_elems(sensor, n_sources, mode)).total;
+  const size_t need = workspace_for(scene, sensor, n_sources, mode).total;
   if (need > (size_t)IACT_NOALLOC_SCRATCH_BYTES)
     return set_error(IACT_E_UNSUPPORTED, "iact_render_noalloc: this render needs " + std::to_string(need) +
                                              " bytes of scratch, more than the fixed " +

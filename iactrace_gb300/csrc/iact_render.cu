@@ -27,23 +27,6 @@
 
 namespace iact {
 
-// Offsets (floats) of the record groups inside the table region.
-struct TableOffsets {
-  int cyl, box, sph, obox, tri, mir, total;
-};
-__host__ __device__ inline TableOffsets table_offsets(int n_cyl, int n_box, int n_sph, int n_obox,
-                                                      int n_tri, int n_mir) {
-  TableOffsets t;
-  t.cyl = 0;
-  t.box = t.cyl + n_cyl * kCylF;
-  t.sph = t.box + n_box * kBoxF;
-  t.obox = t.sph + n_sph * kSphF;
-  t.tri = t.obox + n_obox * kOboxF;
-  t.mir = (t.tri + n_tri * kTriF + 3) & ~3;
-  t.total = t.mir + n_mir * kMirF;
-  return t;
-}
-
 struct PrepK {
   int F, M;
   const float* facet_pos;
@@ -55,6 +38,7 @@ struct PrepK {
   const float* weights;
   float4* P4;
   float4* N4;
+  float4* D4;  // optional: world delta / |n + scale delta| (roughness-scale gradients)
   float* tables;
   const float* cyl;
   const float* box;
@@ -142,6 +126,7 @@ __global__ void __launch_bounds__(256) k_prep(const PrepK p) {
   float nn = sqrtf(dot(pe, pe));
   p.P4[i] = make_float4(pw.x, pw.y, pw.z, 1.f / p.weights[i]);
   p.N4[i] = make_float4(pe.x / nn, pe.y / nn, pe.z / nn, 0.f);
+  if (p.D4) p.D4[i] = make_float4(dw.x / nn, dw.y / nn, dw.z / nn, 0.f);
 }
 
 struct RenderK {
@@ -454,14 +439,7 @@ __global__ void __launch_bounds__(256) k_debug(const RenderK p, float* pts, floa
 
 // ------------------------------------------------------------------ host side
 
-namespace {
-
 inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
-
-struct DevInfo {
-  int sm_count = 0;
-  int smem_optin = 0;
-};
 
 DevInfo device_info() {
   static std::mutex mu;
@@ -519,13 +497,14 @@ SensorK make_sensor(const iact_sensor_t* s) {
   return k;
 }
 
-int launch_prep(const iact_scene_t* sc, const WsLayout& L, char* ws, cudaStream_t st) {
+int launch_prep(const iact_scene_t* sc, const WsLayout& L, char* ws, cudaStream_t st, bool with_delta) {
   PrepK p;
   p.F = sc->n_facets; p.M = sc->n_samples;
   p.facet_pos = sc->facet_pos; p.facet_rot = sc->facet_rot; p.facet_scale = sc->facet_scale;
   p.points = sc->points; p.normals = sc->normals; p.delta = sc->delta; p.weights = sc->weights;
   p.P4 = reinterpret_cast<float4*>(ws + L.p4);
   p.N4 = reinterpret_cast<float4*>(ws + L.n4);
+  p.D4 = with_delta ? reinterpret_cast<float4*>(ws + L.d4) : nullptr;
   p.tables = reinterpret_cast<float*>(ws + L.tables);
   p.cyl = sc->cyl; p.box = sc->box; p.sph = sc->sph; p.obox = sc->obox; p.tri = sc->tri;
   p.mirrors = sc->mirrors;
@@ -593,9 +572,7 @@ int dispatch_soft(bool soft, int mode, bool stages, RenderK p, int block, size_t
               : dispatch_mode<SRC, false>(mode, stages, p, block, smem, st, ev);
 }
 
-}  // namespace
-
-WsLayout workspace_layout(const iact_scene_t* sc, size_t acc_elems) {
+WsLayout workspace_layout(const iact_scene_t* sc, size_t acc_elems, bool with_delta) {
   WsLayout L;
   TableOffsets to = table_offsets(sc->n_cyl, sc->n_box, sc->n_sph, sc->n_obox, sc->n_tri, sc->n_mirrors);
   L.n_table_floats = to.total;
@@ -609,6 +586,8 @@ WsLayout workspace_layout(const iact_scene_t* sc, size_t acc_elems) {
   off = align256(off + sizeof(float4) * n);
   L.n4 = off;
   off = align256(off + sizeof(float4) * n);
+  L.d4 = off;
+  if (with_delta) off = align256(off + sizeof(float4) * n);
   L.acc = off;
   off = align256(off + sizeof(double) * acc_elems);
   L.total = off;
@@ -621,12 +600,18 @@ size_t acc_elems(const iact_sensor_t* sn, int S, int mode) {
   return 0;
 }
 
+WsLayout workspace_for(const iact_scene_t* sc, const iact_sensor_t* sn, int S, int mode) {
+  if (mode == IACT_MODE_BACKWARD)
+    return workspace_layout(sc, (size_t)std::max(sc->n_facets, 0) * kFacetGrad + (size_t)std::max(S, 0) * 4, true);
+  return workspace_layout(sc, acc_elems(sn, S, mode), false);
+}
+
 int launch_render(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type, const float* sources,
                   const float* values, int S, int mode, float* out, void* ws, size_t ws_bytes,
                   const iact_opts_t* opts, cudaStream_t st) {
   (void)ws_bytes;
   const size_t n_acc = acc_elems(sn, S, mode);
-  const WsLayout L = workspace_layout(sc, n_acc);
+  const WsLayout L = workspace_layout(sc, n_acc, false);
   char* w = static_cast<char*>(ws);
   const size_t P = (size_t)sn->n_pixels;
   int rc;
@@ -638,7 +623,7 @@ int launch_render(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type,
   if (rc) return rc;
   rc = check_cuda(cudaMemsetAsync(w + L.acc, 0, n_acc * sizeof(double), st), "zero accumulator");
   if (rc) return rc;
-  rc = launch_prep(sc, L, w, st);
+  rc = launch_prep(sc, L, w, st, false);
   if (rc) return rc;
 
   RenderK p = base_params(sc, sn, L, w, sources, values, S);
@@ -696,9 +681,9 @@ int launch_debug(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type, 
                  void* ws, size_t ws_bytes, cudaStream_t st) {
   (void)ws_bytes;
   if (S == 0 || sc->n_facets == 0 || sc->n_samples == 0) return IACT_OK;
-  const WsLayout L = workspace_layout(sc, 0);
+  const WsLayout L = workspace_layout(sc, 0, false);
   char* w = static_cast<char*>(ws);
-  int rc = launch_prep(sc, L, w, st);
+  int rc = launch_prep(sc, L, w, st, false);
   if (rc) return rc;
   RenderK p = base_params(sc, sn, L, w, sources, values, S);
   const size_t smem = sizeof(float) * (size_t)((L.n_table_floats + 3) & ~3);

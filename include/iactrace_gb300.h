@@ -56,7 +56,7 @@ extern "C" {
 #define IACT_MAX_OBSTRUCTIONS 2048 /* primitives over all obstruction kinds */
 
 enum { IACT_SRC_POINT = 0, IACT_SRC_PARALLEL = 1 };
-enum { IACT_MODE_IMAGE = 0, IACT_MODE_RESPONSE = 1, IACT_MODE_DEBUG = 2 };
+enum { IACT_MODE_IMAGE = 0, IACT_MODE_RESPONSE = 1, IACT_MODE_DEBUG = 2, IACT_MODE_BACKWARD = 3 };
 enum {
   IACT_SENSOR_SQUARE = 0,      /* sensors/square.py:28-91     SquareSensor */
   IACT_SENSOR_HEX = 1,         /* sensors/hexagonal.py:104-194 HexagonalSensor */
@@ -192,6 +192,24 @@ int iact_render_debug(const iact_scene_t* scene, const iact_sensor_t* sensor,
                       const float* values, int32_t n_sources, float* pts,
                       float* vals, int32_t* pix, int32_t* hit_mirror,
                       void* workspace, size_t workspace_bytes, void* stream);
+
+/* Adjoint of iact_render (mode IMAGE or RESPONSE) for single-stage scenes:
+ * given grad_out = dL/d(out), writes dL/d(facet rotations) [F,3] (per
+ * degree), dL/d(facet positions) [F,3], dL/d(facet perturbation scales) [F],
+ * dL/d(sources) [S,3] and dL/d(values) [S]; any of them may be NULL. Each
+ * ray's forward path is recomputed, nothing is stored between the calls.
+ * Pixel ids and shadow masks carry no gradient (as under jax.grad); soft
+ * sensors also pass gradients through the sensor-plane position. Workspace:
+ * iact_workspace_size(..., IACT_MODE_BACKWARD, ...). Replaces jax.grad of
+ * core/render.py:174-220 / :271-324 (no dedicated reference function). */
+int iact_render_backward(const iact_scene_t* scene, const iact_sensor_t* sensor,
+                         int32_t source_type, const float* sources,
+                         const float* values, int32_t n_sources, int32_t mode,
+                         const float* grad_out, float* g_facet_rot,
+                         float* g_facet_pos, float* g_facet_scale,
+                         float* g_sources, float* g_values, void* workspace,
+                         size_t workspace_bytes, const iact_opts_t* opts,
+                         void* stream);
 
 #ifdef __cplusplus
 }
