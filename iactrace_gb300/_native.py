@@ -63,7 +63,7 @@ class IactScene(ctypes.Structure):
         ("facet_pos", ctypes.c_void_p), ("facet_rot", ctypes.c_void_p), ("facet_scale", ctypes.c_void_p),
         ("points", ctypes.c_void_p), ("normals", ctypes.c_void_p), ("delta", ctypes.c_void_p),
         ("weights", ctypes.c_void_p),
-        ("n_mirrors", _i), ("mirrors", ctypes.c_void_p),
+        ("n_mirrors", _i), ("n_stages", _i), ("mirrors", ctypes.c_void_p),
         ("n_cyl", _i), ("n_box", _i), ("n_sph", _i), ("n_obox", _i), ("n_tri", _i),
         ("cyl", ctypes.c_void_p), ("box", ctypes.c_void_p), ("sph", ctypes.c_void_p),
         ("obox", ctypes.c_void_p), ("tri", ctypes.c_void_p),
@@ -110,8 +110,9 @@ _SIGS = {
     "iact_probe_fma": ([ctypes.c_void_p, _i, _i, ctypes.c_void_p], ctypes.c_int),
     "iact_render_backward": ([ctypes.POINTER(IactScene), ctypes.POINTER(IactSensor), _i, ctypes.c_void_p,
                               ctypes.c_void_p, _i, _i, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
-                              ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
-                              ctypes.POINTER(IactOpts), ctypes.c_void_p], ctypes.c_int),
+                              ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                              ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(IactOpts),
+                              ctypes.c_void_p], ctypes.c_int),
     "iact_render_debug": ([ctypes.POINTER(IactScene), ctypes.POINTER(IactSensor), _i, ctypes.c_void_p,
                            ctypes.c_void_p, _i, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                            ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p], ctypes.c_int),

@@ -62,11 +62,13 @@ class RenderFunction(torch.autograd.Function):
     """iact_render forward, iact_render_backward (recompute-based adjoint) backward.
 
     Differentiable inputs: concatenated stage-0 facet rotations (F,3, degrees),
-    positions (F,3), perturbation scales (F,), sources (S,3), values (S,).
+    positions (F,3), perturbation scales (F,), sources (S,3), values (S,), and
+    per stage mirror rotations (n,3), positions (n,3) and surface parameters
+    (n, 10: curvature, conic, 8 aspheric coefficients).
     """
 
     @staticmethod
-    def forward(ctx, meta, rot, pos, scale, src, val):
+    def forward(ctx, meta, rot, pos, scale, src, val, mrot, mpos, msurf):
         ps, sensor, code, mode, shape, opts = meta
         device = src.device
         sdesc, keep = sensor.pack(device)
@@ -74,6 +76,7 @@ class RenderFunction(torch.autograd.Function):
         src_, val_ = src.detach().contiguous(), val.detach().contiguous()
         out = _forward(ps, _desc_with(ps, rot_, pos_, scale_), sdesc, code, src_, val_, mode, shape, opts, device)
         ctx.meta = meta
+        ctx.n_mir = mrot.shape[0]
         ctx.save_for_backward(rot_, pos_, scale_, src_, val_)
         del keep
         return out
@@ -86,6 +89,9 @@ class RenderFunction(torch.autograd.Function):
         sdesc, keep = sensor.pack(device)
         need = ctx.needs_input_grad
         g = [torch.empty_like(t) if need[i + 1] else None for i, t in enumerate((rot, pos, scale, src, val))]
+        nm = ctx.n_mir
+        gm = [torch.empty(sh, device=device) if need[6 + i] and nm else None
+              for i, sh in enumerate(((nm, 3), (nm, 3), (nm, 10)))]
         ws = torch.empty(max(ps.workspace_bytes(sdesc, src.shape[0], N.MODE_BACKWARD), 256), dtype=torch.uint8,
                          device=device)
         gout = gout.detach().to(torch.float32).contiguous()
@@ -94,9 +100,12 @@ class RenderFunction(torch.autograd.Function):
         N.check(N.load().iact_render_backward(
             ctypes.byref(_desc_with(ps, rot, pos, scale)), ctypes.byref(sdesc), code, src.data_ptr(),
             val.data_ptr(), int(src.shape[0]), mode, gout.data_ptr(), ptr(g[0]), ptr(g[1]), ptr(g[2]),
-            ptr(g[3]), ptr(g[4]), ws.data_ptr(), ws.numel(), None, stream))
+            ptr(g[3]), ptr(g[4]), ptr(gm[0]), ptr(gm[1]), ptr(gm[2]), ws.data_ptr(), ws.numel(), None, stream))
         del keep
-        return (None, *g)
+        gm = [x if x is not None or not need[6 + i] else torch.zeros((0,) + ((3,) if i < 2 else (10,)),
+                                                                      device=device)
+              for i, x in enumerate(gm)]
+        return (None, *g, *gm)
 
 
 def _primary_params(tel, device):
@@ -107,13 +116,42 @@ def _primary_params(tel, device):
     return cat("rotations"), cat("positions"), cat("perturbation_scale")
 
 
+def _as_t(x, device):
+    return x.to(device=device, dtype=torch.float32) if isinstance(x, torch.Tensor) else \
+        torch.tensor(float(x), device=device)
+
+
+def _stage_params(tel, device):
+    """Per stage mirror (packing order): rotations, positions, (c, k, a[8])."""
+    rots, poss, surfs = [], [], []
+    for stage, groups in stages_of(tel).items():
+        if stage == 0:
+            continue
+        for g in groups:
+            n = len(g)
+            rots.append(g.rotations.reshape(n, 3).to(device=device, dtype=torch.float32))
+            poss.append(g.positions.reshape(n, 3).to(device=device, dtype=torch.float32))
+            a = g.aspheric.reshape(-1).to(device=device, dtype=torch.float32)
+            a = torch.cat([a, torch.zeros(N.IACT_MAX_ASPH - a.shape[0], device=device)])
+            surf = torch.cat([_as_t(g.curvature, device).reshape(1), _as_t(g.conic, device).reshape(1), a])
+            surfs.append(surf[None, :].expand(n, 2 + N.IACT_MAX_ASPH))
+    if not rots:
+        z = torch.zeros((0, 3), device=device)
+        return z, z, torch.zeros((0, 2 + N.IACT_MAX_ASPH), device=device)
+    return torch.cat(rots), torch.cat(poss), torch.cat(surfs)
+
+
 def _needs_grad(tel, src, val):
     if not torch.is_grad_enabled():
         return False
     if src.requires_grad or val.requires_grad:
         return True
-    return any(t.requires_grad for g in stages_of(tel).get(0, [])
-               for t in (g.rotations, g.positions, g.perturbation_scale))
+    for stage, groups in stages_of(tel).items():
+        for g in groups:
+            ts = [g.rotations, g.positions, g.perturbation_scale, g.aspheric, g.curvature, g.conic]
+            if any(isinstance(t, torch.Tensor) and t.requires_grad for t in ts):
+                return True
+    return False
 
 
 def _launch(tel, sources, values, source_type, sensor_idx, mode, opts=None):
@@ -128,10 +166,12 @@ def _launch(tel, sources, values, source_type, sensor_idx, mode, opts=None):
     ps = pack_scene(tel, device)
     code = source_code(source_type)
     if _needs_grad(tel, src, val):
-        if ps.n_mirrors > 0:
-            raise NotImplementedError("gradients through mirror stages >= 1 are not available yet")
+        if ps.n_stages > 2:
+            raise NotImplementedError("gradients through more than two mirror stages are not available")
         rot, pos, scale = _primary_params(tel, device)
-        return RenderFunction.apply((ps, sensor, code, mode, shape, opts), rot, pos, scale, src, val)
+        mrot, mpos, msurf = _stage_params(tel, device)
+        return RenderFunction.apply((ps, sensor, code, mode, shape, opts), rot, pos, scale, src, val,
+                                    mrot, mpos, msurf)
     sdesc, keep = sensor.pack(device)
     out = _forward(ps, ps.desc, sdesc, code, src, val, mode, shape, opts, device)
     del keep

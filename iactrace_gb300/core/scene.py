@@ -46,7 +46,7 @@ def _mirror_records(stage_groups) -> np.ndarray:
                 m.pos[:] = g.positions[i].detach().cpu().tolist()
                 m.rot[:] = g.rotations[i].detach().cpu().tolist()
                 m.offset[:] = g.offsets[i].detach().cpu().tolist()
-                m.curvature, m.conic = g.curvature, g.conic
+                m.curvature, m.conic = float(g.curvature), float(g.conic)
                 for k, a in enumerate(asph):
                     m.asph[k] = a
                 if polygon:
@@ -95,6 +95,8 @@ class PackedScene:
         self.n_mirrors = len(recs) // ctypes.sizeof(N.IactMirror)
         self.mirrors = torch.from_numpy(recs.copy()).to(device) if self.n_mirrors else None
         d.n_mirrors = self.n_mirrors
+        d.n_stages = len(later)
+        self.n_stages = len(later)
         d.mirrors = self.mirrors.data_ptr() if self.n_mirrors else None
         kinds = defaultdict(list)
         for g in (tel.obstruction_groups or []):
@@ -124,7 +126,7 @@ def _fingerprint(tel):
             t = getattr(g, name, None)
             if t is not None:
                 fp.append((id(t), t._version))
-        fp.append((g.optical_stage, g.curvature, g.conic))
+        fp.append((g.optical_stage, float(g.curvature), float(g.conic)))
     for g in (tel.obstruction_groups or []):
         fp.append(id(g))
     return tuple(fp)

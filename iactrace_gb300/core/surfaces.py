@@ -12,10 +12,13 @@ import torch
 class AsphericSurface:
     """core/surfaces.py:8: curvature c, conic k and coefficients a_i of r^(4(i+1))."""
 
-    def __init__(self, curvature: float, conic: float, aspheric=()):
-        self.curvature = float(curvature)
-        self.conic = float(conic)
-        self.aspheric = torch.as_tensor(aspheric, dtype=torch.float32).reshape(-1)
+    def __init__(self, curvature, conic, aspheric=()):
+        # floats, or 0-d tensors when they are optimised
+        self.curvature = curvature if isinstance(curvature, torch.Tensor) else float(curvature)
+        self.conic = conic if isinstance(conic, torch.Tensor) else float(conic)
+        self.aspheric = aspheric if isinstance(aspheric, torch.Tensor) else \
+            torch.as_tensor(aspheric, dtype=torch.float32)
+        self.aspheric = self.aspheric.reshape(-1)
 
     @staticmethod
     def from_template(tmpl) -> "AsphericSurface":
@@ -24,7 +27,7 @@ class AsphericSurface:
         return AsphericSurface(float(s["curvature"]), float(s["conic"]), s.get("aspheric", []) or [])
 
     def key(self):
-        return (self.curvature, self.conic, tuple(float(a) for a in self.aspheric.tolist()))
+        return (float(self.curvature), float(self.conic), tuple(float(a) for a in self.aspheric.tolist()))
 
     def _sag_raw(self, x, y):
         """core/surfaces.py:25-39 (aspheric term i multiplies r2**(2(i+1)))."""

@@ -1,4 +1,4 @@
-// Adjoint (reverse-mode) of the single-stage render path.
+// Adjoint (reverse-mode) of the render path.
 //
 // The reference has no backward of its own; users differentiate `render`
 // with jax.grad (core/render.py:118-171 through sensors/*.py accumulate).
@@ -13,8 +13,10 @@
 //   hard bins: d img[pix] / d val = 1 (pixel ids carry no gradient)
 //   soft bins: val * w_k(x, y) / sum_k w_k                 (square.py:144-172, hexagonal.py:264-315)
 //
-// Shadow and hit masks are piecewise constant and carry no gradient, as in
-// jax.grad. Gradients reach facet rotations (Euler degrees), facet
+// Later mirror stages (core/render.py:44-115, at most two on this path)
+// are recorded during the re-trace and reversed with the implicit-function
+// derivative of their Newton root (stage_bwd). Shadow and hit masks are
+// piecewise constant and carry no gradient, as in jax.grad. Gradients reach facet rotations (Euler degrees), facet
 // positions, facet roughness scales, source positions/directions and source
 // values. Each lane keeps running sums for its current facet and source;
 // when a warp moves to another facet or source it reduces them across the
@@ -49,6 +51,8 @@ struct AdjK {
   SensorK sn;
   double* gfacet;  // [F, kFacetGrad]
   double* gsrc;    // [S, 4]: d/dsource (3), d/dvalue
+  double* gmir;    // [n_mir, kMirGrad]: dL/dR (9), dL/dpos (3), dL/dc, dL/dk, dL/da (8)
+  int n_mir;
   int SB, FC, CC, n_fchunk, n_cchunk, n_tiles;
   int* counter;
 };
@@ -166,7 +170,107 @@ __device__ __forceinline__ void soft_hex_bwd(const SensorK& s, const TT* table, 
   gy = -s.gs * gxg + s.gc * gyg;
 }
 
-template <int SRC, bool SOFT, int MODE>
+
+constexpr int kMaxAdjStages = 2;
+
+// One stage >= 1 reflection as recorded by the forward re-trace.
+struct StageRec {
+  V3 o, r;      // incoming ray (world)
+  float val;    // value before this stage
+  int j;        // mirror index (scene order)
+  float t;      // Newton root
+  V3 pl, nl;    // local hit point and unit normal
+  float c2;     // r . n_world
+};
+
+// Reverse of core/render.py:44-115 for one ray at one stage: from dL/d(o',
+// r', val') after the reflection to dL/d(o, r, val) before it, adding the
+// mirror's parameter gradients into g (kMirGrad floats). The hit t(o, r,
+// theta) is the Newton root of g(t) = o_z + t d_z - sag(o_xy + t d_xy) = 0,
+// differentiated implicitly (dt = -(dG) / G_t with G_t = N . d_local,
+// N = (-sag_x, -sag_y, 1)); the reference unrolls its 10 Newton steps, which
+// agrees to the root's residual.
+__device__ __forceinline__ void stage_bwd(const float* m, const StageRec& R, V3& go, V3& gr, float& gv,
+                                          float* g) {
+  const float* Rj = m;
+  const V3 Pj = mk(m[9], m[10], m[11]);
+  const V3 nw = rmul(Rj, R.nl);
+  // val' = val |c2|
+  const float sgn = R.c2 >= 0.f ? 1.f : -1.f;
+  float gc2 = gv * R.val * sgn;
+  const float gval_in = gv * fabsf(R.c2);
+  // r' = r - 2 c2 nw, c2 = r . nw
+  gc2 += -2.f * dot(gr, nw);
+  V3 gnw = (-2.f * R.c2) * gr;
+  V3 gr_in = gr + gc2 * nw;
+  gnw = gnw + gc2 * R.r;
+  // o' = Rj pl + Pj, nw = Rj nl
+  const V3 gpl = rtmul(Rj, go);
+  const V3 gnl = rtmul(Rj, gnw);
+  float gR[9];
+  gR[0] = go.x * R.pl.x + gnw.x * R.nl.x; gR[1] = go.x * R.pl.y + gnw.x * R.nl.y; gR[2] = go.x * R.pl.z + gnw.x * R.nl.z;
+  gR[3] = go.y * R.pl.x + gnw.y * R.nl.x; gR[4] = go.y * R.pl.y + gnw.y * R.nl.y; gR[5] = go.y * R.pl.z + gnw.y * R.nl.z;
+  gR[6] = go.z * R.pl.x + gnw.z * R.nl.x; gR[7] = go.z * R.pl.y + gnw.z * R.nl.y; gR[8] = go.z * R.pl.z + gnw.z * R.nl.z;
+  V3 gP = go;
+  // nl = N/|N|, |N| = 1/nl_z
+  const float ndg = dot(R.nl, gnl);
+  const V3 gN = R.nl.z * (gnl - ndg * R.nl);
+  // surface derivatives at the hit and at the facet offset (z0)
+  const double x0 = m[12], y0 = m[13];
+  const double Xs = (double)R.pl.x + x0, Ys = (double)R.pl.y + y0;
+  SagD D, D0;
+  sag_derivs(m, Xs * Xs + Ys * Ys, D);
+  sag_derivs(m, x0 * x0 + y0 * y0, D0);
+  const double sX = 2.0 * Xs * D.Sr, sY = 2.0 * Ys * D.Sr;
+  const double sXX = 2.0 * D.Sr + 4.0 * Xs * Xs * D.Srr, sXY = 4.0 * Xs * Ys * D.Srr, sYY = 2.0 * D.Sr + 4.0 * Ys * Ys * D.Srr;
+  double gX = -(gN.x * sXX + gN.y * sXY), gY = -(gN.x * sXY + gN.y * sYY);
+  const double wN = -(2.0 * Xs * gN.x + 2.0 * Ys * gN.y);  // dL/dS_rho through the normal
+  double gth_c = wN * D.Src, gth_k = wN * D.Srk;
+  double gth_a[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) gth_a[i] = wN * D.Sra[i];
+  // pl = (X, Y, S(rho) - S(rho0))
+  gX += gpl.x + gpl.z * sX;
+  gY += gpl.y + gpl.z * sY;
+  gth_c += gpl.z * (D.Sc - D0.Sc);
+  gth_k += gpl.z * (D.Sk - D0.Sk);
+#pragma unroll
+  for (int i = 0; i < 8; ++i) gth_a[i] += gpl.z * (D.Sa[i] - D0.Sa[i]);
+  // X = ol_x + t dl_x, Y = ol_y + t dl_y ; t implicit
+  const V3 ol = rtmul(Rj, R.o - Pj), dl = rtmul(Rj, R.r);
+  V3 gol = mk((float)gX, (float)gY, 0.f);
+  V3 gdl = mk((float)(R.t * gX), (float)(R.t * gY), 0.f);
+  const double gt = gX * dl.x + gY * dl.y;
+  const double Gt = -sX * dl.x - sY * dl.y + dl.z;
+  const double lam = gt / Gt;
+  const V3 Nv = mk((float)-sX, (float)-sY, 1.f);
+  gol = gol - (float)lam * Nv;
+  gdl = gdl - (float)(lam * R.t) * Nv;
+  gth_c += lam * (D.Sc - D0.Sc);
+  gth_k += lam * (D.Sk - D0.Sk);
+#pragma unroll
+  for (int i = 0; i < 8; ++i) gth_a[i] += lam * (D.Sa[i] - D0.Sa[i]);
+  (void)ol;
+  // ol = Rj^T (o - Pj), dl = Rj^T r
+  const V3 Rg_ol = rmul(Rj, gol), Rg_dl = rmul(Rj, gdl);
+  go = Rg_ol;
+  gP = gP - Rg_ol;
+  const V3 op = R.o - Pj;
+  gR[0] += op.x * gol.x + R.r.x * gdl.x; gR[1] += op.x * gol.y + R.r.x * gdl.y; gR[2] += op.x * gol.z + R.r.x * gdl.z;
+  gR[3] += op.y * gol.x + R.r.y * gdl.x; gR[4] += op.y * gol.y + R.r.y * gdl.y; gR[5] += op.y * gol.z + R.r.y * gdl.z;
+  gR[6] += op.z * gol.x + R.r.z * gdl.x; gR[7] += op.z * gol.y + R.r.z * gdl.y; gR[8] += op.z * gol.z + R.r.z * gdl.z;
+  gr = gr_in + Rg_dl;
+  gv = gval_in;
+#pragma unroll
+  for (int i = 0; i < 9; ++i) g[i] = gR[i];
+  g[9] = gP.x; g[10] = gP.y; g[11] = gP.z;
+  g[12] = (float)gth_c;
+  g[13] = (float)gth_k;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) g[14 + i] = (float)gth_a[i];
+}
+
+template <int SRC, bool SOFT, int MODE, bool STAGES>
 __global__ void __launch_bounds__(256) k_adjoint(const AdjK p) {
   extern __shared__ __align__(16) float smem[];
   __shared__ int s_tile;
@@ -178,7 +282,10 @@ __global__ void __launch_bounds__(256) k_adjoint(const AdjK p) {
   for (int i = threadIdx.x; i < p.n_table_floats; i += nthr) tab[i] = p.tables[i];
   for (int i = threadIdx.x; i < htab_n; i += nthr)
     htab[i] = (short)(i < p.sn.table_q * p.sn.table_r ? p.hex_table[i] : -1);
+  float* mgrad = reinterpret_cast<float*>(htab + htab_n);  // [n_mir, kMirGrad] CTA partial sums
+  for (int i = threadIdx.x; i < (STAGES ? p.n_mir * kMirGrad : 0); i += nthr) mgrad[i] = 0.f;
   const Obst ob = make_obst(tab, p.n_cyl, p.n_box, p.n_sph, p.n_obox, p.n_tri);
+  const float* mir = tab + table_offsets(p.n_cyl, p.n_box, p.n_sph, p.n_obox, p.n_tri, p.n_mir).mir;
   const SensorK& sn = p.sn;
   // sensor plane frame (intersections.py:19-21)
   const V3 u1 = mk(sn.R[0], sn.R[3], sn.R[6]), u2 = mk(sn.R[1], sn.R[4], sn.R[7]), ns = mk(sn.R[2], sn.R[5], sn.R[8]);
@@ -239,18 +346,58 @@ __global__ void __launch_bounds__(256) k_adjoint(const AdjK p) {
         }
         const bool shadowed = occluded(ob, tp, mk(-d.x, -d.y, -d.z));
         const float c = dot(d, nn);
-        const V3 r = d - (2.f * c) * nn;
-        const float val = v * -c * iw;
+        const V3 r0 = d - (2.f * c) * nn;
+        const float val0 = v * -c * iw;
+        // later stages, recorded for the reverse sweep (core/render.py:44-79)
+        StageRec rec[kMaxAdjStages];
+        int nst = 0;
+        bool alive = !shadowed;
+        V3 o = tp, r = r0;
+        float val = val0;
+        if (STAGES) {
+          int mi = 0;
+          while (mi < p.n_mir) {
+            const int stg = (int)mir[mi * kMirF + 22];
+            float best_t = __int_as_float(0x7f800000);
+            V3 bpl = mk(0.f, 0.f, 0.f), bnl = mk(0.f, 0.f, 0.f);
+            int bi = -1;
+            int mj = mi;
+            for (; mj < p.n_mir && (int)mir[mj * kMirF + 22] == stg; ++mj) {
+              const float* mm = mir + mj * kMirF;
+              const V3 pos = mk(mm[9], mm[10], mm[11]);
+              V3 pl, nl;
+              const float tt = mirror_hit(mm, rtmul(mm, o - pos), rtmul(mm, r), pl, nl);
+              if (tt < best_t) {
+                best_t = tt; bpl = pl; bnl = nl; bi = mj;
+              }
+            }
+            const bool hit = best_t < kBig;
+            alive = alive && hit && !occluded(ob, o, r);
+            if (hit && nst < kMaxAdjStages) {
+              const float* mm = mir + bi * kMirF;
+              const V3 nw = rmul(mm, bnl);
+              StageRec& R = rec[nst++];
+              R.o = o; R.r = r; R.val = val; R.j = bi; R.t = best_t; R.pl = bpl; R.nl = bnl;
+              R.c2 = dot(r, nw);
+              val = val * fabsf(R.c2);
+              o = rmul(mm, bpl) + mk(mm[9], mm[10], mm[11]);
+              r = r - (2.f * R.c2) * nw;
+            } else {
+              alive = false;
+            }
+            mi = mj;
+          }
+        }
         const float ndotd = dot(r, ns);
         const bool parallel = fabsf(ndotd) < 1e-10f;
         const float inv_nd = rcp_a(parallel ? 1.f : ndotd);
-        const float tpl = (dot(ns, C) - dot(tp, ns)) * inv_nd;
-        const V3 op = (tp + tpl * r) - C;
+        const float tpl = (dot(ns, C) - dot(o, ns)) * inv_nd;
+        const V3 op = (o + tpl * r) - C;
         const bool hit_plane = !parallel && (tpl > 0.f);
         const float x = hit_plane ? dot(op, u1) : kBig, y = hit_plane ? dot(op, u2) : kBig;
         // ---- reverse of the deposit
         float gval = 0.f, gx = 0.f, gy = 0.f;
-        if (!shadowed) {
+        if (alive) {
           if (SOFT) {
             if (sn.type == IACT_SENSOR_SOFT_SQUARE) soft_square_bwd(sn, p.grad_out, rowbase, x, y, val, gval, gx, gy);
             else if (p.hex_in_smem) soft_hex_bwd(sn, htab, p.grad_out, rowbase, x, y, val, gval, gx, gy);
@@ -262,13 +409,24 @@ __global__ void __launch_bounds__(256) k_adjoint(const AdjK p) {
           }
         }
         if ((gval != 0.f) | (gx != 0.f) | (gy != 0.f)) {
-          // plane (intersections.py:23-35): p = tp + t r, t = ns.(C - tp) / ns.r
+          // plane (intersections.py:23-35): p = o + t r, t = ns.(C - o) / ns.r
           V3 gpl = gx * u1 + gy * u2;  // dL/dp
           const float dLdt = dot(gpl, r);
-          V3 a = gpl - (dLdt * inv_nd) * ns;            // dL/dtp through the plane
+          V3 a = gpl - (dLdt * inv_nd) * ns;               // dL/do through the plane
           V3 gr = tpl * gpl - (dLdt * tpl * inv_nd) * ns;  // dL/dr through the plane
+          float gv0 = gval;
+          if (STAGES) {
+            for (int k = nst - 1; k >= 0; --k) {
+              float gm[kMirGrad];
+              stage_bwd(mir + rec[k].j * kMirF, rec[k], a, gr, gv0, gm);
+              float* dst = mgrad + rec[k].j * kMirGrad;
+#pragma unroll
+              for (int i = 0; i < kMirGrad; ++i)
+                if (gm[i] != 0.f) atomicAdd(dst + i, gm[i]);
+            }
+          }
           // val = v (-c) iw ; r = d - 2 c n'
-          const float dLdc = -gval * v * iw - 2.f * dot(gr, nn);
+          const float dLdc = -gv0 * v * iw - 2.f * dot(gr, nn);
           const V3 b = (-2.f * c) * gr + dLdc * d;  // dL/dn'
           const V3 gd = gr + dLdc * nn;             // dL/dd
           V3 gsrc;
@@ -291,7 +449,7 @@ __global__ void __launch_bounds__(256) k_adjoint(const AdjK p) {
             acc.gs += dot(b, dw) - dot(b, nn) * dot(nn, dw);
           }
           acc.gsrc[0] += gsrc.x; acc.gsrc[1] += gsrc.y; acc.gsrc[2] += gsrc.z;
-          acc.gv += gval * -c * iw;
+          acc.gv += gv0 * -c * iw;
         }
       }
       if (++cl == CCc) {
@@ -306,44 +464,78 @@ __global__ void __launch_bounds__(256) k_adjoint(const AdjK p) {
     if (cur_f >= 0) flush_facet(acc, p.gfacet, cur_f);
     if (cur_s >= 0) flush_src(acc, p.gsrc, cur_s);
   }
+  if (STAGES) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < p.n_mir * kMirGrad; i += nthr)
+      if (mgrad[i] != 0.f) atomicAdd(p.gmir + i, (double)mgrad[i]);
+  }
 }
 
 // Per facet: dL/dR = H R, then dL/d(tip, tilt, rot) in degrees with
 // R = Rz(rot) Ry(tilt) Rx(tip) (core/transforms.py:72-107); per source the
 // FP64 sums to float.
+__device__ void euler_grads(const double* G, const float* deg, double* out) {
+  // dL/d(tip, tilt, rot) per degree from dL/dR, R = Rz(rot) Ry(tilt) Rx(tip)
+  const double k = 0.017453292519943295;
+  const double a = deg[0] * k, b = deg[1] * k, c = deg[2] * k;
+  const double ca = cos(a), sa = sin(a), cb = cos(b), sb = sin(b), cc = cos(c), sc = sin(c);
+  const double Rx[9] = {1, 0, 0, 0, ca, -sa, 0, sa, ca}, dRx[9] = {0, 0, 0, 0, -sa, -ca, 0, ca, -sa};
+  const double Ry[9] = {cb, 0, sb, 0, 1, 0, -sb, 0, cb}, dRy[9] = {-sb, 0, cb, 0, 0, 0, -cb, 0, -sb};
+  const double Rz[9] = {cc, -sc, 0, sc, cc, 0, 0, 0, 1}, dRz[9] = {-sc, -cc, 0, cc, -sc, 0, 0, 0, 0};
+  auto mm = [](const double* A, const double* B, double* Cm) {
+    for (int r = 0; r < 3; ++r)
+      for (int q = 0; q < 3; ++q) Cm[3 * r + q] = A[3 * r] * B[q] + A[3 * r + 1] * B[3 + q] + A[3 * r + 2] * B[6 + q];
+  };
+  double ZY[9], T1[9], D[9];
+  mm(Rz, Ry, ZY);
+  mm(ZY, dRx, D);
+  out[0] = 0;
+  for (int j = 0; j < 9; ++j) out[0] += G[j] * D[j];
+  mm(Rz, dRy, T1);
+  mm(T1, Rx, D);
+  out[1] = 0;
+  for (int j = 0; j < 9; ++j) out[1] += G[j] * D[j];
+  mm(dRz, Ry, T1);
+  mm(T1, Rx, D);
+  out[2] = 0;
+  for (int j = 0; j < 9; ++j) out[2] += G[j] * D[j];
+  for (int j = 0; j < 3; ++j) out[j] *= k;
+}
+
+__global__ void k_adjoint_mirrors(const double* gmir, const iact_mirror_t* mirrors, int n_mir, float* g_rot,
+                                  float* g_pos, float* g_surf) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_mir) return;
+  const double* h = gmir + (size_t)i * kMirGrad;
+  double out[3];
+  euler_grads(h, mirrors[i].rot, out);
+  if (g_rot)
+    for (int j = 0; j < 3; ++j) g_rot[3 * i + j] = (float)out[j];
+  if (g_pos)
+    for (int j = 0; j < 3; ++j) g_pos[3 * i + j] = (float)h[9 + j];
+  if (g_surf)
+    for (int j = 0; j < 2 + IACT_MAX_ASPH; ++j) g_surf[(2 + IACT_MAX_ASPH) * i + j] = (float)h[12 + j];
+}
+
 __global__ void k_adjoint_finish(const double* gfacet, const double* gsrc, const float* facet_rot, int F, int S,
                                  float* g_rot, float* g_pos, float* g_scale, float* g_src, float* g_val) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < F) {
     const double* h = gfacet + (size_t)i * kFacetGrad;
     const double k = 0.017453292519943295;
+    // dL/dR = H R with R the facet rotation
     const double a = facet_rot[3 * i] * k, b = facet_rot[3 * i + 1] * k, c = facet_rot[3 * i + 2] * k;
     const double ca = cos(a), sa = sin(a), cb = cos(b), sb = sin(b), cc = cos(c), sc = sin(c);
-    const double Rx[9] = {1, 0, 0, 0, ca, -sa, 0, sa, ca}, dRx[9] = {0, 0, 0, 0, -sa, -ca, 0, ca, -sa};
-    const double Ry[9] = {cb, 0, sb, 0, 1, 0, -sb, 0, cb}, dRy[9] = {-sb, 0, cb, 0, 0, 0, -cb, 0, -sb};
-    const double Rz[9] = {cc, -sc, 0, sc, cc, 0, 0, 0, 1}, dRz[9] = {-sc, -cc, 0, cc, -sc, 0, 0, 0, 0};
-    auto mm = [](const double* A, const double* B, double* Cm) {
-      for (int r = 0; r < 3; ++r)
-        for (int q = 0; q < 3; ++q) Cm[3 * r + q] = A[3 * r] * B[q] + A[3 * r + 1] * B[3 + q] + A[3 * r + 2] * B[6 + q];
-    };
-    double ZY[9], R[9], G[9], T1[9], D[9];
-    mm(Rz, Ry, ZY);
-    mm(ZY, Rx, R);
-    mm(h, R, G);  // dL/dR = H R
+    const double R[9] = {cc * cb, cc * sb * sa - sc * ca, cc * sb * ca + sc * sa,
+                         sc * cb, sc * sb * sa + cc * ca, sc * sb * ca - cc * sa,
+                         -sb, cb * sa, cb * ca};
+    double G[9];
+    for (int r = 0; r < 3; ++r)
+      for (int q = 0; q < 3; ++q) G[3 * r + q] = h[3 * r] * R[q] + h[3 * r + 1] * R[3 + q] + h[3 * r + 2] * R[6 + q];
     double out[3];
-    mm(ZY, dRx, D);  // dR/dtip
-    out[0] = 0;
-    for (int j = 0; j < 9; ++j) out[0] += G[j] * D[j];
-    mm(Rz, dRy, T1);  // dR/dtilt
-    mm(T1, Rx, D);
-    out[1] = 0;
-    for (int j = 0; j < 9; ++j) out[1] += G[j] * D[j];
-    mm(dRz, Ry, T1);  // dR/drot
-    mm(T1, Rx, D);
-    out[2] = 0;
-    for (int j = 0; j < 9; ++j) out[2] += G[j] * D[j];
+    euler_grads(G, facet_rot + 3 * i, out);
     if (g_rot)
-      for (int j = 0; j < 3; ++j) g_rot[3 * i + j] = (float)(out[j] * k);
+      for (int j = 0; j < 3; ++j) g_rot[3 * i + j] = (float)out[j];
     if (g_pos)
       for (int j = 0; j < 3; ++j) g_pos[3 * i + j] = (float)h[9 + j];
     if (g_scale) g_scale[i] = (float)h[12];
@@ -357,9 +549,9 @@ __global__ void k_adjoint_finish(const double* gfacet, const double* gsrc, const
 
 namespace {
 
-template <int SRC, bool SOFT, int MODE>
+template <int SRC, bool SOFT, int MODE, bool STAGES>
 int run_adjoint(const AdjK& p, int block, size_t smem, cudaStream_t st) {
-  auto kern = k_adjoint<SRC, SOFT, MODE>;
+  auto kern = k_adjoint<SRC, SOFT, MODE, STAGES>;
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return check_cuda(e, "cudaFuncSetAttribute(k_adjoint smem)");
@@ -373,25 +565,32 @@ int run_adjoint(const AdjK& p, int block, size_t smem, cudaStream_t st) {
   return check_cuda(cudaGetLastError(), "k_adjoint launch");
 }
 
-template <int SRC, bool SOFT>
+template <int SRC, bool SOFT, bool STAGES>
 int adj_mode(int mode, const AdjK& p, int block, size_t smem, cudaStream_t st) {
-  return mode == IACT_MODE_RESPONSE ? run_adjoint<SRC, SOFT, IACT_MODE_RESPONSE>(p, block, smem, st)
-                                    : run_adjoint<SRC, SOFT, IACT_MODE_IMAGE>(p, block, smem, st);
+  return mode == IACT_MODE_RESPONSE ? run_adjoint<SRC, SOFT, IACT_MODE_RESPONSE, STAGES>(p, block, smem, st)
+                                    : run_adjoint<SRC, SOFT, IACT_MODE_IMAGE, STAGES>(p, block, smem, st);
+}
+template <int SRC, bool SOFT>
+int adj_stages(bool stages, int mode, const AdjK& p, int block, size_t smem, cudaStream_t st) {
+  return stages ? adj_mode<SRC, SOFT, true>(mode, p, block, smem, st)
+                : adj_mode<SRC, SOFT, false>(mode, p, block, smem, st);
 }
 
 }  // namespace
 
 int launch_backward(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type, const float* sources,
                     const float* values, int S, int mode, const float* grad_out, float* g_rot, float* g_pos,
-                    float* g_scale, float* g_src, float* g_val, void* ws, size_t ws_bytes, const iact_opts_t* opts,
-                    cudaStream_t st) {
+                    float* g_scale, float* g_src, float* g_val, float* g_mrot, float* g_mpos, float* g_msurf,
+                    void* ws, size_t ws_bytes, const iact_opts_t* opts, cudaStream_t st) {
   (void)ws_bytes;
   const int F = sc->n_facets;
   const WsLayout L = workspace_for(sc, sn, S, IACT_MODE_BACKWARD);
   char* w = static_cast<char*>(ws);
   double* gfacet = reinterpret_cast<double*>(w + L.acc);
   double* gsrc = gfacet + (size_t)F * kFacetGrad;
-  const size_t nacc = (size_t)F * kFacetGrad + (size_t)S * 4;
+  double* gmir = gsrc + (size_t)S * 4;
+  const int n_mir = sc->n_mirrors;
+  const size_t nacc = (size_t)F * kFacetGrad + (size_t)S * 4 + (size_t)n_mir * kMirGrad;
   int rc = check_cuda(cudaMemsetAsync(gfacet, 0, nacc * sizeof(double), st), "zero gradient buckets");
   if (rc) return rc;
   if (S > 0 && F > 0 && sc->n_samples > 0) {
@@ -414,6 +613,8 @@ int launch_backward(const iact_scene_t* sc, const iact_sensor_t* sn, int src_typ
     p.sn = make_sensor(sn);
     p.gfacet = gfacet;
     p.gsrc = gsrc;
+    p.gmir = gmir;
+    p.n_mir = n_mir;
     p.counter = reinterpret_cast<int*>(w + L.counter);
     const int block = (opts && opts->block_threads > 0) ? opts->block_threads : 256;
     const int nw = block / 32;
@@ -432,16 +633,17 @@ int launch_backward(const iact_scene_t* sc, const iact_sensor_t* sn, int src_typ
     const size_t htab = hex ? (size_t)sn->table_q * sn->table_r : 0;
     const size_t htab_bytes = sizeof(short) * ((htab + 7) & ~(size_t)7);
     p.hex_in_smem = (hex && sn->n_pixels < 32768 && tab_bytes + htab_bytes <= 96 * 1024) ? 1 : 0;
-    const size_t smem = tab_bytes + (p.hex_in_smem ? htab_bytes : 0);
+    const size_t smem = tab_bytes + (p.hex_in_smem ? htab_bytes : 0) + sizeof(float) * (size_t)n_mir * kMirGrad;
     const bool soft = sn->type == IACT_SENSOR_SOFT_SQUARE || sn->type == IACT_SENSOR_SOFT_HEX;
     void* const* ev = opts ? opts->kernel_events : nullptr;
     if (ev && ev[0]) cudaEventRecord(static_cast<cudaEvent_t>(ev[0]), st);
+    const bool stages = n_mir > 0;
     if (src_type == IACT_SRC_POINT)
-      rc = soft ? adj_mode<IACT_SRC_POINT, true>(mode, p, block, smem, st)
-                : adj_mode<IACT_SRC_POINT, false>(mode, p, block, smem, st);
+      rc = soft ? adj_stages<IACT_SRC_POINT, true>(stages, mode, p, block, smem, st)
+                : adj_stages<IACT_SRC_POINT, false>(stages, mode, p, block, smem, st);
     else
-      rc = soft ? adj_mode<IACT_SRC_PARALLEL, true>(mode, p, block, smem, st)
-                : adj_mode<IACT_SRC_PARALLEL, false>(mode, p, block, smem, st);
+      rc = soft ? adj_stages<IACT_SRC_PARALLEL, true>(stages, mode, p, block, smem, st)
+                : adj_stages<IACT_SRC_PARALLEL, false>(stages, mode, p, block, smem, st);
     if (rc) return rc;
     if (ev && ev[1]) cudaEventRecord(static_cast<cudaEvent_t>(ev[1]), st);
   }
@@ -450,6 +652,11 @@ int launch_backward(const iact_scene_t* sc, const iact_sensor_t* sn, int src_typ
     k_adjoint_finish<<<(n + 255) / 256, 256, 0, st>>>(gfacet, gsrc, sc->facet_rot, F, S, g_rot, g_pos, g_scale,
                                                         g_src, g_val);
     rc = check_cuda(cudaGetLastError(), "k_adjoint_finish launch");
+    if (rc) return rc;
+  }
+  if (n_mir > 0 && (g_mrot || g_mpos || g_msurf)) {
+    k_adjoint_mirrors<<<(n_mir + 63) / 64, 64, 0, st>>>(gmir, sc->mirrors, n_mir, g_mrot, g_mpos, g_msurf);
+    rc = check_cuda(cudaGetLastError(), "k_adjoint_mirrors launch");
   }
   return rc;
 }

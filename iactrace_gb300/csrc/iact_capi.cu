@@ -38,6 +38,8 @@ int validate_scene(const iact_scene_t* sc) {
   if (sc->n_mirrors < 0 || sc->n_mirrors > IACT_MAX_STAGE_MIRRORS)
     return set_error(IACT_E_UNSUPPORTED, "stage-mirror count outside [0, IACT_MAX_STAGE_MIRRORS]");
   if (sc->n_mirrors > 0 && !sc->mirrors) return set_error(IACT_E_INVALID, "mirrors is NULL");
+  if (sc->n_stages < 0 || sc->n_stages > sc->n_mirrors || (sc->n_mirrors > 0 && sc->n_stages == 0))
+    return set_error(IACT_E_INVALID, "n_stages must count the distinct stages of the mirror table");
   const int counts[5] = {sc->n_cyl, sc->n_box, sc->n_sph, sc->n_obox, sc->n_tri};
   const void* ptrs[5] = {sc->cyl, sc->box, sc->sph, sc->obox, sc->tri};
   long long total = 0;
@@ -163,19 +165,20 @@ int iact_render_debug(const iact_scene_t* scene, const iact_sensor_t* sensor, in
 int iact_render_backward(const iact_scene_t* scene, const iact_sensor_t* sensor, int32_t source_type,
                          const float* sources, const float* values, int32_t n_sources, int32_t mode,
                          const float* grad_out, float* g_facet_rot, float* g_facet_pos, float* g_facet_scale,
-                         float* g_sources, float* g_values, void* workspace, size_t workspace_bytes,
-                         const iact_opts_t* opts, void* stream) {
+                         float* g_sources, float* g_values, float* g_mirror_rot, float* g_mirror_pos,
+                         float* g_mirror_surface, void* workspace, size_t workspace_bytes, const iact_opts_t* opts,
+                         void* stream) {
   if (mode != IACT_MODE_IMAGE && mode != IACT_MODE_RESPONSE)
     return set_error(IACT_E_INVALID, "mode must be IACT_MODE_IMAGE or IACT_MODE_RESPONSE");
   int rc = check_common(scene, sensor, source_type, sources, values, n_sources, IACT_MODE_BACKWARD, workspace,
                         workspace_bytes);
   if (rc) return rc;
-  if (scene->n_mirrors > 0)
-    return set_error(IACT_E_UNSUPPORTED, "iact_render_backward: scenes with mirror stages >= 1 are not supported");
+  if (scene->n_stages > 2)
+    return set_error(IACT_E_UNSUPPORTED, "iact_render_backward: at most 2 mirror stages after the primary");
   if (!grad_out && acc_elems(sensor, n_sources, mode) > 0) return set_error(IACT_E_INVALID, "grad_out is NULL");
   return launch_backward(scene, sensor, source_type, sources, values, n_sources, mode, grad_out, g_facet_rot,
-                         g_facet_pos, g_facet_scale, g_sources, g_values, workspace, workspace_bytes, opts,
-                         static_cast<cudaStream_t>(stream));
+                         g_facet_pos, g_facet_scale, g_sources, g_values, g_mirror_rot, g_mirror_pos,
+                         g_mirror_surface, workspace, workspace_bytes, opts, static_cast<cudaStream_t>(stream));
 }
 
 }  // extern "C"

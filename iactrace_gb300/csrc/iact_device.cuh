@@ -442,3 +442,51 @@ __device__ __forceinline__ float warp_sum(float v) {
 }
 
 }  // namespace iact
+
+namespace iact {
+
+// Sag derivatives of one stage mirror for the adjoint (core/surfaces.py:25-58).
+// S(rho) = c rho / (1 + q) + sum_i a_i rho^(2(i+1)), q = sqrt(1 - (1+k) c^2 rho):
+//   S_rho = c / (2q) + sum_i p_i a_i rho^(p_i - 1),  S_rhorho = c (1+k) c^2 / (4 q^3) + ...
+//   S_c = rho/(1+q) + (1+k) c^2 rho^2 / (q (1+q)^2),  S_k = c^3 rho^2 / (2 q (1+q)^2)
+//   S_rho,c = 1/(2q) + (1+k) c^2 rho / (2 q^3),       S_rho,k = c^3 rho / (4 q^3)
+//   S_a_i = rho^p_i,  S_rho,a_i = p_i rho^(p_i - 1)
+struct SagD {
+  double S, Sr, Srr, Sc, Sk, Src, Srk;
+  double Sa[8], Sra[8];
+};
+
+__device__ __forceinline__ void sag_derivs(const float* m, double rho, SagD& o) {
+  const double c = m[15], k = m[23];
+  const double al = (1.0 + k) * c * c;
+  const double q = sqrt(1.0 - al * rho);
+  const double q3 = q * q * q, opq = 1.0 + q;
+  o.S = c * rho / opq;
+  o.Sr = c / (2.0 * q);
+  o.Srr = c * al / (4.0 * q3);
+  o.Sc = rho / opq + (1.0 + k) * c * c * rho * rho / (q * opq * opq);
+  o.Sk = c * c * c * rho * rho / (2.0 * q * opq * opq);
+  o.Src = 1.0 / (2.0 * q) + (1.0 + k) * c * c * rho / (2.0 * q3);
+  o.Srk = c * c * c * rho / (4.0 * q3);
+  const int na = (int)m[19];
+  for (int i = 0; i < 8; ++i) {
+    o.Sa[i] = 0.0;
+    o.Sra[i] = 0.0;
+  }
+  double rp = rho * rho;  // rho^p, p = 2
+  double rpm1 = rho;      // rho^(p-1)
+  double rpm2 = 1.0;      // rho^(p-2)
+  for (int i = 0; i < na; ++i) {
+    const double p = 2.0 * (i + 1), a = m[24 + i];
+    o.S += a * rp;
+    o.Sr += a * p * rpm1;
+    o.Srr += a * p * (p - 1.0) * rpm2;
+    o.Sa[i] = rp;
+    o.Sra[i] = p * rpm1;
+    rp *= rho * rho;
+    rpm1 *= rho * rho;
+    rpm2 *= rho * rho;
+  }
+}
+
+}  // namespace iact

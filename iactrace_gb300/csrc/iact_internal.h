@@ -32,6 +32,7 @@ struct WsLayout {
   int n_table_floats;
 };
 constexpr int kFacetGrad = 13;  // per facet: dL/dR world-frame H (9), dL/dpos (3), dL/dscale (1)
+constexpr int kMirGrad = 22;    // per stage mirror: dL/dR (9), dL/dpos (3), dL/dc, dL/dk, dL/da (8)
 WsLayout workspace_layout(const iact_scene_t* sc, size_t acc_elems, bool with_delta);
 size_t acc_elems(const iact_sensor_t* sn, int S, int mode);  // 0 for DEBUG
 WsLayout workspace_for(const iact_scene_t* sc, const iact_sensor_t* sn, int S, int mode);
@@ -56,7 +57,7 @@ int launch_debug(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type,
 int launch_probe_fma(float* out, int blocks, int iters, cudaStream_t stream);
 int launch_backward(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type, const float* sources,
                     const float* values, int S, int mode, const float* grad_out, float* g_rot, float* g_pos,
-                    float* g_scale, float* g_src, float* g_val, void* ws, size_t ws_bytes, const iact_opts_t* opts,
-                    cudaStream_t stream);
+                    float* g_scale, float* g_src, float* g_val, float* g_mrot, float* g_mpos, float* g_msurf,
+                    void* ws, size_t ws_bytes, const iact_opts_t* opts, cudaStream_t stream);
 
 }  // namespace iact

@@ -52,8 +52,9 @@ class MirrorGroup:
     def _init_common(self, positions, rotations, surface, optical_stage, offsets):
         self.positions = _t(positions).reshape(-1, 3)
         self.rotations = _t(rotations).reshape(-1, 3)
-        self.curvature = float(surface.curvature)
-        self.conic = float(surface.conic)
+        # floats, or 0-d tensors when they are optimised (stage >= 1 mirrors)
+        self.curvature = surface.curvature if isinstance(surface.curvature, torch.Tensor) else float(surface.curvature)
+        self.conic = surface.conic if isinstance(surface.conic, torch.Tensor) else float(surface.conic)
         self.aspheric = surface.aspheric.clone()
         self.optical_stage = int(optical_stage)
         n = self.positions.shape[0]

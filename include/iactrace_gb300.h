@@ -95,6 +95,7 @@ typedef struct {
   const float* weights;     /* [F,M]   sample weights */
   /* stages >= 1, flattened in (stage, group, mirror) order */
   int32_t n_mirrors;
+  int32_t n_stages; /* distinct stage values among the mirrors */
   const iact_mirror_t* mirrors; /* [n_mirrors] */
   /* obstructions (core/obstructions.py) */
   int32_t n_cyl, n_box, n_sph, n_obox, n_tri;
@@ -193,10 +194,13 @@ int iact_render_debug(const iact_scene_t* scene, const iact_sensor_t* sensor,
                       float* vals, int32_t* pix, int32_t* hit_mirror,
                       void* workspace, size_t workspace_bytes, void* stream);
 
-/* Adjoint of iact_render (mode IMAGE or RESPONSE) for single-stage scenes:
- * given grad_out = dL/d(out), writes dL/d(facet rotations) [F,3] (per
- * degree), dL/d(facet positions) [F,3], dL/d(facet perturbation scales) [F],
- * dL/d(sources) [S,3] and dL/d(values) [S]; any of them may be NULL. Each
+/* Adjoint of iact_render (mode IMAGE or RESPONSE), scenes with at most two
+ * mirror stages after the primary: given grad_out = dL/d(out), writes
+ * dL/d(facet rotations) [F,3] (per degree), dL/d(facet positions) [F,3],
+ * dL/d(facet perturbation scales) [F], dL/d(sources) [S,3], dL/d(values)
+ * [S], and per stage mirror dL/d(rotation) [n_mirrors,3], dL/d(position)
+ * [n_mirrors,3] and dL/d(curvature, conic, aspheric[8]) [n_mirrors,10];
+ * any output may be NULL. Each
  * ray's forward path is recomputed, nothing is stored between the calls.
  * Pixel ids and shadow masks carry no gradient (as under jax.grad); soft
  * sensors also pass gradients through the sensor-plane position. Workspace:
@@ -207,7 +211,9 @@ int iact_render_backward(const iact_scene_t* scene, const iact_sensor_t* sensor,
                          const float* values, int32_t n_sources, int32_t mode,
                          const float* grad_out, float* g_facet_rot,
                          float* g_facet_pos, float* g_facet_scale,
-                         float* g_sources, float* g_values, void* workspace,
+                         float* g_sources, float* g_values,
+                         float* g_mirror_rot, float* g_mirror_pos,
+                         float* g_mirror_surface, void* workspace,
                          size_t workspace_bytes, const iact_opts_t* opts,
                          void* stream);
 

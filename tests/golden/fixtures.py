@@ -77,6 +77,13 @@ def telescope(fx):
                                                   kernel_size=d["kernel_size"])
             else:
                 s = HexagonalSensor(d["position"], d["rotation"], centers, edge_width=d["edge_width"])
+            # the grid constants the reference derived in this precision: its
+            # float32 and float64 runs can detect different (60-degree
+            # equivalent) grid frames and build different lookup tables
+            s.hex_size, s.hex_inradius, s.grid_rotation = d["hex_size"], d["hex_inradius"], d["grid_rotation"]
+            s.grid_offset = tuple(d["grid_offset"])
+            s.q_min, s.r_min = d["q_min"], d["r_min"]
+            s.lookup_table = torch.from_numpy(np.ascontiguousarray(fx[f"hex_table_{i}"].astype(np.int32)))
         sensors.append(s)
     return Telescope(groups, obst, sensors, name="golden")
 

@@ -1,0 +1,43 @@
+"""The CUDA path against the reference's own outputs (golden fixtures written
+by tests/golden/make_golden.py from GerritRo/iactrace itself, float64 run on
+the same sampled arrays), through the C ABI."""
+from __future__ import annotations
+
+import json
+import os
+import sys
+
+import numpy as np
+import pytest
+
+import iactrace_gb300 as it
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "golden"))
+import fixtures as FX  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("case", FX.CASES)
+def test_gpu_rays_and_images_match_reference(cuda, case):
+    if not os.path.exists(FX.path(case, "f64")):
+        pytest.skip("fixture not generated")
+    fx = FX.load(case, "f64")
+    tel = FX.telescope(fx)
+    src, val, st = FX.inputs(fx)
+    sens = json.loads(str(fx["sensors_json"]))
+    si0 = FX.sensor_ids(fx)[0]
+    pts, vals = (t.cpu().double().numpy() for t in it.render_debug(tel, src, val, st, si0))
+    rp, rv = fx["debug_pts"], fx["debug_vals"]
+    ok = (rp[:, 0] < 1e9) & (pts[:, 0] < 1e9)
+    assert np.abs(pts[ok] - rp[ok]).max() < 8e-6
+    flip = (rv == 0) != (vals == 0)
+    assert flip.sum() <= max(1, 1e-4 * flip.size)
+    assert (np.abs(vals[~flip] - rv[~flip]).max() / np.abs(rv).max()) < 2e-5
+    for si in FX.sensor_ids(fx):
+        ref = FX.image(fx, si).reshape(-1)
+        img = it.render(tel, src, val, st, si).cpu().double().numpy().reshape(-1)
+        err = np.linalg.norm(img - ref) / np.linalg.norm(ref)
+        soft = "Differentiable" in sens[si]["class"]
+        assert err < (1e-4 if soft else 2e-3), f"sensor {si}: relative L2 {err:.3g}"
