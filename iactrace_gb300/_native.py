@@ -28,6 +28,7 @@ IACT_MAX_OBSTRUCTIONS = 2048
 
 SRC_POINT = 0
 SRC_PARALLEL = 1
+SRC_EXTENDED = 2
 MODE_IMAGE = 0
 MODE_RESPONSE = 1
 MODE_DEBUG = 2
@@ -86,7 +87,7 @@ class IactSensor(ctypes.Structure):
 
 class IactOpts(ctypes.Structure):
     _fields_ = [("block_threads", _i), ("sources_per_cta", _i), ("facets_per_tile", _i), ("hist_mode", _i),
-                ("kernel_events", ctypes.c_void_p * 2)]
+                ("seed", ctypes.c_uint32), ("kernel_events", ctypes.c_void_p * 2)]
 
 
 class IactError(RuntimeError):
@@ -115,7 +116,7 @@ _SIGS = {
                               ctypes.c_void_p], ctypes.c_int),
     "iact_render_debug": ([ctypes.POINTER(IactScene), ctypes.POINTER(IactSensor), _i, ctypes.c_void_p,
                            ctypes.c_void_p, _i, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
-                           ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p], ctypes.c_int),
+                           ctypes.c_void_p, ctypes.c_size_t, ctypes.c_uint32, ctypes.c_void_p], ctypes.c_int),
 }
 
 # symbols declared by include/iactrace_gb300.h that bindings resolve

@@ -13,7 +13,7 @@ import math
 import torch
 
 from .. import _native as N
-from .scene import pack_scene, stages_of
+from .scene import pack_scene, primary_params, stages_of
 
 
 def _device():
@@ -23,12 +23,21 @@ def _device():
 
 
 def source_code(source_type) -> int:
-    """core/render.py:129-133: 'point' is a point source, anything else parallel."""
-    return N.SRC_POINT if source_type == "point" else N.SRC_PARALLEL
+    """core/render.py:129-133: 'point' is a point source, anything else parallel.
+
+    'extended' (not a reference type) is a parallel source with a Gaussian
+    angular profile: sources are (S, 4) = (direction, sigma in radians) and
+    every ray draws its own tilt from a counter-based stream (``seed``)."""
+    if source_type == "point":
+        return N.SRC_POINT
+    if source_type == "extended":
+        return N.SRC_EXTENDED
+    return N.SRC_PARALLEL
 
 
-def _inputs(sources, values, device):
-    src = torch.as_tensor(sources).to(device=device, dtype=torch.float32).reshape(-1, 3).contiguous()
+def _inputs(sources, values, device, source_type="point"):
+    width = 4 if source_type == "extended" else 3
+    src = torch.as_tensor(sources).to(device=device, dtype=torch.float32).reshape(-1, width).contiguous()
     val = torch.as_tensor(values).to(device=device, dtype=torch.float32).reshape(-1).contiguous()
     if src.shape[0] != val.shape[0]:
         raise ValueError(f"sources ({src.shape[0]}) and values ({val.shape[0]}) disagree in length")
@@ -97,23 +106,18 @@ class RenderFunction(torch.autograd.Function):
         gout = gout.detach().to(torch.float32).contiguous()
         stream = torch.cuda.current_stream(device).cuda_stream
         ptr = lambda t: t.data_ptr() if t is not None else None
+        if code == N.SRC_EXTENDED and g[3] is not None:
+            raise NotImplementedError("no gradients with respect to extended sources")
         N.check(N.load().iact_render_backward(
             ctypes.byref(_desc_with(ps, rot, pos, scale)), ctypes.byref(sdesc), code, src.data_ptr(),
             val.data_ptr(), int(src.shape[0]), mode, gout.data_ptr(), ptr(g[0]), ptr(g[1]), ptr(g[2]),
-            ptr(g[3]), ptr(g[4]), ptr(gm[0]), ptr(gm[1]), ptr(gm[2]), ws.data_ptr(), ws.numel(), None, stream))
+            ptr(g[3]), ptr(g[4]), ptr(gm[0]), ptr(gm[1]), ptr(gm[2]), ws.data_ptr(), ws.numel(),
+            ctypes.byref(opts) if opts is not None else None, stream))
         del keep
         gm = [x if x is not None or not need[6 + i] else torch.zeros((0,) + ((3,) if i < 2 else (10,)),
                                                                       device=device)
               for i, x in enumerate(gm)]
         return (None, *g, *gm)
-
-
-def _primary_params(tel, device):
-    prim = stages_of(tel).get(0, [])
-    cat = lambda name: torch.cat([getattr(g, name).reshape(len(g), -1) if name != "perturbation_scale"
-                                  else getattr(g, name).reshape(-1) for g in prim]).to(device=device,
-                                                                                      dtype=torch.float32)
-    return cat("rotations"), cat("positions"), cat("perturbation_scale")
 
 
 def _as_t(x, device):
@@ -154,47 +158,59 @@ def _needs_grad(tel, src, val):
     return False
 
 
-def _launch(tel, sources, values, source_type, sensor_idx, mode, opts=None):
+def _opts_with_seed(opts, seed):
+    if not seed:
+        return opts
+    o = N.IactOpts()
+    if opts is not None:
+        ctypes.memmove(ctypes.addressof(o), ctypes.addressof(opts), ctypes.sizeof(o))
+    o.seed = int(seed) & 0xFFFFFFFF
+    return o
+
+
+def _launch(tel, sources, values, source_type, sensor_idx, mode, opts=None, seed=0):
     device = _device()
     sensor = tel.sensors[sensor_idx]
-    src, val = _inputs(sources, values, device)
+    src, val = _inputs(sources, values, device, source_type)
+    opts = _opts_with_seed(opts, seed)
     S = int(src.shape[0])
     P = int(math.prod(sensor.get_accumulator_shape()))
     shape = (S, P) if mode == N.MODE_RESPONSE else tuple(sensor.get_accumulator_shape())
     if 0 not in stages_of(tel):  # core/render.py:197-199 empty telescope
         return torch.zeros(shape, device=device)
-    ps = pack_scene(tel, device)
     code = source_code(source_type)
     if _needs_grad(tel, src, val):
+        rot, pos, scale = primary_params(tel, device)
+        ps = pack_scene(tel, device, tuple(t.detach().contiguous() for t in (rot, pos, scale)))
         if ps.n_stages > 2:
             raise NotImplementedError("gradients through more than two mirror stages are not available")
-        rot, pos, scale = _primary_params(tel, device)
         mrot, mpos, msurf = _stage_params(tel, device)
         return RenderFunction.apply((ps, sensor, code, mode, shape, opts), rot, pos, scale, src, val,
                                     mrot, mpos, msurf)
+    ps = pack_scene(tel, device)
     sdesc, keep = sensor.pack(device)
     out = _forward(ps, ps.desc, sdesc, code, src, val, mode, shape, opts, device)
     del keep
     return out
 
 
-def render(tel, sources, values, source_type="point", sensor_idx=0, opts=None):
+def render(tel, sources, values, source_type="point", sensor_idx=0, opts=None, seed=0):
     """core/render.py:174-220: image with the sensor's accumulator shape."""
-    return _launch(tel, sources, values, source_type, sensor_idx, N.MODE_IMAGE, opts)
+    return _launch(tel, sources, values, source_type, sensor_idx, N.MODE_IMAGE, opts, seed)
 
 
-def render_response_matrix(tel, sources, values, source_type="point", sensor_idx=0, opts=None):
+def render_response_matrix(tel, sources, values, source_type="point", sensor_idx=0, opts=None, seed=0):
     """core/render.py:271-324: (n_sources, n_pixels) per-source rows."""
-    return _launch(tel, sources, values, source_type, sensor_idx, N.MODE_RESPONSE, opts)
+    return _launch(tel, sources, values, source_type, sensor_idx, N.MODE_RESPONSE, opts, seed)
 
 
-def render_debug(tel, sources, values, source_type="point", sensor_idx=0, extras=False):
+def render_debug(tel, sources, values, source_type="point", sensor_idx=0, extras=False, seed=0):
     """core/render.py:223-268: raw hits (F*S*M, 2) and values (F*S*M,), ray
     order (facet, source, sample). With extras=True also the hard pixel id
     and the index of the last stage mirror hit per ray."""
     device = _device()
     sensor = tel.sensors[sensor_idx]
-    src, val = _inputs(sources, values, device)
+    src, val = _inputs(sources, values, device, source_type)
     S = int(src.shape[0])
     if 0 not in stages_of(tel):
         z = (torch.zeros((0, 2), device=device), torch.zeros((0,), device=device))
@@ -212,6 +228,6 @@ def render_debug(tel, sources, values, source_type="point", sensor_idx=0, extras
     N.check(lib.iact_render_debug(ctypes.byref(ps.desc), ctypes.byref(sdesc), source_code(source_type),
                                   src.data_ptr(), val.data_ptr(), S, pts.data_ptr(), vals.data_ptr(),
                                   pix.data_ptr() if extras else None, hm.data_ptr() if extras else None,
-                                  ws.data_ptr(), ws.numel(), stream))
+                                  ws.data_ptr(), ws.numel(), int(seed) & 0xFFFFFFFF, stream))
     del keep
     return (pts, vals, pix, hm) if extras else (pts, vals)

@@ -65,7 +65,12 @@ def _mirror_records(stage_groups) -> np.ndarray:
 
 
 class PackedScene:
-    """Device-resident tables + the iact_scene_t that points at them."""
+    """Device-resident tables + the iact_scene_t that points at them.
+
+    The sample arrays, stage-mirror records and obstruction tables are packed
+    once and cached; the per-facet transforms (rotation, position, roughness
+    scale: F x 7 floats, the parameters an optimiser changes) are refreshed by
+    `set_facets` on every call."""
 
     def __init__(self, tel, device):
         device = torch.device(device)
@@ -81,14 +86,11 @@ class PackedScene:
         d.n_facets, d.n_samples = self.F, self.M
         if self.F and self.M:
             cat = lambda name: torch.cat([getattr(g, name).detach().float() for g in prim])
-            self.facet_pos = _f32(cat("positions"), device)
-            self.facet_rot = _f32(cat("rotations"), device)
-            self.facet_scale = _f32(cat("perturbation_scale"), device)
             self.points = _f32(cat("points"), device)
             self.normals = _f32(cat("normals"), device)
             self.delta = _f32(cat("perturbation_delta"), device)
             self.weights = _f32(cat("weights").reshape(self.F, self.M), device)
-            for name in ("facet_pos", "facet_rot", "facet_scale", "points", "normals", "delta", "weights"):
+            for name in ("points", "normals", "delta", "weights"):
                 setattr(d, name, getattr(self, name).data_ptr())
         later = [(s, gs) for s, gs in st.items() if s != 0]
         recs = _mirror_records(later)
@@ -111,6 +113,13 @@ class PackedScene:
         self.desc = d
         self.device = device
 
+    def set_facets(self, rot, pos, scale):
+        """Point the descriptor at these (F,3), (F,3), (F,) float32 device tensors."""
+        self.facet_rot, self.facet_pos, self.facet_scale = rot, pos, scale
+        if self.F and self.M:
+            self.desc.facet_rot, self.desc.facet_pos = rot.data_ptr(), pos.data_ptr()
+            self.desc.facet_scale = scale.data_ptr()
+
     def workspace_bytes(self, sensor_desc, n_sources: int, mode: int) -> int:
         size = ctypes.c_size_t(0)
         N.check(N.load().iact_workspace_size(ctypes.byref(self.desc), ctypes.byref(sensor_desc), int(n_sources),
@@ -118,28 +127,48 @@ class PackedScene:
         return int(size.value)
 
 
+def primary_params(tel, device):
+    """Concatenated stage-0 facet rotations (F,3), positions (F,3), scales (F,):
+    float32 on `device`, differentiable (torch.cat / .to keep the graph)."""
+    prim = stages_of(tel).get(0, [])
+    if not prim:
+        z = torch.zeros((0, 3), device=device)
+        return z, z, torch.zeros(0, device=device)
+    cat = lambda name, w: torch.cat([getattr(g, name).reshape(len(g), w) if w else getattr(g, name).reshape(-1)
+                                     for g in prim]).to(device=device, dtype=torch.float32)
+    return cat("rotations", 3), cat("positions", 3), cat("perturbation_scale", 0)
+
+
 def _fingerprint(tel):
-    fp = [id(tel)]
+    """Identity of everything packed once (not the per-facet transforms)."""
+    fp = []
     for g in tel.mirror_groups:
-        for name in ("positions", "rotations", "perturbation_scale", "points", "normals", "perturbation_delta",
-                     "weights", "offsets", "aspheric"):
+        names = ("points", "normals", "perturbation_delta", "weights") if g.optical_stage == 0 else \
+            ("positions", "rotations", "offsets", "aspheric")
+        for name in names:
             t = getattr(g, name, None)
             if t is not None:
                 fp.append((id(t), t._version))
-        fp.append((g.optical_stage, float(g.curvature), float(g.conic)))
+        fp.append((g.optical_stage, float(g.curvature), float(g.conic), len(g)))
     for g in (tel.obstruction_groups or []):
         fp.append(id(g))
     return tuple(fp)
 
 
-def pack_scene(tel, device) -> PackedScene:
-    """Packed tables of `tel` on `device`, cached until a tensor changes."""
+def pack_scene(tel, device, facets=None) -> PackedScene:
+    """Packed tables of `tel` on `device` (cached while the sample arrays,
+    stage mirrors and obstructions are unchanged), with the current facet
+    transforms (or the given detached `facets` = (rot, pos, scale))."""
     cache = tel.__dict__.setdefault("_packed", {})
     key = str(torch.device(device))
     fp = _fingerprint(tel)
     hit = cache.get(key)
     if hit is not None and hit[0] == fp:
-        return hit[1]
-    ps = PackedScene(tel, device)
-    cache[key] = (fp, ps)
+        ps = hit[1]
+    else:
+        ps = PackedScene(tel, device)
+        cache[key] = (fp, ps)
+    if facets is None:
+        facets = tuple(t.detach().contiguous() for t in primary_params(tel, ps.device))
+    ps.set_facets(*facets)
     return ps

@@ -55,6 +55,7 @@ struct AdjK {
   int n_mir;
   int SB, FC, CC, n_fchunk, n_cchunk, n_tiles;
   int* counter;
+  uint32_t seed;  // jitter stream of extended sources
 };
 
 // Per-lane running sums of one (facet, source) stream of rays.
@@ -105,7 +106,10 @@ __device__ __forceinline__ void flush_src(Acc& a, double* gsrc, int s) {
 
 // dL/dval and dL/d(x, y) of one ray's deposit (sensors/square.py:144-172).
 // Soft square: w_k = exp(-0.5 (dx_k^2 + dy_k^2)/sigma^2) over the pixel
-// offsets; L = sum_k g_k val w_k / W. dL/dx = val/W sum_k (g_k - gbar) dw_k/dx.
+// offsets; L = sum_k g_k val w_k / W, so dL/dval = gbar = sum_k g_k w_k / W
+// and dL/dx = val/W sum_k (g_k - gbar) dw_k/dx. The sums run on g_k - g_0
+// (g_0: the centre tap), which is exact for the dominant tap: the direct
+// form cancels catastrophically in float32 when one tap carries the ray.
 __device__ __forceinline__ void soft_square_bwd(const SensorK& s, const float* g, int rowbase, float x, float y,
                                                 float val, float& gval, float& gx, float& gy) {
   gval = gx = gy = 0.f;
@@ -116,6 +120,8 @@ __device__ __forceinline__ void soft_square_bwd(const SensorK& s, const float* g
   const int K = s.kernel_size, n = 2 * K + 1;
   const float is2 = 1.f / (s.sigma * s.sigma);
   const int xi0 = (int)xb, yi0 = (int)yb;
+  const bool c_in = xi0 >= 0 && xi0 < s.width && yi0 >= 0 && yi0 < s.height;
+  const float g0 = c_in ? g[rowbase + yi0 * s.width + xi0] : 0.f;
   float W = 0.f, sgw = 0.f, dWx = 0.f, dWy = 0.f, sgdx = 0.f, sgdy = 0.f;
   for (int i = 0; i < n; ++i)
     for (int j = 0; j < n; ++j) {
@@ -124,15 +130,18 @@ __device__ __forceinline__ void soft_square_bwd(const SensorK& s, const float* g
       float wx = -w * ddx * is2 * s.inv_dx, wy = -w * ddy * is2 * s.inv_dy;  // dw/dx, dw/dy
       int xi = xi0 + j - K, yi = yi0 + i - K;
       float gk = (xi >= 0 && xi < s.width && yi >= 0 && yi < s.height) ? g[rowbase + yi * s.width + xi] : 0.f;
-      W += w; sgw += gk * w; dWx += wx; dWy += wy; sgdx += gk * wx; sgdy += gk * wy;
+      const float dg = gk - g0;
+      W += w; sgw += dg * w; dWx += wx; dWy += wy; sgdx += dg * wx; sgdy += dg * wy;
     }
   const float iW = 1.f / W;
-  gval = sgw * iW;
-  gx = val * iW * (sgdx - gval * dWx);
-  gy = val * iW * (sgdy - gval * dWy);
+  const float dbar = sgw * iW;  // gbar - g0
+  gval = g0 + dbar;
+  gx = val * iW * (sgdx - dbar * dWx);
+  gy = val * iW * (sgdy - dbar * dWy);
 }
 
-// sensors/hexagonal.py:264-315 soft hex deposit, reverse.
+// sensors/hexagonal.py:264-315 soft hex deposit, reverse (same centred sums
+// as soft_square_bwd, centred on the base hexagon's gradient).
 template <typename TT>
 __device__ __forceinline__ void soft_hex_bwd(const SensorK& s, const TT* table, const float* g, int rowbase, float x,
                                              float y, float val, float& gval, float& gx, float& gy) {
@@ -143,6 +152,8 @@ __device__ __forceinline__ void soft_hex_bwd(const SensorK& s, const TT* table, 
   float ddx = xg - s.hex_sx * (qi + 0.5f * ri), ddy = yg - s.hex_sy * ri;
   const int K = s.kernel_size;
   const float isg = 1.f / s.sigma;
+  const int p0 = hex_lookup(s, table, qi, ri);
+  const float g0 = p0 >= 0 ? g[rowbase + p0] : 0.f;
   float W = 0.f, sgw = 0.f, dWx = 0.f, dWy = 0.f, sgdx = 0.f, sgdy = 0.f;  // d/d(grid x, grid y)
   for (int q = -K; q <= K; ++q)
     for (int r = -K; r <= K; ++r) {
@@ -159,17 +170,17 @@ __device__ __forceinline__ void soft_hex_bwd(const SensorK& s, const TT* table, 
       float dwda = -w * a * isg;  // dw/dhd
       float wx = dwda * dhx, wy = dwda * dhy;
       int p = hex_lookup(s, table, qi + (float)q, ri + (float)r);
-      float gk = p >= 0 ? g[rowbase + p] : 0.f;
-      W += w; sgw += gk * w; dWx += wx; dWy += wy; sgdx += gk * wx; sgdy += gk * wy;
+      float dg = (p >= 0 ? g[rowbase + p] : 0.f) - g0;
+      W += w; sgw += dg * w; dWx += wx; dWy += wy; sgdx += dg * wx; sgdy += dg * wy;
     }
   const float iW = 1.f / W;
-  gval = sgw * iW;
-  const float gxg = val * iW * (sgdx - gval * dWx), gyg = val * iW * (sgdy - gval * dWy);
+  const float dbar = sgw * iW;
+  gval = g0 + dbar;
+  const float gxg = val * iW * (sgdx - dbar * dWx), gyg = val * iW * (sgdy - dbar * dWy);
   // grid = rotate(x - off, -rot): xg = gc x' - gs y', yg = gs x' + gc y'
   gx = s.gc * gxg + s.gs * gyg;
   gy = -s.gs * gxg + s.gc * gyg;
 }
-
 
 constexpr int kMaxAdjStages = 2;
 
@@ -325,7 +336,8 @@ __global__ void __launch_bounds__(256) k_adjoint(const AdjK p) {
         cur_s = s;
       }
       const int m = (c0 + cl) * 32 + lane;
-      const V3 src = mk(__ldg(p.sources + 3 * s), __ldg(p.sources + 3 * s + 1), __ldg(p.sources + 3 * s + 2));
+      constexpr int SS = (SRC == IACT_SRC_EXTENDED) ? 4 : 3;
+      const V3 src = mk(__ldg(p.sources + SS * s), __ldg(p.sources + SS * s + 1), __ldg(p.sources + SS * s + 2));
       const float v = __ldg(p.values + s);
       const V3 fpos = mk(__ldg(p.facet_pos + 3 * f), __ldg(p.facet_pos + 3 * f + 1), __ldg(p.facet_pos + 3 * f + 2));
       const int rowbase = (MODE == IACT_MODE_RESPONSE) ? s * p.P : 0;
@@ -341,6 +353,10 @@ __global__ void __launch_bounds__(256) k_adjoint(const AdjK p) {
           w = tp - src;
           inv_len = rsqrtf(dot(w, w));
           d = inv_len * w;
+        } else if (SRC == IACT_SRC_EXTENDED) {  // jitter regenerated from its counter
+          float z0, z1;
+          ray_normals(p.seed, s, f, m, z0, z1);
+          d = jitter_dir(rsqrtf(dot(src, src)) * src, __ldg(p.sources + SS * s + 3), z0, z1);
         } else {
           d = src;
         }
@@ -638,9 +654,13 @@ int launch_backward(const iact_scene_t* sc, const iact_sensor_t* sn, int src_typ
     void* const* ev = opts ? opts->kernel_events : nullptr;
     if (ev && ev[0]) cudaEventRecord(static_cast<cudaEvent_t>(ev[0]), st);
     const bool stages = n_mir > 0;
+    p.seed = opts ? opts->seed : 0u;
     if (src_type == IACT_SRC_POINT)
       rc = soft ? adj_stages<IACT_SRC_POINT, true>(stages, mode, p, block, smem, st)
                 : adj_stages<IACT_SRC_POINT, false>(stages, mode, p, block, smem, st);
+    else if (src_type == IACT_SRC_EXTENDED)
+      rc = soft ? adj_stages<IACT_SRC_EXTENDED, true>(stages, mode, p, block, smem, st)
+                : adj_stages<IACT_SRC_EXTENDED, false>(stages, mode, p, block, smem, st);
     else
       rc = soft ? adj_stages<IACT_SRC_PARALLEL, true>(stages, mode, p, block, smem, st)
                 : adj_stages<IACT_SRC_PARALLEL, false>(stages, mode, p, block, smem, st);

@@ -84,8 +84,8 @@ int check_common(const iact_scene_t* sc, const iact_sensor_t* sn, int32_t src_ty
   if (rc) return rc;
   rc = validate_sensor(sn);
   if (rc) return rc;
-  if (src_type != IACT_SRC_POINT && src_type != IACT_SRC_PARALLEL)
-    return set_error(IACT_E_INVALID, "source_type must be IACT_SRC_POINT or IACT_SRC_PARALLEL");
+  if (src_type != IACT_SRC_POINT && src_type != IACT_SRC_PARALLEL && src_type != IACT_SRC_EXTENDED)
+    return set_error(IACT_E_INVALID, "source_type must be IACT_SRC_POINT, IACT_SRC_PARALLEL or IACT_SRC_EXTENDED");
   if (S < 0) return set_error(IACT_E_INVALID, "negative source count");
   if (S > 0 && (!sources || !values)) return set_error(IACT_E_INVALID, "sources/values are NULL");
   const WsLayout L = workspace_for(sc, sn, S, mode);
@@ -152,14 +152,15 @@ int iact_render(const iact_scene_t* scene, const iact_sensor_t* sensor, int32_t 
 
 int iact_render_debug(const iact_scene_t* scene, const iact_sensor_t* sensor, int32_t source_type,
                       const float* sources, const float* values, int32_t n_sources, float* pts, float* vals,
-                      int32_t* pix, int32_t* hit_mirror, void* workspace, size_t workspace_bytes, void* stream) {
+                      int32_t* pix, int32_t* hit_mirror, void* workspace, size_t workspace_bytes, uint32_t seed,
+                      void* stream) {
   int rc = check_common(scene, sensor, source_type, sources, values, n_sources, IACT_MODE_DEBUG, workspace,
                         workspace_bytes);
   if (rc) return rc;
   const long long n = (long long)scene->n_facets * n_sources * scene->n_samples;
   if (n > 0 && (!pts || !vals)) return set_error(IACT_E_INVALID, "pts/vals are NULL");
   return launch_debug(scene, sensor, source_type, sources, values, n_sources, pts, vals, pix, hit_mirror,
-                      workspace, workspace_bytes, static_cast<cudaStream_t>(stream));
+                      workspace, workspace_bytes, seed, static_cast<cudaStream_t>(stream));
 }
 
 int iact_render_backward(const iact_scene_t* scene, const iact_sensor_t* sensor, int32_t source_type,
@@ -175,6 +176,8 @@ int iact_render_backward(const iact_scene_t* scene, const iact_sensor_t* sensor,
   if (rc) return rc;
   if (scene->n_stages > 2)
     return set_error(IACT_E_UNSUPPORTED, "iact_render_backward: at most 2 mirror stages after the primary");
+  if (source_type == IACT_SRC_EXTENDED && g_sources)
+    return set_error(IACT_E_UNSUPPORTED, "iact_render_backward: no source gradients for extended sources");
   if (!grad_out && acc_elems(sensor, n_sources, mode) > 0) return set_error(IACT_E_INVALID, "grad_out is NULL");
   return launch_backward(scene, sensor, source_type, sources, values, n_sources, mode, grad_out, g_facet_rot,
                          g_facet_pos, g_facet_scale, g_sources, g_values, g_mirror_rot, g_mirror_pos,

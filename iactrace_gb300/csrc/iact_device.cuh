@@ -490,3 +490,49 @@ __device__ __forceinline__ void sag_derivs(const float* m, double rho, SagD& o) 
 }
 
 }  // namespace iact
+
+namespace iact {
+
+// Counter-based generator for per-ray jitter: Philox4x32-10 (Salmon, Moraes,
+// Dror, Shaw, "Parallel random numbers: as easy as 1, 2, 3", SC 2011).
+__host__ __device__ __forceinline__ void philox4x32_10(uint32_t c[4], uint32_t k0, uint32_t k1) {
+  const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u, W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#pragma unroll
+  for (int i = 0; i < 10; ++i) {
+    const uint64_t p0 = (uint64_t)M0 * c[0], p1 = (uint64_t)M1 * c[2];
+    const uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+    const uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+    const uint32_t n0 = hi1 ^ c[1] ^ k0, n2 = hi0 ^ c[3] ^ k1;
+    c[0] = n0; c[1] = lo1; c[2] = n2; c[3] = lo0;
+    k0 += W0;
+    k1 += W1;
+  }
+}
+
+// Two N(0,1) draws for ray (source s, facet f, sample m) by Box-Muller on
+// the first two Philox words: u1 in (0, 1], u2 in [0, 1), 24-bit resolution.
+__device__ __forceinline__ void ray_normals(uint32_t seed, int s, int f, int m, float& z0, float& z1) {
+  uint32_t c[4] = {(uint32_t)m, (uint32_t)f, (uint32_t)s, 0x1ACE7u};
+  philox4x32_10(c, seed, 0x5EEDu);
+  const float u1 = (float)((c[0] >> 8) + 1u) * (1.0f / 16777216.0f);
+  const float u2 = (float)(c[1] >> 8) * (1.0f / 16777216.0f);
+  const float rad = sqrtf(-2.f * logf(u1));
+  float sn, cs;
+  sincospif(2.f * u2, &sn, &cs);
+  z0 = rad * cs;
+  z1 = rad * sn;
+}
+
+// Extended source: unit direction dh (normalised source direction) tilted by
+// sigma * (z0 t1 + z1 t2) in its tangent plane, t1 = normalize(dh x ref),
+// ref = x if |dh_z| > 0.9 else z (the basis of core/reflection.py:40-47), t2 = dh x t1.
+__device__ __forceinline__ V3 jitter_dir(V3 dh, float sigma, float z0, float z1) {
+  const V3 ref = fabsf(dh.z) > 0.9f ? mk(1.f, 0.f, 0.f) : mk(0.f, 0.f, 1.f);
+  V3 t1 = mk(dh.y * ref.z - dh.z * ref.y, dh.z * ref.x - dh.x * ref.z, dh.x * ref.y - dh.y * ref.x);
+  t1 = rsqrtf(dot(t1, t1)) * t1;
+  const V3 t2 = mk(dh.y * t1.z - dh.z * t1.y, dh.z * t1.x - dh.x * t1.z, dh.x * t1.y - dh.y * t1.x);
+  V3 d = dh + sigma * (z0 * t1 + z1 * t2);
+  return rsqrtf(dot(d, d)) * d;
+}
+
+}  // namespace iact

@@ -51,7 +51,7 @@ int launch_render(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type,
                   void* ws, size_t ws_bytes, const iact_opts_t* opts, cudaStream_t stream);
 int launch_debug(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type,
                  const float* sources, const float* values, int S, float* pts, float* vals,
-                 int32_t* pix, int32_t* hit_mirror, void* ws, size_t ws_bytes,
+                 int32_t* pix, int32_t* hit_mirror, void* ws, size_t ws_bytes, uint32_t seed,
                  cudaStream_t stream);
 
 int launch_probe_fma(float* out, int blocks, int iters, cudaStream_t stream);

@@ -17,11 +17,11 @@ class Telescope:
         self.sensors = list(sensors) if sensors else []
         self.name = name
 
-    def __call__(self, sources, values, source_type="point", sensor_idx: int = 0, debug: bool = False):
-        """telescope/telescope.py:56-83."""
+    def __call__(self, sources, values, source_type="point", sensor_idx: int = 0, debug: bool = False, seed: int = 0):
+        """telescope/telescope.py:56-83 (seed: jitter stream of 'extended' sources)."""
         if debug:
-            return render_debug(self, sources, values, source_type, sensor_idx)
-        return render(self, sources, values, source_type, sensor_idx)
+            return render_debug(self, sources, values, source_type, sensor_idx, seed=seed)
+        return render(self, sources, values, source_type, sensor_idx, seed=seed)
 
     def __getstate__(self):
         st = dict(self.__dict__)

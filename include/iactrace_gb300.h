@@ -55,7 +55,11 @@ extern "C" {
 #define IACT_MAX_STAGE_MIRRORS 64 /* mirrors over all stages >= 1          */
 #define IACT_MAX_OBSTRUCTIONS 2048 /* primitives over all obstruction kinds */
 
-enum { IACT_SRC_POINT = 0, IACT_SRC_PARALLEL = 1 };
+/* EXTENDED: a parallel source with a Gaussian angular profile; sources are
+ * [S,4] = (direction xyz, sigma in radians); each ray's direction is the
+ * normalised direction tilted by sigma * (z0, z1) in its tangent plane, with
+ * (z0, z1) ~ N(0,1) from Philox4x32-10 keyed on (opts->seed, s, f, m). */
+enum { IACT_SRC_POINT = 0, IACT_SRC_PARALLEL = 1, IACT_SRC_EXTENDED = 2 };
 enum { IACT_MODE_IMAGE = 0, IACT_MODE_RESPONSE = 1, IACT_MODE_DEBUG = 2, IACT_MODE_BACKWARD = 3 };
 enum {
   IACT_SENSOR_SQUARE = 0,      /* sensors/square.py:28-91     SquareSensor */
@@ -133,6 +137,7 @@ typedef struct {
   int32_t sources_per_cta;  /* warps per CTA each own one source at a time */
   int32_t facets_per_tile;  /* primary facets per work tile               */
   int32_t hist_mode;        /* 0 auto, 1 shared-memory rows, 2 global     */
+  uint32_t seed;            /* jitter stream of EXTENDED sources            */
   /* optional cudaEvent_t pair recorded on `stream` right before and after
    * the render kernel (profiling); NULL to skip */
   void* kernel_events[2];
@@ -192,7 +197,8 @@ int iact_render_debug(const iact_scene_t* scene, const iact_sensor_t* sensor,
                       int32_t source_type, const float* sources,
                       const float* values, int32_t n_sources, float* pts,
                       float* vals, int32_t* pix, int32_t* hit_mirror,
-                      void* workspace, size_t workspace_bytes, void* stream);
+                      void* workspace, size_t workspace_bytes, uint32_t seed,
+                      void* stream);
 
 /* Adjoint of iact_render (mode IMAGE or RESPONSE), scenes with at most two
  * mirror stages after the primary: given grad_out = dL/d(out), writes

@@ -40,7 +40,8 @@ void deposit_ray(const iact_sensor_t& sn, T x, T y, T v, T* row) {
 // reference's lax.scan order when n_threads == 1.
 template <typename T>
 int render_impl(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type, const float* sources,
-                const float* values, int S, int mode, T* out, int n_threads) {
+                const float* values, int S, int mode, T* out, int n_threads, uint32_t seed) {
+  const int SS = src_type == IACT_SRC_EXTENDED ? 4 : 3;
   if (!scene_ok(sc, sn, S)) return IACT_E_INVALID;
   const size_t P = (size_t)sn->n_pixels;
   const size_t F = (size_t)sc->n_facets, M = (size_t)sc->n_samples;
@@ -57,7 +58,7 @@ int render_impl(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type, c
       T* row = out + (size_t)s * P;
       for (size_t f = 0; f < F; ++f) {
         for (size_t m = 0; m < M; ++m) {
-          RayOut<T> r = trace_ray<T>(*sc, pr, w, f * M + m, src_type, sources + 3 * s, T(values[s]));
+          RayOut<T> r = trace_ray<T>(*sc, pr, w, f * M + m, src_type, sources + SS * s, T(values[s]), seed, s);
           deposit_ray<T>(*sn, r.x, r.y, r.val, row);
         }
       }
@@ -71,7 +72,8 @@ int render_impl(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type, c
     T* img = acc[(size_t)omp_get_thread_num()].data();
     for (int s = 0; s < S; ++s)
       for (size_t m = 0; m < M; ++m) {
-        RayOut<T> r = trace_ray<T>(*sc, pr, w, (size_t)f * M + m, src_type, sources + 3 * s, T(values[s]));
+        RayOut<T> r = trace_ray<T>(*sc, pr, w, (size_t)f * M + m, src_type, sources + SS * s, T(values[s]),
+                                   seed, s);
         deposit_ray<T>(*sn, r.x, r.y, r.val, img);
       }
   }
@@ -84,7 +86,8 @@ int render_impl(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type, c
 template <typename T>
 int debug_impl(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type, const float* sources,
                const float* values, int S, T* pts, T* vals, int32_t* pix, int32_t* hit_mirror,
-               T* margin) {
+               T* margin, uint32_t seed) {
+  const int SS = src_type == IACT_SRC_EXTENDED ? 4 : 3;
   if (!scene_ok(sc, sn, S)) return IACT_E_INVALID;
   const size_t F = (size_t)sc->n_facets, M = (size_t)sc->n_samples;
   if (F == 0 || M == 0 || S == 0) return IACT_OK;
@@ -95,7 +98,8 @@ int debug_impl(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type, co
     for (int s = 0; s < S; ++s)
       for (size_t m = 0; m < M; ++m) {
         size_t i = ((size_t)f * S + s) * M + m;
-        RayOut<T> r = trace_ray<T>(*sc, pr, w, (size_t)f * M + m, src_type, sources + 3 * s, T(values[s]));
+        RayOut<T> r = trace_ray<T>(*sc, pr, w, (size_t)f * M + m, src_type, sources + SS * s, T(values[s]),
+                                   seed, s);
         pts[2 * i] = r.x;
         pts[2 * i + 1] = r.y;
         vals[i] = r.val;
@@ -121,26 +125,28 @@ extern "C" {
 
 int oracle_render_f64(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type,
                       const float* sources, const float* values, int S, int mode, double* out,
-                      int n_threads) {
-  return render_impl<double>(sc, sn, src_type, sources, values, S, mode, out, n_threads);
+                      int n_threads, uint32_t seed) {
+  return render_impl<double>(sc, sn, src_type, sources, values, S, mode, out, n_threads, seed);
 }
 
 int oracle_render_f32(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type,
                       const float* sources, const float* values, int S, int mode, float* out,
-                      int n_threads) {
-  return render_impl<float>(sc, sn, src_type, sources, values, S, mode, out, n_threads);
+                      int n_threads, uint32_t seed) {
+  return render_impl<float>(sc, sn, src_type, sources, values, S, mode, out, n_threads, seed);
 }
 
 int oracle_render_debug_f64(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type,
                             const float* sources, const float* values, int S, double* pts,
-                            double* vals, int32_t* pix, int32_t* hit_mirror, double* margin) {
-  return debug_impl<double>(sc, sn, src_type, sources, values, S, pts, vals, pix, hit_mirror, margin);
+                            double* vals, int32_t* pix, int32_t* hit_mirror, double* margin,
+                            uint32_t seed) {
+  return debug_impl<double>(sc, sn, src_type, sources, values, S, pts, vals, pix, hit_mirror, margin, seed);
 }
 
 int oracle_render_debug_f32(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type,
                             const float* sources, const float* values, int S, float* pts,
-                            float* vals, int32_t* pix, int32_t* hit_mirror, float* margin) {
-  return debug_impl<float>(sc, sn, src_type, sources, values, S, pts, vals, pix, hit_mirror, margin);
+                            float* vals, int32_t* pix, int32_t* hit_mirror, float* margin,
+                            uint32_t seed) {
+  return debug_impl<float>(sc, sn, src_type, sources, values, S, pts, vals, pix, hit_mirror, margin, seed);
 }
 
 // telescope/mirrors.py:64-79 transform_to_world, for direct checks

@@ -630,6 +630,48 @@ inline World<T> transform_to_world(const iact_scene_t& sc) {
   return w;
 }
 
+// Philox4x32-10 (Salmon et al., SC 2011): the per-ray jitter stream of
+// extended sources (include/iactrace_gb300.h, IACT_SRC_EXTENDED).
+inline void philox4x32_10(uint32_t c[4], uint32_t k0, uint32_t k1) {
+  const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u, W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+  for (int i = 0; i < 10; ++i) {
+    const uint64_t p0 = (uint64_t)M0 * c[0], p1 = (uint64_t)M1 * c[2];
+    const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c[1] ^ k0, n2 = (uint32_t)(p0 >> 32) ^ c[3] ^ k1;
+    c[1] = (uint32_t)p1;
+    c[3] = (uint32_t)p0;
+    c[0] = n0;
+    c[2] = n2;
+    k0 += W0;
+    k1 += W1;
+  }
+}
+
+template <typename T>
+inline void ray_normals(uint32_t seed, int s, int f, int m, T* z0, T* z1) {
+  uint32_t c[4] = {(uint32_t)m, (uint32_t)f, (uint32_t)s, 0x1ACE7u};
+  philox4x32_10(c, seed, 0x5EEDu);
+  const T u1 = T((c[0] >> 8) + 1u) * T(1.0 / 16777216.0);
+  const T u2 = T(c[1] >> 8) * T(1.0 / 16777216.0);
+  const T rad = std::sqrt(T(-2) * std::log(u1));
+  *z0 = rad * std::cos(T(2 * M_PI) * u2);
+  *z1 = rad * std::sin(T(2 * M_PI) * u2);
+}
+
+// direction dh tilted by sigma (z0 t1 + z1 t2), tangent basis as
+// core/reflection.py:40-47
+template <typename T>
+inline Vec3<T> jitter_dir(Vec3<T> dh, T sigma, T z0, T z1) {
+  Vec3<T> ref = std::fabs(dh.z) > T(0.9) ? Vec3<T>{1, 0, 0} : Vec3<T>{0, 0, 1};
+  Vec3<T> t1 = cross3(dh, ref);
+  T n1 = norm3(t1);
+  t1 = {t1.x / n1, t1.y / n1, t1.z / n1};
+  Vec3<T> t2 = cross3(dh, t1);
+  Vec3<T> d = {dh.x + sigma * (z0 * t1.x + z1 * t2.x), dh.y + sigma * (z0 * t1.y + z1 * t2.y),
+               dh.z + sigma * (z0 * t1.z + z1 * t2.z)};
+  T nd = norm3(d);
+  return {d.x / nd, d.y / nd, d.z / nd};
+}
+
 template <typename T>
 struct RayOut {
   T x, y, val;
@@ -665,13 +707,22 @@ inline Prepared<T> prepare(const iact_scene_t& sc, const iact_sensor_t& sn) {
 // core/render.py:44-115 _reflect_at_stage / _intersect_group for stages >= 1
 template <typename T>
 inline RayOut<T> trace_ray(const iact_scene_t& sc, const Prepared<T>& pr, const World<T>& w,
-                           size_t sample, int src_type, const float* src, T value) {
+                           size_t sample, int src_type, const float* src, T value, uint32_t seed = 0,
+                           int s = 0) {
   Vec3<T> tp = w.tp[sample], tn = w.tn[sample];
   Vec3<T> d;
   if (src_type == IACT_SRC_POINT) {
     Vec3<T> dd = sub3(tp, ld3<T>(src));
     T nn = norm3(dd);
     d = {dd.x / nn, dd.y / nn, dd.z / nn};
+  } else if (src_type == IACT_SRC_EXTENDED) {
+    const int M = sc.n_samples;
+    const int f = (int)(sample / (size_t)M), m = (int)(sample % (size_t)M);
+    T z0, z1;
+    ray_normals<T>(seed, s, f, m, &z0, &z1);
+    Vec3<T> dh = ld3<T>(src);
+    T nh = norm3(dh);
+    d = jitter_dir<T>({dh.x / nh, dh.y / nh, dh.z / nh}, T(src[3]), z0, z1);
   } else {
     d = ld3<T>(src);
   }

@@ -40,12 +40,12 @@ def load():
     if _lib is None:
         build()
         lib = ctypes.CDLL(LIB)
-        vp, i = ctypes.c_void_p, ctypes.c_int
+        vp, i, u = ctypes.c_void_p, ctypes.c_int, ctypes.c_uint32
         for name in ("oracle_render_f64", "oracle_render_f32"):
-            getattr(lib, name).argtypes = [vp, vp, i, vp, vp, i, i, vp, i]
+            getattr(lib, name).argtypes = [vp, vp, i, vp, vp, i, i, vp, i, u]
             getattr(lib, name).restype = i
         for name in ("oracle_render_debug_f64", "oracle_render_debug_f32"):
-            getattr(lib, name).argtypes = [vp, vp, i, vp, vp, i, vp, vp, vp, vp, vp]
+            getattr(lib, name).argtypes = [vp, vp, i, vp, vp, i, vp, vp, vp, vp, vp, u]
             getattr(lib, name).restype = i
         lib.oracle_transform_f64.argtypes = [vp, vp, vp, vp]
         lib.oracle_max_threads.restype = i
@@ -54,27 +54,28 @@ def load():
 
 
 def _host(tel, sensor_idx):
-    from iactrace_gb300.core.scene import PackedScene
-    ps = PackedScene(tel, "cpu")
+    from iactrace_gb300.core.scene import pack_scene
+    ps = pack_scene(tel, "cpu")
     sdesc, keep = tel.sensors[sensor_idx].pack("cpu")
     return ps, sdesc, keep
 
 
-def _src(sources, values):
-    s = np.ascontiguousarray(torch.as_tensor(sources).detach().cpu().float().numpy().reshape(-1, 3))
+def _src(sources, values, source_type="point"):
+    width = 4 if source_type == "extended" else 3
+    s = np.ascontiguousarray(torch.as_tensor(sources).detach().cpu().float().numpy().reshape(-1, width))
     v = np.ascontiguousarray(torch.as_tensor(values).detach().cpu().float().numpy().reshape(-1))
     return s, v
 
 
 def source_code(source_type) -> int:
-    return 0 if source_type == "point" else 1
+    return {"point": 0, "extended": 2}.get(source_type, 1)
 
 
-def render(tel, sources, values, source_type="point", sensor_idx=0, mode="image", dtype="f64", threads=1):
+def render(tel, sources, values, source_type="point", sensor_idx=0, mode="image", dtype="f64", threads=1, seed=0):
     """Image (accumulator shape) or response matrix (S, P) from the oracle."""
     lib = load()
     ps, sd, keep = _host(tel, sensor_idx)
-    s, v = _src(sources, values)
+    s, v = _src(sources, values, source_type)
     S = s.shape[0]
     P = int(math.prod(tel.sensors[sensor_idx].get_accumulator_shape()))
     m = 1 if mode == "response" else 0
@@ -83,18 +84,18 @@ def render(tel, sources, values, source_type="point", sensor_idx=0, mode="image"
     fn = lib.oracle_render_f64 if dtype == "f64" else lib.oracle_render_f32
     if ps.F and ps.M:
         rc = fn(ctypes.addressof(ps.desc), ctypes.addressof(sd), source_code(source_type), s.ctypes.data,
-                v.ctypes.data, S, m, out.ctypes.data, threads)
+                v.ctypes.data, S, m, out.ctypes.data, threads, seed)
         if rc:
             raise RuntimeError(f"oracle render failed: {rc}")
     del keep
     return out if m else out.reshape(tel.sensors[sensor_idx].get_accumulator_shape())
 
 
-def render_debug(tel, sources, values, source_type="point", sensor_idx=0, dtype="f64"):
+def render_debug(tel, sources, values, source_type="point", sensor_idx=0, dtype="f64", seed=0):
     """Per-ray (x, y), value, hard pixel id, last stage-mirror hit, pixel-edge margin."""
     lib = load()
     ps, sd, keep = _host(tel, sensor_idx)
-    s, v = _src(sources, values)
+    s, v = _src(sources, values, source_type)
     S = s.shape[0]
     n = ps.F * S * ps.M
     npd = np.float64 if dtype == "f64" else np.float32
@@ -106,7 +107,8 @@ def render_debug(tel, sources, values, source_type="point", sensor_idx=0, dtype=
     fn = lib.oracle_render_debug_f64 if dtype == "f64" else lib.oracle_render_debug_f32
     if n:
         rc = fn(ctypes.addressof(ps.desc), ctypes.addressof(sd), source_code(source_type), s.ctypes.data,
-                v.ctypes.data, S, pts.ctypes.data, vals.ctypes.data, pix.ctypes.data, hm.ctypes.data, mg.ctypes.data)
+                v.ctypes.data, S, pts.ctypes.data, vals.ctypes.data, pix.ctypes.data, hm.ctypes.data, mg.ctypes.data,
+                seed)
         if rc:
             raise RuntimeError(f"oracle debug failed: {rc}")
     del keep

@@ -19,7 +19,7 @@ import torch
 from iactrace_gb300 import _native as N
 from iactrace_gb300 import workloads as W
 from iactrace_gb300.core.render import source_code
-from iactrace_gb300.core.scene import PackedScene
+from iactrace_gb300.core.scene import pack_scene
 
 pytestmark = pytest.mark.gpu
 
@@ -49,7 +49,7 @@ def test_noalloc_matches_workspace_render_twice(cuda, mode):
     lib = N.load()
     fn = _bind(lib)
     tel, src, val, st = W.plain_forward(n_samples=128, n_sources=8)
-    ps = PackedScene(tel, cuda)
+    ps = pack_scene(tel, cuda)
     sd, keep = tel.sensors[0].pack(cuda)
     src, val = src.to(cuda).contiguous(), val.to(cuda).contiguous()
     P = tel.sensors[0].n_pixels
@@ -73,7 +73,7 @@ def test_noalloc_rejects_work_beyond_its_scratch(cuda):
     lib = N.load()
     fn = _bind(lib)
     tel, src, val, st = W.response_matrix(n_samples=8, n_side=64)  # 4096 x 2048 FP64 accumulator
-    ps = PackedScene(tel, cuda)
+    ps = pack_scene(tel, cuda)
     sd, keep = tel.sensors[0].pack(cuda)
     src, val = src.to(cuda).contiguous(), val.to(cuda).contiguous()
     out = torch.zeros((src.shape[0], tel.sensors[0].n_pixels), device=cuda)

@@ -90,6 +90,48 @@ def _gprime(t, ox, oy, oz, dx, dy, dz, x0, y0, c, k, asph):
     return dz - (sr * 2 * xs * dx + sr * 2 * ys * dy)
 
 
+def philox_normals(seed, F, S, M):
+    """N(0,1) pairs of every ray (f, s, m) from Philox4x32-10 (the extended-
+    source jitter stream), Box-Muller in float64: arrays (F, S, M)."""
+    m = np.arange(M, dtype=np.uint64)[None, None, :]
+    f = np.arange(F, dtype=np.uint64)[:, None, None]
+    s = np.arange(S, dtype=np.uint64)[None, :, None]
+    shape = (F, S, M)
+    c0 = np.broadcast_to(m, shape).astype(np.uint64)
+    c1 = np.broadcast_to(f, shape).astype(np.uint64)
+    c2 = np.broadcast_to(s, shape).astype(np.uint64)
+    c3 = np.full(shape, 0x1ACE7, np.uint64)
+    k0, k1 = np.uint64(seed & 0xFFFFFFFF), np.uint64(0x5EED)
+    M0, M1, W0, W1 = np.uint64(0xD2511F53), np.uint64(0xCD9E8D57), np.uint64(0x9E3779B9), np.uint64(0xBB67AE85)
+    mask = np.uint64(0xFFFFFFFF)
+    for _ in range(10):
+        p0, p1 = M0 * c0, M1 * c2
+        n0 = ((p1 >> np.uint64(32)) ^ c1 ^ k0) & mask
+        n2 = ((p0 >> np.uint64(32)) ^ c3 ^ k1) & mask
+        c1, c3 = p1 & mask, p0 & mask
+        c0, c2 = n0, n2
+        k0, k1 = (k0 + W0) & mask, (k1 + W1) & mask
+    u1 = ((c0 >> np.uint64(8)) + np.uint64(1)).astype(np.float64) / 16777216.0
+    u2 = (c1 >> np.uint64(8)).astype(np.float64) / 16777216.0
+    rad = np.sqrt(-2.0 * np.log(u1))
+    return rad * np.cos(2 * np.pi * u2), rad * np.sin(2 * np.pi * u2)
+
+
+def jitter_dirs(src, z0, z1):
+    """Extended sources (S, 4): unit direction tilted by sigma (z0 t1 + z1 t2)."""
+    dh = src[:, :3] / torch.linalg.norm(src[:, :3], dim=-1, keepdim=True)
+    ex = torch.tensor([1.0, 0.0, 0.0], dtype=D).expand_as(dh)
+    ez = torch.tensor([0.0, 0.0, 1.0], dtype=D).expand_as(dh)
+    ref = torch.where((torch.abs(dh[:, 2:3]) > 0.9), ex, ez)
+    t1 = torch.linalg.cross(dh, ref)
+    t1 = t1 / torch.linalg.norm(t1, dim=-1, keepdim=True)
+    t2 = torch.linalg.cross(dh, t1)
+    z0, z1 = torch.as_tensor(z0, dtype=D), torch.as_tensor(z1, dtype=D)
+    sig = src[:, 3][None, :, None, None]
+    d = dh[None, :, None, :] + sig * (z0[..., None] * t1[None, :, None, :] + z1[..., None] * t2[None, :, None, :])
+    return d / torch.linalg.norm(d, dim=-1, keepdim=True)
+
+
 def render(scene, params, decisions, sensor, mode="image"):
     """Image (P,) or response (S, P) as a differentiable function of params.
 
@@ -113,6 +155,9 @@ def render(scene, params, decisions, sensor, mode="image"):
     if scene["source_type"] == "point":
         wv = tp4 - params["src"][None, :, None, :]
         d = wv / torch.linalg.norm(wv, dim=-1, keepdim=True)
+    elif scene["source_type"] == "extended":
+        z0, z1 = philox_normals(scene.get("seed", 0), F, S, M)
+        d = jitter_dirs(params["src"], z0, z1)
     else:
         d = params["src"][None, :, None, :].expand(F, S, M, 3)
     c = (d * nn4).sum(-1)
