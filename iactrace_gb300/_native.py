@@ -37,6 +37,7 @@ SENSOR_SQUARE = 0
 SENSOR_HEX = 1
 SENSOR_SOFT_SQUARE = 2
 SENSOR_SOFT_HEX = 3
+FLAG_NO_CULL = 1
 APERTURE_DISK = 0
 APERTURE_POLYGON = 1
 
@@ -87,7 +88,13 @@ class IactSensor(ctypes.Structure):
 
 class IactOpts(ctypes.Structure):
     _fields_ = [("block_threads", _i), ("sources_per_cta", _i), ("facets_per_tile", _i), ("hist_mode", _i),
-                ("seed", ctypes.c_uint32), ("kernel_events", ctypes.c_void_p * 2)]
+                ("tasks_per_warp", _i), ("flags", _i), ("seed", ctypes.c_uint32), ("kernel_events", ctypes.c_void_p * 2)]
+
+
+class IactJob(ctypes.Structure):
+    _fields_ = [("scene", ctypes.POINTER(IactScene)), ("sensor", ctypes.POINTER(IactSensor)),
+                ("sources", ctypes.c_void_p), ("values", ctypes.c_void_p), ("n_sources", _i),
+                ("seed", ctypes.c_uint32), ("out", ctypes.c_void_p)]
 
 
 class IactError(RuntimeError):
@@ -117,6 +124,13 @@ _SIGS = {
     "iact_render_debug": ([ctypes.POINTER(IactScene), ctypes.POINTER(IactSensor), _i, ctypes.c_void_p,
                            ctypes.c_void_p, _i, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                            ctypes.c_void_p, ctypes.c_size_t, ctypes.c_uint32, ctypes.c_void_p], ctypes.c_int),
+    "iact_batch_create": ([ctypes.POINTER(IactJob), _i, _i, _i, ctypes.POINTER(IactOpts),
+                           ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
+    "iact_batch_workspace_size": ([ctypes.c_void_p, ctypes.POINTER(ctypes.c_size_t)], ctypes.c_int),
+    "iact_batch_prepare": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p], ctypes.c_int),
+    "iact_batch_render": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "iact_batch_info": ([ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64), _i], ctypes.c_int),
+    "iact_batch_destroy": ([ctypes.c_void_p], None),
 }
 
 # symbols declared by include/iactrace_gb300.h that bindings resolve
@@ -152,11 +166,12 @@ def load(build_if_missing: bool = False):
 
 
 def check_layout(lib) -> None:
-    out = (ctypes.c_size_t * 4)()
-    rc = lib.iact_abi_layout(out, 4)
+    out = (ctypes.c_size_t * 5)()
+    rc = lib.iact_abi_layout(out, 5)
     if rc != IACT_OK:
         raise IactError(rc, "iact_abi_layout failed")
-    mine = [ctypes.sizeof(IactScene), ctypes.sizeof(IactSensor), ctypes.sizeof(IactMirror), ctypes.sizeof(IactOpts)]
+    mine = [ctypes.sizeof(IactScene), ctypes.sizeof(IactSensor), ctypes.sizeof(IactMirror), ctypes.sizeof(IactOpts),
+            ctypes.sizeof(IactJob)]
     if list(out) != mine:
         raise ImportError(f"ABI struct layout mismatch: library {list(out)} vs binding {mine}")
 

@@ -10,7 +10,10 @@ the nominal orientation by Adam on the L2 image loss, with gradients from the
 adjoint kernel (recompute-based, behind torch.autograd).
 
 Only facet tips and tilts are free; sources, samples and the camera are the
-same in the target and the fit.
+same in the target and the fit. The image loss is the objective: the
+individual tilts are only weakly identifiable from one summed image (two
+facets whose spots trade places give almost the same image), so the RMS tilt
+error is reported beside the loss but is not expected to fall with it.
 """
 from __future__ import annotations
 
@@ -105,7 +108,7 @@ def run(prob, steps: int = 200, lr: float = 2e-3, log_every: int = 0):
         opt.step()
         torch.cuda.synchronize()
         hist["step_ms"].append((time.perf_counter() - t0) * 1e3)
-        hist["loss"].append(float(loss))
+        hist["loss"].append(float(loss.detach()))
         hist["rms_mrad"].append(rms_tilt_error_mrad(rot, prob["truth"]))
         if log_every and (it % log_every == 0 or it == steps - 1):
             print(f"step {it:4d} loss {hist['loss'][-1]:.4e} rms tilt error {hist['rms_mrad'][-1]:.3f} mrad")

@@ -1,4 +1,5 @@
 from .apertures import Aperture, DiskAperture, PolygonAperture
+from .batch import BatchRenderer
 from .integrators import Integrator, MCIntegrator
 from .obstructions import (Box, BoxGroup, Cylinder, CylinderGroup, Obstruction, ObstructionGroup, OrientedBox,
                            OrientedBoxGroup, Sphere, SphereGroup, Triangle, TriangleGroup, group_obstructions)
@@ -10,7 +11,7 @@ from .transforms import euler_to_matrix, look_at_euler, look_at_rotation
 __all__ = [
     "AsphericSurface", "Aperture", "DiskAperture", "PolygonAperture", "Integrator", "MCIntegrator",
     "compute_perturbation_delta", "reflect", "euler_to_matrix", "look_at_rotation", "look_at_euler",
-    "render", "render_debug", "render_response_matrix",
+    "render", "render_debug", "render_response_matrix", "BatchRenderer",
     "Obstruction", "ObstructionGroup", "Cylinder", "CylinderGroup", "Box", "BoxGroup", "Sphere", "SphereGroup",
     "OrientedBox", "OrientedBoxGroup", "Triangle", "TriangleGroup", "group_obstructions",
 ]

@@ -169,6 +169,16 @@ def pack_scene(tel, device, facets=None) -> PackedScene:
         ps = PackedScene(tel, device)
         cache[key] = (fp, ps)
     if facets is None:
-        facets = tuple(t.detach().contiguous() for t in primary_params(tel, ps.device))
+        # device copies of the facet transforms, reused while the source
+        # tensors are the same objects at the same version (kept alive here so
+        # their ids stay unique)
+        src = [t for g in stages_of(tel).get(0, []) for t in (g.rotations, g.positions, g.perturbation_scale)]
+        fkey = tuple((id(t), getattr(t, "_version", 0)) for t in src)
+        cached = ps.__dict__.get("_facet_cache")
+        if cached is not None and cached[0] == fkey:
+            facets = cached[2]
+        else:
+            facets = tuple(t.detach().contiguous() for t in primary_params(tel, ps.device))
+            ps._facet_cache = (fkey, src, facets)
     ps.set_facets(*facets)
     return ps

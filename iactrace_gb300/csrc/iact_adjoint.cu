@@ -56,6 +56,8 @@ struct AdjK {
   int SB, FC, CC, n_fchunk, n_cchunk, n_tiles;
   int* counter;
   uint32_t seed;  // jitter stream of extended sources
+  const float4* B4;  // per (facet, chunk) bundle bounds (culling on)
+  int n_words;       // 32-bit candidate-mask words per task; 0 = no culling
 };
 
 // Per-lane running sums of one (facet, source) stream of rays.
@@ -294,6 +296,7 @@ __global__ void __launch_bounds__(256) k_adjoint(const AdjK p) {
   for (int i = threadIdx.x; i < htab_n; i += nthr)
     htab[i] = (short)(i < p.sn.table_q * p.sn.table_r ? p.hex_table[i] : -1);
   float* mgrad = reinterpret_cast<float*>(htab + htab_n);  // [n_mir, kMirGrad] CTA partial sums
+  uint32_t* tmask = reinterpret_cast<uint32_t*>(mgrad + (STAGES ? p.n_mir * kMirGrad : 0));  // tile's candidate masks
   for (int i = threadIdx.x; i < (STAGES ? p.n_mir * kMirGrad : 0); i += nthr) mgrad[i] = 0.f;
   const Obst ob = make_obst(tab, p.n_cyl, p.n_box, p.n_sph, p.n_obox, p.n_tri);
   const float* mir = tab + table_offsets(p.n_cyl, p.n_box, p.n_sph, p.n_obox, p.n_tri, p.n_mir).mir;
@@ -320,6 +323,7 @@ __global__ void __launch_bounds__(256) k_adjoint(const AdjK p) {
     const int s0 = sblk * p.SB, f0 = fc * p.FC, c0 = cc * p.CC;
     const int SBc = min(p.SB, p.S - s0), FCc = min(p.FC, p.F - f0), CCc = min(p.CC, nch - c0);
     const int T = SBc * FCc * CCc;
+    if (p.n_words) tile_masks<SRC>(p.B4, p.sources, p.M, p.n_words, ob, s0, f0, c0, FCc, CCc, T, tmask);
     const int tb = (warp * T) / nw, te = ((warp + 1) * T) / nw;
     int sl = tb / (FCc * CCc);
     int fl = (tb - sl * FCc * CCc) / CCc;
@@ -360,7 +364,7 @@ __global__ void __launch_bounds__(256) k_adjoint(const AdjK p) {
         } else {
           d = src;
         }
-        const bool shadowed = occluded(ob, tp, mk(-d.x, -d.y, -d.z));
+        const bool shadowed = occluded_mask(ob, tmask + t * p.n_words, p.n_words, tp, mk(-d.x, -d.y, -d.z));
         const float c = dot(d, nn);
         const V3 r0 = d - (2.f * c) * nn;
         const float val0 = v * -c * iw;
@@ -568,13 +572,9 @@ namespace {
 template <int SRC, bool SOFT, int MODE, bool STAGES>
 int run_adjoint(const AdjK& p, int block, size_t smem, cudaStream_t st) {
   auto kern = k_adjoint<SRC, SOFT, MODE, STAGES>;
-  if (smem > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return check_cuda(e, "cudaFuncSetAttribute(k_adjoint smem)");
-  }
   int per_sm = 0;
-  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, smem);
-  if (e != cudaSuccess) return check_cuda(e, "occupancy query");
+  const int rc = resident_ctas(reinterpret_cast<const void*>(kern), block, smem, &per_sm);
+  if (rc) return rc;
   if (per_sm < 1) return set_error(IACT_E_UNSUPPORTED, "adjoint kernel does not fit on an SM");
   const int grid = std::max(1, std::min(p.n_tiles, per_sm * device_info().sm_count));
   kern<<<grid, block, smem, st>>>(p);
@@ -632,11 +632,13 @@ int launch_backward(const iact_scene_t* sc, const iact_sensor_t* sn, int src_typ
     p.gmir = gmir;
     p.n_mir = n_mir;
     p.counter = reinterpret_cast<int*>(w + L.counter);
+    p.B4 = L.n_b4 ? reinterpret_cast<const float4*>(w + L.b4) : nullptr;
+    p.n_words = (L.n_b4 && !(opts && (opts->flags & IACT_FLAG_NO_CULL))) ? (n_primitives(sc) + 31) / 32 : 0;
     const int block = (opts && opts->block_threads > 0) ? opts->block_threads : 256;
     const int nw = block / 32;
     const int nch = (p.M + 31) / 32;
     p.SB = std::min(S, nw);
-    const int target = nw * 48;
+    const int target = std::max(1, std::min(nw * 48, p.n_words ? 4096 / p.n_words : 1 << 30));
     p.CC = std::min(nch, std::max(1, target / p.SB));
     p.FC = std::min(F, std::max(1, target / (p.SB * p.CC)));
     p.n_fchunk = (F + p.FC - 1) / p.FC;
@@ -649,7 +651,8 @@ int launch_backward(const iact_scene_t* sc, const iact_sensor_t* sn, int src_typ
     const size_t htab = hex ? (size_t)sn->table_q * sn->table_r : 0;
     const size_t htab_bytes = sizeof(short) * ((htab + 7) & ~(size_t)7);
     p.hex_in_smem = (hex && sn->n_pixels < 32768 && tab_bytes + htab_bytes <= 96 * 1024) ? 1 : 0;
-    const size_t smem = tab_bytes + (p.hex_in_smem ? htab_bytes : 0) + sizeof(float) * (size_t)n_mir * kMirGrad;
+    const size_t smem = tab_bytes + (p.hex_in_smem ? htab_bytes : 0) + sizeof(float) * (size_t)n_mir * kMirGrad +
+                        sizeof(uint32_t) * (size_t)p.n_words * p.SB * p.FC * p.CC;
     const bool soft = sn->type == IACT_SENSOR_SOFT_SQUARE || sn->type == IACT_SENSOR_SOFT_HEX;
     void* const* ev = opts ? opts->kernel_events : nullptr;
     if (ev && ev[0]) cudaEventRecord(static_cast<cudaEvent_t>(ev[0]), st);

@@ -219,6 +219,155 @@ __device__ __forceinline__ bool occluded(const Obst& ob, V3 o, V3 d) {
   return s;
 }
 
+// ------------------------------------------------------ bundle culling
+// The 32 rays of a warp task leave one facet's 32-sample chunk towards one
+// source: their shadow rays lie inside a "thick ray" around an axis ray
+// c + t u (t >= 0), of radius R0 + t * dlt (R0 bounds |o_i - c|, dlt bounds
+// |u_i - u|). A primitive whose bounding volume stays farther than that
+// from the axis ray cannot shadow any ray of the bundle and is skipped; the
+// others (the candidates) get the reference's per-ray test unchanged, so
+// shadow masks are identical to testing every primitive. Bounding volumes:
+// the cylinder's capsule, the box itself, the sphere itself, bounding
+// spheres of oriented boxes and triangles. The reach adds 2 mm + 1e-4 of
+// the distance for float32 rounding of the bundle and of the per-ray tests.
+struct Bundle {
+  V3 c, u;
+  float R0, dlt;
+};
+
+// R0 + t dlt at the farthest distance t a hit on a volume of bounding
+// radius `rad` around `q` can lie from a ray origin, plus the margin
+__device__ __forceinline__ float bundle_reach(const Bundle& b, V3 q, float rad) {
+  V3 w = q - b.c;
+  const float T = sqrtf(dot(w, w)) + rad + b.R0;
+  return b.R0 + T * b.dlt + 2e-3f + 1e-4f * T;
+}
+
+// squared distance from point p to the ray c + t u, t >= 0 (|u| = 1)
+__device__ __forceinline__ float ray_point_d2(const Bundle& b, V3 p) {
+  V3 w = p - b.c;
+  const float t = fmaxf(dot(w, b.u), 0.f);
+  V3 e = w - t * b.u;
+  return dot(e, e);
+}
+
+__device__ __forceinline__ bool sphere_may_hit(const Bundle& b, V3 q, float rad) {
+  const float lim = rad + bundle_reach(b, q, rad);
+  return ray_point_d2(b, q) <= lim * lim;
+}
+
+// capsule (segment p1 + s ax, s in [0, h], radius r) vs the thick ray: the
+// exact minimum distance between the ray and the segment is the smaller of
+// the interior stationary point (if feasible) and the three edge minima
+__device__ __forceinline__ bool capsule_may_hit(const Bundle& b, V3 p1, V3 ax, float h, float r) {
+  const V3 mid = p1 + (0.5f * h) * ax;
+  const float lim = r + bundle_reach(b, mid, 0.5f * h + r);
+  const V3 w0 = b.c - p1;
+  const float bb = dot(b.u, ax), d = dot(b.u, w0), e = dot(ax, w0);
+  const float den = 1.f - bb * bb;
+  if (den < 1e-2f) return true;  // ray within ~6 deg of the axis: always a candidate
+  float best = fminf(ray_point_d2(b, p1), ray_point_d2(b, p1 + h * ax));
+  {  // t = 0: the ray origin against the segment
+    const float s = fminf(fmaxf(e, 0.f), h);
+    V3 q = w0 - s * ax;
+    best = fminf(best, dot(q, q));
+  }
+  const float t = (bb * e - d) / den, s = e + t * bb;
+  if (t >= 0.f && s >= 0.f && s <= h) {
+    V3 q = w0 + t * b.u - s * ax;
+    best = fminf(best, dot(q, q));
+  }
+  return best <= lim * lim;
+}
+
+// axis ray against the box grown by the reach (slab test, t >= 0)
+__device__ __forceinline__ bool aabb_may_hit(const Bundle& b, const float* bx) {
+  const V3 lo = mk(bx[0], bx[1], bx[2]), hi = mk(bx[3], bx[4], bx[5]);
+  const V3 ctr = 0.5f * (lo + hi), half = 0.5f * (hi - lo);
+  const float g = bundle_reach(b, ctr, sqrtf(dot(half, half)));
+  float t0 = 0.f, t1 = 3.0e38f;
+  const float cc[3] = {b.c.x, b.c.y, b.c.z}, uu[3] = {b.u.x, b.u.y, b.u.z};
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const float l = bx[a] - g, hgh = bx[3 + a] + g;
+    if (fabsf(uu[a]) < 1e-20f) {
+      if (cc[a] < l || cc[a] > hgh) return false;
+    } else {
+      const float inv = 1.f / uu[a];
+      const float ta = (l - cc[a]) * inv, tb = (hgh - cc[a]) * inv;
+      t0 = fmaxf(t0, fminf(ta, tb));
+      t1 = fminf(t1, fmaxf(ta, tb));
+    }
+  }
+  return t0 <= t1;
+}
+
+// primitive k of the unified index space (cylinders, boxes, spheres,
+// oriented boxes, triangles) may shadow some ray of the bundle
+__device__ __forceinline__ bool prim_may_hit(const Obst& ob, int k, const Bundle& b) {
+  if (k < ob.n_cyl) {
+    const float* c = ob.cyl + k * kCylF;
+    return capsule_may_hit(b, mk(c[0], c[1], c[2]), mk(c[3], c[4], c[5]), c[6], sqrtf(c[7]));
+  }
+  k -= ob.n_cyl;
+  if (k < ob.n_box) return aabb_may_hit(b, ob.box + k * kBoxF);
+  k -= ob.n_box;
+  if (k < ob.n_sph) {
+    const float* s = ob.sph + k * kSphF;
+    return sphere_may_hit(b, mk(s[0], s[1], s[2]), sqrtf(s[3]));
+  }
+  k -= ob.n_sph;
+  if (k < ob.n_obox) {
+    const float* o = ob.obox + k * kOboxF;
+    return sphere_may_hit(b, mk(o[0], o[1], o[2]), sqrtf(o[3] * o[3] + o[4] * o[4] + o[5] * o[5]));
+  }
+  k -= ob.n_obox;
+  const float* t = ob.tri + k * kTriF;
+  const V3 v0 = mk(t[0], t[1], t[2]), e1 = mk(t[3], t[4], t[5]), e2 = mk(t[6], t[7], t[8]);
+  const V3 g = v0 + (1.f / 3.f) * (e1 + e2);
+  V3 a = v0 - g, bq = (v0 + e1) - g, cq = (v0 + e2) - g;
+  const float rad = sqrtf(fmaxf(fmaxf(dot(a, a), dot(bq, bq)), dot(cq, cq)));
+  return sphere_may_hit(b, g, rad);
+}
+
+// core/render.py:21-41 for one ray, primitives restricted to the set bits
+// of the bundle's candidate mask (n_words 32-bit words; 0 words: test all)
+__device__ __forceinline__ bool occluded_mask(const Obst& ob, const uint32_t* mask, int n_words, V3 o, V3 d) {
+  if (n_words <= 0) return occluded(ob, o, d);
+  bool sh = false;
+#pragma unroll 1
+  for (int w = 0; w < n_words; ++w) {
+    uint32_t m = mask[w];
+#pragma unroll 1
+    while (m) {
+      int k = w * 32 + __ffs(m) - 1;
+      m &= m - 1u;
+      if (k < ob.n_cyl) {
+        sh |= cyl_shadows(ob.cyl + k * kCylF, o, d);
+        continue;
+      }
+      k -= ob.n_cyl;
+      if (k < ob.n_box) {
+        sh |= box_shadows(ob.box + k * kBoxF, o, d);
+        continue;
+      }
+      k -= ob.n_box;
+      if (k < ob.n_sph) {
+        sh |= sph_shadows(ob.sph + k * kSphF, o, d);
+        continue;
+      }
+      k -= ob.n_sph;
+      if (k < ob.n_obox) {
+        sh |= obox_shadows(ob.obox + k * kOboxF, o, d);
+        continue;
+      }
+      k -= ob.n_obox;
+      sh |= tri_shadows(ob.tri + k * kTriF, o, d);
+    }
+  }
+  return sh;
+}
+
 // ----------------------------------------------------------------- sensor
 struct SensorK {
   int type, n_pixels, width, height;

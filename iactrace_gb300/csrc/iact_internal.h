@@ -9,6 +9,7 @@
 
 #include "../../include/iactrace_gb300.h"
 #include "iact_device.cuh"
+#include "iact_render_impl.cuh"
 
 namespace iact {
 
@@ -27,6 +28,8 @@ struct WsLayout {
   size_t p4;       // float4 [F*M] world point, 1/weight
   size_t n4;       // float4 [F*M] perturbed world normal
   size_t d4;       // float4 [F*M] world delta / |n + scale delta| (backward only)
+  size_t b4;       // float4 [F*ceil(M/32)] bundle centre, radius (scenes with obstructions)
+  size_t n_b4;     // entries of b4 (0: no obstructions, no culling)
   size_t acc;      // double: [rows * P] render accumulator, or the gradient buckets
   size_t total;
   int n_table_floats;
@@ -42,9 +45,30 @@ struct DevInfo {
   int smem_optin = 0;
 };
 DevInfo device_info();
+// CTAs of `kern` an SM holds at (block, smem), cached per device and launch
+// shape; raises the kernel's dynamic shared-memory limit when smem > 48 KiB.
+int resident_ctas(const void* kern, int block, size_t smem, int* per_sm);
 int launch_prep(const iact_scene_t* sc, const WsLayout& L, char* ws, cudaStream_t st, bool with_delta);
 void host_euler(const float* deg, float* R);
 SensorK make_sensor(const iact_sensor_t* s);
+
+// Work-tile shape (sources x facets x 32-sample chunks) for a block of
+// `block` threads: fills p.SB, FC, CC, n_fchunk, n_cchunk, n_tiles from
+// p.F, p.M, p.S and the opts knobs.
+int plan_tiles(RenderK& p, int mode, int block, const iact_opts_t* opts);
+// Shared-memory plan of one render: tables, int16 hex lookup table (if it
+// fits in half the budget) and FP32 histogram rows (if they fit). Floors let
+// a batch reserve the largest table sizes of all its jobs.
+struct SmemPlan {
+  size_t tab_bytes = 0, htab_bytes = 0, hist_bytes = 0;
+  int hex_in_smem = 0, rows_in_smem = 0;
+};
+int plan_smem(const iact_sensor_t* sn, int n_table_floats, int SB, int mode, int hist_mode, size_t budget,
+              size_t tab_floor, size_t htab_floor, SmemPlan& sp);
+RenderK base_params(const iact_scene_t* sc, const iact_sensor_t* sn, const WsLayout& L, char* ws,
+                    const float* sources, const float* values, int S);
+PrepK prep_params(const iact_scene_t* sc, const WsLayout& L, char* ws, bool with_delta);
+int n_primitives(const iact_scene_t* sc);  // obstruction primitives of all kinds
 
 int launch_render(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type,
                   const float* sources, const float* values, int S, int mode, float* out,

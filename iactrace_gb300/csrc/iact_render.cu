@@ -20,7 +20,10 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <mutex>
+#include <tuple>
+#include <utility>
 
 #include "iact_device.cuh"
 #include "iact_internal.h"
@@ -28,110 +31,14 @@
 
 namespace iact {
 
-struct PrepK {
-  int F, M;
-  const float* facet_pos;
-  const float* facet_rot;
-  const float* facet_scale;
-  const float* points;
-  const float* normals;
-  const float* delta;
-  const float* weights;
-  float4* P4;
-  float4* N4;
-  float4* D4;  // optional: world delta / |n + scale delta| (roughness-scale gradients)
-  float* tables;
-  const float* cyl;
-  const float* box;
-  const float* sph;
-  const float* obox;
-  const float* tri;
-  const iact_mirror_t* mirrors;
-  int n_cyl, n_box, n_sph, n_obox, n_tri, n_mir;
-};
-
 __global__ void __launch_bounds__(256) k_prep(const PrepK p) {
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (blockIdx.x == 0) {
-    TableOffsets to = table_offsets(p.n_cyl, p.n_box, p.n_sph, p.n_obox, p.n_tri, p.n_mir);
-    for (int k = threadIdx.x; k < p.n_cyl; k += blockDim.x) {
-      const float* c = p.cyl + 7 * k;
-      float* o = p.tables + to.cyl + kCylF * k;
-      // core/intersections.py:46-48 axis, height
-      float ax = c[3] - c[0], ay = c[4] - c[1], az = c[5] - c[2];
-      float h = sqrtf(ax * ax + ay * ay + az * az);
-      o[0] = c[0]; o[1] = c[1]; o[2] = c[2];
-      o[3] = ax / h; o[4] = ay / h; o[5] = az / h;
-      o[6] = h;
-      o[7] = c[6] * c[6];
-    }
-    for (int k = threadIdx.x; k < p.n_box; k += blockDim.x) {
-      const float* b = p.box + 6 * k;
-      float* o = p.tables + to.box + kBoxF * k;
-      for (int a = 0; a < 3; ++a) {  // core/intersections.py:94-95
-        o[a] = fminf(b[a], b[3 + a]);
-        o[3 + a] = fmaxf(b[a], b[3 + a]);
-      }
-    }
-    for (int k = threadIdx.x; k < p.n_sph; k += blockDim.x) {
-      const float* s = p.sph + 4 * k;
-      float* o = p.tables + to.sph + kSphF * k;
-      o[0] = s[0]; o[1] = s[1]; o[2] = s[2];
-      o[3] = s[3] * s[3];
-    }
-    for (int k = threadIdx.x; k < p.n_obox * kOboxF; k += blockDim.x) p.tables[to.obox + k] = p.obox[k];
-    for (int k = threadIdx.x; k < p.n_tri; k += blockDim.x) {
-      const float* t = p.tri + 9 * k;
-      float* o = p.tables + to.tri + kTriF * k;
-      o[0] = t[0]; o[1] = t[1]; o[2] = t[2];
-      for (int a = 0; a < 3; ++a) {  // core/intersections.py:166-167 edges
-        o[3 + a] = t[3 + a] - t[a];
-        o[6 + a] = t[6 + a] - t[a];
-      }
-    }
-    for (int k = threadIdx.x; k < p.n_mir; k += blockDim.x) {
-      const iact_mirror_t& m = p.mirrors[k];
-      float* o = p.tables + to.mir + kMirF * k;
-      euler_to_matrix(m.rot[0], m.rot[1], m.rot[2], o);
-      o[9] = m.pos[0]; o[10] = m.pos[1]; o[11] = m.pos[2];
-      o[12] = m.offset[0]; o[13] = m.offset[1];
-      o[14] = 0.f;
-      o[15] = m.curvature;
-      o[16] = 1.f + m.conic;
-      o[17] = (1.f + m.conic) * m.curvature * m.curvature;
-      o[18] = m.radius * m.radius;
-      o[19] = (float)m.n_asph;
-      o[20] = (float)m.aperture;
-      o[21] = (float)m.n_vert;
-      o[22] = (float)m.stage;
-      o[23] = m.conic;
-      for (int a = 0; a < 8; ++a) o[24 + a] = a < m.n_asph ? m.asph[a] : 0.f;
-      for (int a = 0; a < 8; ++a) {
-        o[32 + 2 * a] = a < m.n_vert ? m.vert[a][0] : 0.f;
-        o[33 + 2 * a] = a < m.n_vert ? m.vert[a][1] : 0.f;
-      }
-    }
-  }
-  const long long n = (long long)p.F * p.M;
-  if (i >= n) return;
-  const int f = (int)(i / p.M);
-  float R[9];
-  euler_to_matrix(p.facet_rot[3 * f], p.facet_rot[3 * f + 1], p.facet_rot[3 * f + 2], R);
-  V3 pl = mk(p.points[3 * i], p.points[3 * i + 1], p.points[3 * i + 2]);
-  V3 nl = mk(p.normals[3 * i], p.normals[3 * i + 1], p.normals[3 * i + 2]);
-  V3 dl = mk(p.delta[3 * i], p.delta[3 * i + 1], p.delta[3 * i + 2]);
-  V3 pw = rmul(R, pl) + mk(p.facet_pos[3 * f], p.facet_pos[3 * f + 1], p.facet_pos[3 * f + 2]);
-  V3 nw = rmul(R, nl), dw = rmul(R, dl);
-  float sc = p.facet_scale[f];
-  V3 pe = nw + sc * dw;  // perturbed = normals_world + scale * delta_world
-  float nn = sqrtf(dot(pe, pe));
-  p.P4[i] = make_float4(pw.x, pw.y, pw.z, 1.f / p.weights[i]);
-  p.N4[i] = make_float4(pe.x / nn, pe.y / nn, pe.z / nn, 0.f);
-  if (p.D4) p.D4[i] = make_float4(dw.x / nn, dw.y / nn, dw.z / nn, 0.f);
+  if (blockIdx.x == 0) prep_tables(p);
+  const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  prep_chunks(p, w, ((long long)gridDim.x * blockDim.x) >> 5);
 }
 
 template <int SRC, bool SOFT, int MODE, bool STAGES>
-__global__ void __launch_bounds__(256) k_render(const RenderK p) {
+__global__ void __launch_bounds__(256, STAGES ? 2 : IACT_RENDER_MIN_CTAS) k_render(const RenderK p) {
   extern __shared__ __align__(16) float smem[];
   __shared__ int s_tile;
   const int tab_n = (p.n_table_floats + 3) & ~3;
@@ -140,6 +47,7 @@ __global__ void __launch_bounds__(256) k_render(const RenderK p) {
   short* htab = reinterpret_cast<short*>(smem + tab_n);
   float* sh_hist = smem + tab_n + htab_n / 2;
   const int hist_n = p.rows_in_smem * p.P;
+  uint32_t* tmask = reinterpret_cast<uint32_t*>(sh_hist + hist_n);  // candidate masks of a tile's tasks
   const int nthr = blockDim.x;
 
   for (int i = threadIdx.x; i < p.n_table_floats; i += nthr) tab[i] = p.tables[i];
@@ -159,7 +67,7 @@ __global__ void __launch_bounds__(256) k_render(const RenderK p) {
     __syncthreads();
     const int tile = s_tile;
     if (tile >= p.n_tiles) break;
-    render_tile<SRC, SOFT, MODE, STAGES>(p, ob, mir, htab, sh_hist, sink, tile);
+    render_tile<SRC, SOFT, MODE, STAGES>(p, ob, mir, htab, sh_hist, sink, tile, tmask);
   }
 }
 
@@ -197,7 +105,8 @@ __global__ void __launch_bounds__(256) k_debug(const RenderK p, float* pts, floa
     if (SRC == IACT_SRC_EXTENDED) ray_normals(p.seed, s, f, m, z0, z1);
     trace_ray<SRC, STAGES>(p, ob, mir, p.P4[si], p.N4[si],
                            mk(p.sources[SS * s], p.sources[SS * s + 1], p.sources[SS * s + 2]),
-                           SRC == IACT_SRC_EXTENDED ? p.sources[SS * s + 3] : 0.f, z0, z1, p.values[s], x, y, val, hm);
+                           SRC == IACT_SRC_EXTENDED ? p.sources[SS * s + 3] : 0.f, z0, z1, p.values[s], x, y, val, hm,
+                           nullptr, 0);
     pts[2 * i] = x;
     pts[2 * i + 1] = y;
     vals[i] = val;
@@ -271,7 +180,9 @@ SensorK make_sensor(const iact_sensor_t* s) {
   return k;
 }
 
-int launch_prep(const iact_scene_t* sc, const WsLayout& L, char* ws, cudaStream_t st, bool with_delta) {
+int n_primitives(const iact_scene_t* sc) { return sc->n_cyl + sc->n_box + sc->n_sph + sc->n_obox + sc->n_tri; }
+
+PrepK prep_params(const iact_scene_t* sc, const WsLayout& L, char* ws, bool with_delta) {
   PrepK p;
   p.F = sc->n_facets; p.M = sc->n_samples;
   p.facet_pos = sc->facet_pos; p.facet_rot = sc->facet_rot; p.facet_scale = sc->facet_scale;
@@ -279,13 +190,19 @@ int launch_prep(const iact_scene_t* sc, const WsLayout& L, char* ws, cudaStream_
   p.P4 = reinterpret_cast<float4*>(ws + L.p4);
   p.N4 = reinterpret_cast<float4*>(ws + L.n4);
   p.D4 = with_delta ? reinterpret_cast<float4*>(ws + L.d4) : nullptr;
+  p.B4 = L.n_b4 ? reinterpret_cast<float4*>(ws + L.b4) : nullptr;
   p.tables = reinterpret_cast<float*>(ws + L.tables);
   p.cyl = sc->cyl; p.box = sc->box; p.sph = sc->sph; p.obox = sc->obox; p.tri = sc->tri;
   p.mirrors = sc->mirrors;
   p.n_cyl = sc->n_cyl; p.n_box = sc->n_box; p.n_sph = sc->n_sph; p.n_obox = sc->n_obox; p.n_tri = sc->n_tri;
   p.n_mir = sc->n_mirrors;
-  long long n = (long long)p.F * p.M;
-  int blocks = (int)std::max<long long>(1, (n + 255) / 256);
+  return p;
+}
+
+int launch_prep(const iact_scene_t* sc, const WsLayout& L, char* ws, cudaStream_t st, bool with_delta) {
+  const PrepK p = prep_params(sc, L, ws, with_delta);
+  const long long units = (long long)p.F * ((p.M + 31) / 32);  // one warp per (facet, 32-sample chunk)
+  const int blocks = (int)std::min<long long>(std::max<long long>(1, (units + 7) / 8), 65535);
   k_prep<<<blocks, 256, 0, st>>>(p);
   return check_cuda(cudaGetLastError(), "k_prep launch");
 }
@@ -305,26 +222,49 @@ RenderK base_params(const iact_scene_t* sc, const iact_sensor_t* sn, const WsLay
   p.hex_table = sn->table;
   p.sn = make_sensor(sn);
   p.counter = reinterpret_cast<int*>(ws + L.counter);
+  p.B4 = L.n_b4 ? reinterpret_cast<const float4*>(ws + L.b4) : nullptr;
+  p.n_words = L.n_b4 ? (n_primitives(sc) + 31) / 32 : 0;
   return p;
+}
+
+int resident_ctas(const void* kern, int block, size_t smem, int* per_sm) {
+  static std::mutex mu;
+  static std::map<std::pair<int, const void*>, size_t> smem_set;              // per (device, kernel)
+  static std::map<std::tuple<int, const void*, int, size_t>, int> occ_cache;  // per launch shape
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> g(mu);
+  const auto okey = std::make_tuple(dev, kern, block, smem);
+  auto it = occ_cache.find(okey);
+  if (it != occ_cache.end()) {
+    *per_sm = it->second;
+    return IACT_OK;
+  }
+  size_t& have = smem_set[std::make_pair(dev, kern)];
+  if (smem > 48 * 1024 && smem > have) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return check_cuda(e, "cudaFuncSetAttribute(dynamic shared memory)");
+    have = smem;
+  }
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, kern, block, smem);
+  if (e != cudaSuccess) return check_cuda(e, "occupancy query");
+  occ_cache[okey] = *per_sm;
+  return IACT_OK;
 }
 
 template <int SRC, bool SOFT, int MODE, bool STAGES>
 int run_render(RenderK p, int block, size_t smem, cudaStream_t st, void* const* ev) {
   auto kern = k_render<SRC, SOFT, MODE, STAGES>;
-  if (smem > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return check_cuda(e, "cudaFuncSetAttribute(k_render smem)");
-  }
   int per_sm = 0;
-  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, smem);
-  if (e != cudaSuccess) return check_cuda(e, "occupancy query");
+  int rc = resident_ctas(reinterpret_cast<const void*>(kern), block, smem, &per_sm);
+  if (rc) return rc;
   if (per_sm < 1) return set_error(IACT_E_UNSUPPORTED, "render kernel does not fit on an SM with this configuration");
   DevInfo di = device_info();
   int grid = std::min(p.n_tiles, per_sm * di.sm_count);
   grid = std::max(grid, 1);
   if (ev && ev[0]) cudaEventRecord(static_cast<cudaEvent_t>(ev[0]), st);
   kern<<<grid, block, smem, st>>>(p);
-  int rc = check_cuda(cudaGetLastError(), "k_render launch");
+  rc = check_cuda(cudaGetLastError(), "k_render launch");
   if (ev && ev[1]) cudaEventRecord(static_cast<cudaEvent_t>(ev[1]), st);
   return rc;
 }
@@ -362,6 +302,9 @@ WsLayout workspace_layout(const iact_scene_t* sc, size_t acc_elems, bool with_de
   off = align256(off + sizeof(float4) * n);
   L.d4 = off;
   if (with_delta) off = align256(off + sizeof(float4) * n);
+  L.b4 = off;  // bundle bounds, only for scenes with obstructions
+  L.n_b4 = n_primitives(sc) > 0 ? (size_t)std::max(sc->n_facets, 0) * ((std::max(sc->n_samples, 0) + 31) / 32) : 0;
+  off = align256(off + sizeof(float4) * L.n_b4);
   L.acc = off;
   off = align256(off + sizeof(double) * acc_elems);
   L.total = off;
@@ -381,6 +324,50 @@ WsLayout workspace_for(const iact_scene_t* sc, const iact_sensor_t* sn, int S, i
   return workspace_layout(sc, acc_elems(sn, S, mode), false);
 }
 
+int plan_tiles(RenderK& p, int mode, int block, const iact_opts_t* opts) {
+  const int nw = block / 32;
+  const int nch = (p.M + 31) / 32;
+  const int S = p.S;
+  // a response tile keeps one FP32 shared-memory row per source: two warps per
+  // source halves that footprint and doubles the CTAs an SM holds
+  int SB = (opts && opts->sources_per_cta > 0) ? opts->sources_per_cta
+                                               : std::min(S, mode == IACT_MODE_RESPONSE ? std::max(1, nw / 2) : nw);
+  SB = std::max(1, std::min(SB, S));
+  const int tpw = (opts && opts->tasks_per_warp > 0) ? opts->tasks_per_warp : 48;
+  // warp tasks (32 rays each) per tile; candidate masks stay within 16 KiB
+  const int target = std::max(1, std::min(nw * tpw, p.n_words ? 4096 / p.n_words : 1 << 30));
+  int CC = std::max(1, std::min(nch, std::max(1, target / SB)));
+  int FC = (opts && opts->facets_per_tile > 0) ? opts->facets_per_tile : std::max(1, target / (SB * CC));
+  FC = std::max(1, std::min(FC, p.F));
+  p.SB = SB; p.FC = FC; p.CC = CC;
+  p.n_fchunk = (p.F + FC - 1) / FC;
+  p.n_cchunk = (nch + CC - 1) / CC;
+  const long long tiles =
+      (S > 0 && p.F > 0 && p.M > 0) ? (long long)((S + SB - 1) / SB) * p.n_fchunk * p.n_cchunk : 0;
+  if (tiles > 0x7fffffffLL) return set_error(IACT_E_UNSUPPORTED, "too many work tiles");
+  p.n_tiles = (int)tiles;
+  return IACT_OK;
+}
+
+int plan_smem(const iact_sensor_t* sn, int n_table_floats, int SB, int mode, int hist_mode, size_t budget,
+              size_t tab_floor, size_t htab_floor, SmemPlan& sp) {
+  const size_t P = (size_t)sn->n_pixels;
+  sp.tab_bytes = std::max(tab_floor, sizeof(float) * (size_t)((n_table_floats + 3) & ~3));
+  const bool hex = (sn->type == IACT_SENSOR_HEX || sn->type == IACT_SENSOR_SOFT_HEX);
+  const size_t htab_elems = hex ? (size_t)sn->table_q * sn->table_r : 0;
+  size_t htab_bytes = sizeof(short) * ((htab_elems + 7) & ~(size_t)7);
+  sp.hex_in_smem = (hex && sn->n_pixels < 32768 && sp.tab_bytes + std::max(htab_bytes, htab_floor) <= budget / 2) ? 1 : 0;
+  sp.htab_bytes = sp.hex_in_smem ? std::max(htab_bytes, htab_floor) : htab_floor;
+  if (sp.tab_bytes + sp.htab_bytes > budget) return set_error(IACT_E_UNSUPPORTED, "scene tables exceed shared memory");
+  const int rows = (mode == IACT_MODE_RESPONSE) ? SB : 1;
+  const size_t hist_bytes = sizeof(float) * (size_t)rows * P;
+  const bool use_smem = (hist_mode != 2) && (sp.tab_bytes + sp.htab_bytes + hist_bytes <= budget);
+  if (hist_mode == 1 && !use_smem) return set_error(IACT_E_UNSUPPORTED, "histogram rows do not fit in shared memory");
+  sp.rows_in_smem = use_smem ? rows : 0;
+  sp.hist_bytes = use_smem ? hist_bytes : 0;
+  return IACT_OK;
+}
+
 int launch_render(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type, const float* sources,
                   const float* values, int S, int mode, float* out, void* ws, size_t ws_bytes,
                   const iact_opts_t* opts, cudaStream_t st) {
@@ -388,7 +375,6 @@ int launch_render(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type,
   const size_t n_acc = acc_elems(sn, S, mode);
   const WsLayout L = workspace_layout(sc, n_acc, false);
   char* w = static_cast<char*>(ws);
-  const size_t P = (size_t)sn->n_pixels;
   int rc;
   if (S == 0 || sc->n_facets == 0 || sc->n_samples == 0) {
     if (n_acc) return check_cuda(cudaMemsetAsync(out, 0, n_acc * sizeof(float), st), "zero output");
@@ -403,42 +389,20 @@ int launch_render(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type,
 
   RenderK p = base_params(sc, sn, L, w, sources, values, S);
   p.acc = reinterpret_cast<double*>(w + L.acc);
+  if (opts && (opts->flags & IACT_FLAG_NO_CULL)) p.n_words = 0;
   int block = (opts && opts->block_threads > 0) ? opts->block_threads : 256;
   if (block % 32 || block > 256) return set_error(IACT_E_INVALID, "opts.block_threads must be a multiple of 32, <= 256");
-  const int nw = block / 32;
-  const int nch = (p.M + 31) / 32;
-  // a response tile keeps one FP32 shared-memory row per source: two warps per
-  // source halves that footprint and doubles the CTAs an SM holds
-  int SB = (opts && opts->sources_per_cta > 0) ? opts->sources_per_cta
-                                               : std::min(S, mode == IACT_MODE_RESPONSE ? std::max(1, nw / 2) : nw);
-  SB = std::min(SB, S);
-  const int target = nw * 48;  // warp tasks (32 rays each) per tile
-  int CC = std::min(nch, std::max(1, target / SB));
-  int FC = (opts && opts->facets_per_tile > 0) ? opts->facets_per_tile : std::max(1, target / (SB * CC));
-  FC = std::min(FC, p.F);
-  p.SB = SB; p.FC = FC; p.CC = CC;
-  p.n_fchunk = (p.F + FC - 1) / FC;
-  p.n_cchunk = (nch + CC - 1) / CC;
-  const long long tiles = (long long)((S + SB - 1) / SB) * p.n_fchunk * p.n_cchunk;
-  if (tiles > 0x7fffffffLL) return set_error(IACT_E_UNSUPPORTED, "too many work tiles");
-  p.n_tiles = (int)tiles;
-
+  rc = plan_tiles(p, mode, block, opts);
+  if (rc) return rc;
   DevInfo di = device_info();
-  const size_t budget = (size_t)std::min(di.smem_optin > 0 ? di.smem_optin : 49152, 200 * 1024);
-  const size_t tab_bytes = sizeof(float) * (size_t)((L.n_table_floats + 3) & ~3);
-  const bool hex = (sn->type == IACT_SENSOR_HEX || sn->type == IACT_SENSOR_SOFT_HEX);
-  const size_t htab_elems = hex ? (size_t)sn->table_q * sn->table_r : 0;
-  size_t htab_bytes = sizeof(short) * ((htab_elems + 7) & ~(size_t)7);
-  p.hex_in_smem = (hex && sn->n_pixels < 32768 && tab_bytes + htab_bytes <= budget / 2) ? 1 : 0;
-  if (!p.hex_in_smem) htab_bytes = 0;
-  if (tab_bytes + htab_bytes > budget) return set_error(IACT_E_UNSUPPORTED, "scene tables exceed shared memory");
-  const int rows = (mode == IACT_MODE_RESPONSE) ? SB : 1;
-  const size_t hist_bytes = sizeof(float) * (size_t)rows * P;
-  const int hist_mode = opts ? opts->hist_mode : 0;
-  bool use_smem = (hist_mode != 2) && (tab_bytes + htab_bytes + hist_bytes <= budget);
-  if (hist_mode == 1 && !use_smem) return set_error(IACT_E_UNSUPPORTED, "histogram rows do not fit in shared memory");
-  p.rows_in_smem = use_smem ? rows : 0;
-  const size_t smem = tab_bytes + htab_bytes + (use_smem ? hist_bytes : 0);
+  const size_t mask_bytes = sizeof(uint32_t) * (size_t)p.n_words * p.SB * p.FC * p.CC;
+  const size_t budget = (size_t)std::min(di.smem_optin > 0 ? di.smem_optin : 49152, 200 * 1024) - mask_bytes;
+  SmemPlan sp;
+  rc = plan_smem(sn, L.n_table_floats, p.SB, mode, opts ? opts->hist_mode : 0, budget, 0, 0, sp);
+  if (rc) return rc;
+  p.hex_in_smem = sp.hex_in_smem;
+  p.rows_in_smem = sp.rows_in_smem;
+  const size_t smem = sp.tab_bytes + sp.htab_bytes + sp.hist_bytes + mask_bytes;
 
   const bool soft = (sn->type == IACT_SENSOR_SOFT_SQUARE || sn->type == IACT_SENSOR_SOFT_HEX);
   const bool stages = sc->n_mirrors > 0;

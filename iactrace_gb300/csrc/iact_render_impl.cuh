@@ -5,7 +5,150 @@
 
 #include "iact_device.cuh"
 
+// Resident CTAs per SM the single-stage render kernels are compiled for
+// (256 threads each): 5 caps them at 48 registers per thread.
+#ifndef IACT_RENDER_MIN_CTAS
+#define IACT_RENDER_MIN_CTAS 5
+#endif
+
 namespace iact {
+
+struct PrepK {
+  int F, M;
+  const float* facet_pos;
+  const float* facet_rot;
+  const float* facet_scale;
+  const float* points;
+  const float* normals;
+  const float* delta;
+  const float* weights;
+  float4* P4;
+  float4* N4;
+  float4* D4;  // optional: world delta / |n + scale delta| (roughness-scale gradients)
+  float4* B4;  // optional: per (facet, 32-sample chunk) bundle centre and radius
+  float* tables;
+  const float* cyl;
+  const float* box;
+  const float* sph;
+  const float* obox;
+  const float* tri;
+  const iact_mirror_t* mirrors;
+  int n_cyl, n_box, n_sph, n_obox, n_tri, n_mir;
+};
+
+// Per-launch constant tables: telescope/mirrors.py and core/obstructions.py
+// constants precomputed once (one CTA).
+__device__ __forceinline__ void prep_tables(const PrepK& p) {
+  TableOffsets to = table_offsets(p.n_cyl, p.n_box, p.n_sph, p.n_obox, p.n_tri, p.n_mir);
+  for (int k = threadIdx.x; k < p.n_cyl; k += blockDim.x) {
+    const float* c = p.cyl + 7 * k;
+    float* o = p.tables + to.cyl + kCylF * k;
+    // core/intersections.py:46-48 axis, height
+    float ax = c[3] - c[0], ay = c[4] - c[1], az = c[5] - c[2];
+    float h = sqrtf(ax * ax + ay * ay + az * az);
+    o[0] = c[0]; o[1] = c[1]; o[2] = c[2];
+    o[3] = ax / h; o[4] = ay / h; o[5] = az / h;
+    o[6] = h;
+    o[7] = c[6] * c[6];
+  }
+  for (int k = threadIdx.x; k < p.n_box; k += blockDim.x) {
+    const float* b = p.box + 6 * k;
+    float* o = p.tables + to.box + kBoxF * k;
+    for (int a = 0; a < 3; ++a) {  // core/intersections.py:94-95
+      o[a] = fminf(b[a], b[3 + a]);
+      o[3 + a] = fmaxf(b[a], b[3 + a]);
+    }
+  }
+  for (int k = threadIdx.x; k < p.n_sph; k += blockDim.x) {
+    const float* s = p.sph + 4 * k;
+    float* o = p.tables + to.sph + kSphF * k;
+    o[0] = s[0]; o[1] = s[1]; o[2] = s[2];
+    o[3] = s[3] * s[3];
+  }
+  for (int k = threadIdx.x; k < p.n_obox * kOboxF; k += blockDim.x) p.tables[to.obox + k] = p.obox[k];
+  for (int k = threadIdx.x; k < p.n_tri; k += blockDim.x) {
+    const float* t = p.tri + 9 * k;
+    float* o = p.tables + to.tri + kTriF * k;
+    o[0] = t[0]; o[1] = t[1]; o[2] = t[2];
+    for (int a = 0; a < 3; ++a) {  // core/intersections.py:166-167 edges
+      o[3 + a] = t[3 + a] - t[a];
+      o[6 + a] = t[6 + a] - t[a];
+    }
+  }
+  for (int k = threadIdx.x; k < p.n_mir; k += blockDim.x) {
+    const iact_mirror_t& m = p.mirrors[k];
+    float* o = p.tables + to.mir + kMirF * k;
+    euler_to_matrix(m.rot[0], m.rot[1], m.rot[2], o);
+    o[9] = m.pos[0]; o[10] = m.pos[1]; o[11] = m.pos[2];
+    o[12] = m.offset[0]; o[13] = m.offset[1];
+    o[14] = 0.f;
+    o[15] = m.curvature;
+    o[16] = 1.f + m.conic;
+    o[17] = (1.f + m.conic) * m.curvature * m.curvature;
+    o[18] = m.radius * m.radius;
+    o[19] = (float)m.n_asph;
+    o[20] = (float)m.aperture;
+    o[21] = (float)m.n_vert;
+    o[22] = (float)m.stage;
+    o[23] = m.conic;
+    for (int a = 0; a < 8; ++a) o[24 + a] = a < m.n_asph ? m.asph[a] : 0.f;
+    for (int a = 0; a < 8; ++a) {
+      o[32 + 2 * a] = a < m.n_vert ? m.vert[a][0] : 0.f;
+      o[33 + 2 * a] = a < m.n_vert ? m.vert[a][1] : 0.f;
+    }
+  }
+}
+
+// telescope/mirrors.py:64-79 transform_to_world for one (facet, sample);
+// returns the world point.
+__device__ __forceinline__ V3 prep_sample(const PrepK& p, long long i) {
+  const int f = (int)(i / p.M);
+  float R[9];
+  euler_to_matrix(p.facet_rot[3 * f], p.facet_rot[3 * f + 1], p.facet_rot[3 * f + 2], R);
+  V3 pl = mk(p.points[3 * i], p.points[3 * i + 1], p.points[3 * i + 2]);
+  V3 nl = mk(p.normals[3 * i], p.normals[3 * i + 1], p.normals[3 * i + 2]);
+  V3 dl = mk(p.delta[3 * i], p.delta[3 * i + 1], p.delta[3 * i + 2]);
+  V3 pw = rmul(R, pl) + mk(p.facet_pos[3 * f], p.facet_pos[3 * f + 1], p.facet_pos[3 * f + 2]);
+  V3 nw = rmul(R, nl), dw = rmul(R, dl);
+  float sc = p.facet_scale[f];
+  V3 pe = nw + sc * dw;  // perturbed = normals_world + scale * delta_world
+  float nn = sqrtf(dot(pe, pe));
+  p.P4[i] = make_float4(pw.x, pw.y, pw.z, 1.f / p.weights[i]);
+  p.N4[i] = make_float4(pe.x / nn, pe.y / nn, pe.z / nn, 0.f);
+  if (p.D4) p.D4[i] = make_float4(dw.x / nn, dw.y / nn, dw.z / nn, 0.f);
+  return pw;
+}
+
+// World samples of (facet, 32-sample chunk) units, one warp per unit (warp
+// `w0` of `nw` warps striding over the units), and each unit's bundle
+// bound B4 = (centre of its world points, largest distance from it).
+__device__ __forceinline__ void prep_chunks(const PrepK& p, long long w0, long long nw) {
+  const int lane = threadIdx.x & 31;
+  const int nch = (p.M + 31) >> 5;
+  const long long units = (long long)p.F * nch;
+  for (long long u = w0; u < units; u += nw) {
+    const int f = (int)(u / nch), m = (int)(u - (long long)f * nch) * 32 + lane;
+    const bool act = m < p.M;
+    V3 pw = mk(0.f, 0.f, 0.f);
+    if (act) pw = prep_sample(p, (long long)f * p.M + m);
+    if (p.B4) {
+      float n = act ? 1.f : 0.f, sx = pw.x, sy = pw.y, sz = pw.z;
+#pragma unroll
+      for (int k = 16; k > 0; k >>= 1) {
+        n += __shfl_xor_sync(kFull, n, k);
+        sx += __shfl_xor_sync(kFull, sx, k);
+        sy += __shfl_xor_sync(kFull, sy, k);
+        sz += __shfl_xor_sync(kFull, sz, k);
+      }
+      const V3 c = (1.f / n) * mk(sx, sy, sz);
+      V3 w = pw - c;
+      float r2 = act ? dot(w, w) : 0.f;
+#pragma unroll
+      for (int k = 16; k > 0; k >>= 1) r2 = fmaxf(r2, __shfl_xor_sync(kFull, r2, k));
+      if (lane == 0) p.B4[u] = make_float4(c.x, c.y, c.z, sqrtf(r2) * 1.0001f + 1e-6f);
+    }
+  }
+}
 
 struct RenderK {
   int F, M, S, P;
@@ -25,6 +168,8 @@ struct RenderK {
   int n_fchunk, n_cchunk, n_tiles;
   int* counter;
   uint32_t seed;  // jitter stream of extended sources
+  const float4* B4;  // per (facet, chunk) bundle bounds (culling on)
+  int n_words;       // 32-bit candidate-mask words per task; 0 = no culling
 };
 
 // Where hits go: FP32 shared-memory rows of the current tile, or the FP64
@@ -111,10 +256,13 @@ __device__ __forceinline__ void splat_hex(const SensorK& s, const TT* table, con
 
 // core/render.py:118-157 for one ray; returns sensor-plane (x, y), value and
 // the index of the last stage mirror hit (-1 if none).
+// The primary shadow test covers the set bits of the warp bundle's
+// candidate mask (n_words == 0: every primitive).
 template <int SRC, bool STAGES>
 __device__ __forceinline__ void trace_ray(const RenderK& p, const Obst& ob, const float* mir, float4 P,
                                           float4 N, V3 src, float sigma, float z0, float z1, float v, float& x,
-                                          float& y, float& val, int& hit_mirror) {
+                                          float& y, float& val, int& hit_mirror, const uint32_t* cmask,
+                                          int n_words) {
   V3 tp = mk(P.x, P.y, P.z), tn = mk(N.x, N.y, N.z);
   V3 d;
   if (SRC == IACT_SRC_POINT) {
@@ -125,7 +273,7 @@ __device__ __forceinline__ void trace_ray(const RenderK& p, const Obst& ob, cons
   } else {
     d = src;  // parallel: the source entry is the direction, as given
   }
-  const bool sh = occluded(ob, tp, mk(-d.x, -d.y, -d.z));
+  const bool sh = occluded_mask(ob, cmask, n_words, tp, mk(-d.x, -d.y, -d.z));
   const float c = dot(d, tn);  // core/reflection.py:5-20
   V3 r = d - (2.f * c) * tn;
   val = (v * -c * P.w) * (sh ? 0.f : 1.f);  // values * cos / tw * shadow
@@ -169,9 +317,55 @@ __device__ __forceinline__ void trace_ray(const RenderK& p, const Obst& ob, cons
 // render: every warp traces its share of the tile's warp tasks, then the
 // tile's shared-memory rows go to the FP64 accumulator. All threads of the
 // CTA call this; it ends after a __syncthreads.
+// Axis and angular spread of a warp task's shadow rays (towards the
+// source): point sources from the bundle centre c, parallel and extended
+// sources along minus the given direction (jitter bounded by the largest
+// Box-Muller radius, 5.8 sigma, of 24-bit uniforms).
+template <int SRC>
+__device__ __forceinline__ void bundle_axis(V3 src, float sigma, V3 c, float R0, V3& u, float& dlt) {
+  if (SRC == IACT_SRC_POINT) {
+    V3 w = src - c;
+    const float L = sqrtf(dot(w, w));
+    u = (1.f / L) * w;
+    dlt = L > 4.f * R0 ? 2.f * R0 / (L - R0) + 1e-6f : 2.f;
+  } else {
+    const float L = sqrtf(dot(src, src));
+    u = (-1.f / L) * src;
+    dlt = (SRC == IACT_SRC_EXTENDED ? 6.f * fabsf(sigma) : 0.f) + 1e-6f;
+  }
+}
+
+// CTA-collective: candidate masks of the T tasks (source sl, facet fl,
+// chunk cl; chunk fastest) of a tile starting at (s0, f0, c0), one (task,
+// primitive) pair per thread step, into mask[T * n_words].
+template <int SRC>
+__device__ __forceinline__ void tile_masks(const float4* B4, const float* sources, int M, int nw, const Obst& ob,
+                                           int s0, int f0, int c0, int FCc, int CCc, int T, uint32_t* mask) {
+  const int nthr = blockDim.x;
+  const int np = ob.n_cyl + ob.n_box + ob.n_sph + ob.n_obox + ob.n_tri;
+  const int nch = (M + 31) >> 5;
+  for (int i = threadIdx.x; i < T * nw; i += nthr) mask[i] = 0u;
+  __syncthreads();
+  constexpr int SS = (SRC == IACT_SRC_EXTENDED) ? 4 : 3;
+  for (int i = threadIdx.x; i < T * np; i += nthr) {
+    const int t = i / np, k = i - t * np;
+    const int sl = t / (FCc * CCc), rem = t - sl * FCc * CCc;
+    const int fl = rem / CCc, cl = rem - fl * CCc;
+    const int s = s0 + sl;
+    const float4 B = __ldg(B4 + (size_t)(f0 + fl) * nch + c0 + cl);
+    Bundle bd;
+    bd.c = mk(B.x, B.y, B.z);
+    bd.R0 = B.w;
+    const V3 src = mk(__ldg(sources + SS * s), __ldg(sources + SS * s + 1), __ldg(sources + SS * s + 2));
+    bundle_axis<SRC>(src, SRC == IACT_SRC_EXTENDED ? __ldg(sources + SS * s + 3) : 0.f, bd.c, bd.R0, bd.u, bd.dlt);
+    if (prim_may_hit(ob, k, bd)) atomicOr(mask + t * nw + (k >> 5), 1u << (k & 31));
+  }
+  __syncthreads();
+}
+
 template <int SRC, bool SOFT, int MODE, bool STAGES>
 __device__ __forceinline__ void render_tile(const RenderK& p, const Obst& ob, const float* mir, const short* htab,
-                                            float* sh_hist, const Sink& sink, int tile) {
+                                            float* sh_hist, const Sink& sink, int tile, uint32_t* tmask) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5, nthr = blockDim.x;
   const int nch = (p.M + 31) >> 5;
   const int per_s = p.n_fchunk * p.n_cchunk;
@@ -184,6 +378,7 @@ __device__ __forceinline__ void render_tile(const RenderK& p, const Obst& ob, co
   int rl_key = -1;  // run-length merged hit of this lane (hard sensors)
   float rl_val = 0.f;
   const int T = SBc * FCc * CCc;
+  if (p.n_words) tile_masks<SRC>(p.B4, p.sources, p.M, p.n_words, ob, s0, f0, c0, FCc, CCc, T, tmask);
   const int tb = (warp * T) / nw, te = ((warp + 1) * T) / nw;
   // task t = (source sl, facet fl, chunk cl), chunk fastest; decoded once
   int sl = tb / (FCc * CCc);
@@ -203,7 +398,8 @@ __device__ __forceinline__ void render_tile(const RenderK& p, const Obst& ob, co
       const size_t si = (size_t)f * p.M + m;
       float z0 = 0.f, z1 = 0.f;
       if (SRC == IACT_SRC_EXTENDED) ray_normals(p.seed, s, f, m, z0, z1);
-      trace_ray<SRC, STAGES>(p, ob, mir, __ldg(p.P4 + si), __ldg(p.N4 + si), src, sig, z0, z1, v, x, y, val, hm);
+      trace_ray<SRC, STAGES>(p, ob, mir, __ldg(p.P4 + si), __ldg(p.N4 + si), src, sig, z0, z1, v, x, y, val, hm,
+                             tmask + t * p.n_words, p.n_words);
     }
     int rowbase;
     if (MODE == IACT_MODE_RESPONSE) rowbase = (p.rows_in_smem ? sl : s) * p.P;

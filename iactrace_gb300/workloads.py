@@ -14,6 +14,11 @@
                          (k = -1.05, f = 10 m) of 61 hex segments with
                          aspheric terms, 3 m hyperboloid secondary, 32 x 32
                          square camera, 64 point sources within 1.5 deg.
+  ragged_batch()         64 Davies-Cotton variants: the first n (uniform
+                         100..900) facets of one 900-facet dish, tip/tilt
+                         errors with sigma uniform in 0.2..1.0 mrad, 960- or
+                         2048-pixel hex camera, log-uniform 1..4096 point
+                         sources within 2.5 deg, 256 samples per facet.
 
 Facet layouts follow the Davies-Cotton construction: facet centres on a
 sphere of radius f about the focus, each facet normal aimed at (0, 0, 2f).
@@ -169,3 +174,39 @@ def cassegrain(n_samples: int = 500, n_sources: int = 64, seed: int = 0, with_as
     tel = Telescope(groups, [], [cam], name="cassegrain10m")
     src = point_sources_disk(n_sources, 1.5, seed + 1)
     return tel, src, torch.ones(n_sources), "point"
+
+
+def _first_facets(g, n: int, rot):
+    """The first n facets of a sampled polygon-aperture group, with rotations `rot`."""
+    return g.replace(positions=g.positions[:n], rotations=rot, offsets=g.offsets[:n], vertices=g.vertices[:n],
+                     points=g.points[:n], normals=g.normals[:n], weights=g.weights[:n],
+                     perturbation_delta=g.perturbation_delta[:n], perturbation_scale=g.perturbation_scale[:n])
+
+
+def ragged_batch(n_instances: int = 64, n_samples: int = 256, seed: int = 0, max_facets: int = 900,
+                 min_facets: int = 100, max_sources: int = 4096, pixels=(960, 2048)):
+    """Ragged batch of telescope variants: (telescopes, sources, values, source_type).
+
+    Instance i draws its facet count n uniform in [min_facets, max_facets]
+    (the first n facets of one Davies-Cotton dish sampled once), a tip/tilt
+    error sigma uniform in 0.2..1.0 mrad, a camera of `pixels` and a
+    log-uniform source count in [1, max_sources]; sources are points at
+    z = 1e10 within 2.5 deg with values U(0.5, 1)."""
+    groups, obst = davies_cotton(n_facets=max_facets, tilt_sigma_mrad=0.0, n_samples=n_samples, seed=seed)
+    if len(groups) != 1:
+        raise ValueError("the Davies-Cotton dish is expected to form one mirror group")
+    g = groups[0]
+    rng = np.random.default_rng(seed + 101)
+    cams = {p: hex_camera(p) for p in pixels}
+    tels, srcs, vals = [], [], []
+    for i in range(n_instances):
+        n = int(rng.integers(min_facets, max_facets + 1))
+        S = int(min(max_sources, max(1, round(math.exp(rng.uniform(0.0, math.log(max_sources)))))))
+        P = int(pixels[int(rng.integers(0, len(pixels)))])
+        sig_deg = math.degrees(float(rng.uniform(0.2, 1.0)) * 1e-3)
+        rot = g.rotations[:n].clone()
+        rot[:, :2] += torch.from_numpy(rng.standard_normal((n, 2))).float() * sig_deg
+        tels.append(Telescope([_first_facets(g, n, rot)], obst, [cams[P]], name=f"dc_variant{i}_{n}f_{P}px"))
+        srcs.append(point_sources_disk(S, 2.5, seed + 1000 + i))
+        vals.append(0.5 + 0.5 * torch.from_numpy(rng.random(S)).float())
+    return tels, srcs, vals, "point"

@@ -27,7 +27,8 @@
  *   iact_render_debug      <- core/render.py:223-268  render_debug()
  *   iact_render_backward   <- jax.grad of render() / render_response_matrix()
  *                             (no dedicated reference function)
- *   iact_sample_facets     <- core/integrators.py:97-187 MCIntegrator.sample_group
+ *   iact_batch_*           <- a Python loop (or jax.vmap) of Telescope.__call__
+ *                             over telescope variants (no reference function)
  */
 #ifndef IACTRACE_GB300_H
 #define IACTRACE_GB300_H
@@ -39,7 +40,7 @@
 extern "C" {
 #endif
 
-#define IACT_ABI_VERSION 1
+#define IACT_ABI_VERSION 2
 
 /* status codes */
 #define IACT_OK 0
@@ -131,12 +132,19 @@ typedef struct {
   int32_t kernel_size;
 } iact_sensor_t;
 
+/* Shadow tests of a warp's 32 rays are restricted to the primitives whose
+ * bounding volume comes near the rays' common bundle (exact: identical
+ * shadow masks); this flag tests every primitive on every ray instead. */
+#define IACT_FLAG_NO_CULL 1
+
 /* Optional launch knobs; NULL or zeros select the built-in defaults. */
 typedef struct {
   int32_t block_threads;    /* threads per CTA (multiple of 32)           */
   int32_t sources_per_cta;  /* warps per CTA each own one source at a time */
   int32_t facets_per_tile;  /* primary facets per work tile               */
   int32_t hist_mode;        /* 0 auto, 1 shared-memory rows, 2 global     */
+  int32_t tasks_per_warp;   /* 32-ray tasks per warp per work tile (0: 48) */
+  int32_t flags;            /* IACT_FLAG_* bits                           */
   uint32_t seed;            /* jitter stream of EXTENDED sources            */
   /* optional cudaEvent_t pair recorded on `stream` right before and after
    * the render kernel (profiling); NULL to skip */
@@ -146,7 +154,8 @@ typedef struct {
 int iact_abi_version(void);
 const char* iact_last_error(void);
 /* sizeof(iact_scene_t), sizeof(iact_sensor_t), sizeof(iact_mirror_t),
- * sizeof(iact_opts_t) as compiled into the library (binding self-check). */
+ * sizeof(iact_opts_t) and, if n >= 5, sizeof(iact_job_t) as compiled into
+ * the library (binding self-check). */
 int iact_abi_layout(size_t* out, int n);
 
 /* Diagnostics: runs `iters` dependent FP32 FMAs per thread over
@@ -222,6 +231,51 @@ int iact_render_backward(const iact_scene_t* scene, const iact_sensor_t* sensor,
                          float* g_mirror_surface, void* workspace,
                          size_t workspace_bytes, const iact_opts_t* opts,
                          void* stream);
+
+/* ---- Batched persistent render -------------------------------------------
+ * Many telescope variants and source sets of uneven size in one persistent
+ * launch. A batch is a fixed list of jobs, each one iact_render call (own
+ * scene, sensor, source count and output); all jobs share source_type and
+ * mode. One persistent kernel per template class (hard/soft sensor x
+ * with/without later mirror stages) walks a global queue of (job, source
+ * block, facet chunk, 32-sample chunk) tiles, largest jobs first; a CTA
+ * restages the job's tables in shared memory when its next tile belongs to
+ * another job. Results equal iact_render's per job up to FP64 summation order.
+ * No reference counterpart: the reference renders variants by a Python loop
+ * (or jax.vmap) over Telescope.__call__ (telescope/telescope.py:56-83). */
+typedef struct {
+  const iact_scene_t* scene;   /* host descriptor of device arrays          */
+  const iact_sensor_t* sensor; /* host descriptor of a device lookup table  */
+  const float* sources;        /* device [S,3] ([S,4] for EXTENDED)         */
+  const float* values;         /* device [S]                                */
+  int32_t n_sources;
+  uint32_t seed;               /* jitter stream of EXTENDED sources         */
+  float* out;                  /* device [P] (IMAGE) or [S,P] (RESPONSE)    */
+} iact_job_t;
+
+typedef struct iact_batch iact_batch;
+
+/* Validates every job and plans tiles and shared memory from opts
+ * (block_threads, tasks_per_warp, hist_mode, kernel_events; the per-call
+ * sources_per_cta, facets_per_tile and seed are not used). Copies the
+ * descriptors: the device arrays they name must outlive the batch. Host
+ * only, no CUDA call. */
+int iact_batch_create(const iact_job_t* jobs, int32_t n_jobs, int32_t source_type,
+                      int32_t mode, const iact_opts_t* opts, iact_batch** out);
+int iact_batch_workspace_size(const iact_batch* batch, size_t* bytes);
+/* Binds the workspace (256-byte aligned) and queues the upload of the job
+ * table on `stream`; sets the kernels' shared-memory limits and grids. */
+int iact_batch_prepare(iact_batch* batch, void* workspace, size_t workspace_bytes,
+                       void* stream);
+/* Renders every job into its out: memsets and kernel launches on `stream`
+ * only (no allocation, no host synchronisation), so the call can be
+ * captured in a CUDA graph and replayed. Job arrays (samples, facet
+ * parameters, sources, values) are read when the kernels run. */
+int iact_batch_render(iact_batch* batch, void* stream);
+/* out[0] jobs, out[1] work tiles, out[2] rays, out[3] kernel launches per
+ * iact_batch_render, out[4] template classes used */
+int iact_batch_info(const iact_batch* batch, int64_t* out, int32_t n);
+void iact_batch_destroy(iact_batch* batch);
 
 #ifdef __cplusplus
 }

@@ -138,7 +138,14 @@ def test_adjoint_soft_sensors_position_path(cuda, kind):
     tel = small_dish(cam)
     d, val = _dirs()
     g = np.random.default_rng(2).standard_normal(P)
-    print(kind, compare(gpu_grads(tel, d, val, "parallel", g), twin_grads(tel, d, val, "parallel", g)))
+    # pixels fed by rays on a kink of the hexagonal norm carry no weight:
+    # the one-sided derivatives there differ between float32 and float64
+    pts, _ = it.render_debug(tel, d, val, "parallel")
+    _, sn = twin.scene_of(tel, 0, "parallel")
+    kink = twin.soft_hex_kink_pixels(sn, pts.cpu().numpy())
+    g[kink] = 0.0
+    print(kind, f"{kink.size} kink pixels", compare(gpu_grads(tel, d, val, "parallel", g),
+                                                     twin_grads(tel, d, val, "parallel", g)))
 
 
 def test_adjoint_cassegrain_through_the_secondary(cuda):

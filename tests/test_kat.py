@@ -1,0 +1,166 @@
+"""Analytic known answers of the render path, on the FP64 oracle (CPU) and
+on the CUDA path (GPU): exact geometric facts that hold for any sample set.
+
+  flux     An untilted facet under an on-axis parallel beam: every ray's
+           value is v * A / M (the integrator weight is cos_z / A * M,
+           core/integrators.py:124-127), so the image sums to v * A.
+  focus    A spherical facet (f = 10 m, 0.5 m radius) focuses that beam
+           into the one pixel at the focus (aberration 0.2 mm).
+  shadow   A flat facet under the same beam: a ray is shadowed exactly when
+           the vertical line through its sample meets an obstruction
+           (horizontal cylinder, sphere, box above the facet).
+  binning  A flat facet reflects the beam straight up: each ray lands on
+           the sensor at its sample's (x, y); the pixel must be the hexagon
+           (square) containing that point, -1 outside the camera.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+import pytest
+import torch
+
+import iactrace_gb300 as it
+from iactrace_gb300 import MCIntegrator, Mirror, SquareSensor, Telescope, workloads as W
+from iactrace_gb300.core import Box, Cylinder, DiskAperture, Sphere, group_obstructions
+from iactrace_gb300.core.surfaces import AsphericSurface
+from iactrace_gb300.telescope.mirrors import group_mirrors
+from iactrace_gb300.utils import keys as K
+
+R_AP = 0.5
+BEAM = torch.tensor([[0.0, 0.0, -1.0]])
+
+
+def facet(curvature=0.0, n_samples=4000, seed=3):
+    m = Mirror([0.0, 0.0, 0.0], [0.0, 0.0, 0.0], AsphericSurface(curvature, 0.0, []), DiskAperture(R_AP),
+               optical_stage=0)
+    g = group_mirrors([m])[0]
+    return MCIntegrator(n_samples).sample_group(g, K.key(seed))
+
+
+def obstructions():
+    return group_obstructions([Cylinder([-2.0, 0.0, 5.0], [2.0, 0.0, 5.0], 0.05),
+                               Sphere([0.2, 0.1, 4.0], 0.1),
+                               Box([-0.3, 0.2, 6.0], [-0.1, 0.3, 7.0])])
+
+
+def expected_shadow(x, y, band):
+    """Shadowed iff the vertical line through (x, y) meets an obstruction;
+    `edge` marks samples within `band` metres of a boundary."""
+    d_cyl = np.abs(y) - 0.05
+    d_sph = np.hypot(x - 0.2, y - 0.1) - 0.1
+    inside_box = (x > -0.3) & (x < -0.1) & (y > 0.2) & (y < 0.3)
+    d_box = np.minimum.reduce([np.abs(x + 0.3), np.abs(x + 0.1), np.abs(y - 0.2), np.abs(y - 0.3)])
+    shadow = (d_cyl < 0) | (d_sph < 0) | inside_box
+    edge = (np.abs(d_cyl) < band) | (np.abs(d_sph) < band) | (d_box < band)
+    return shadow, edge
+
+
+# The float32 quadratics of the reference's cylinder and sphere tests cancel
+# |o - centre|^2 (~25 m^2 here) against r^2 (0.0025 m^2): their decisions are
+# exact only farther than ~2e-5 m from the surface; FP64 (the oracle) to 1e-6 m.
+SHADOW_BAND = {"oracle": 1e-6, "gpu": 1e-4}
+
+
+def _debug(kind, tel, src, val, st):
+    if kind == "gpu":
+        pts, vals, pix, _ = it.render_debug(tel, src, val, st, extras=True)
+        return pts.cpu().double().numpy(), vals.cpu().double().numpy(), pix.cpu().numpy()
+    import oracle.oracle as O
+    d = O.render_debug(tel, src, val, st, 0, "f64")
+    return d["pts"], d["vals"], d["pix"]
+
+
+def _image(kind, tel, src, val, st):
+    if kind == "gpu":
+        return it.render(tel, src, val, st).cpu().double().numpy()
+    import oracle.oracle as O
+    return O.render(tel, src, val, st)
+
+
+KINDS = ["oracle", pytest.param("gpu", marks=pytest.mark.gpu)]
+
+
+@pytest.mark.parametrize("kind", KINDS)
+def test_kat_flux_and_focus(kind, request):
+    if kind == "gpu":
+        request.getfixturevalue("cuda")
+    else:
+        request.getfixturevalue("built")
+    g = facet(curvature=1.0 / 20.0)  # R = 2f, f = 10 m
+    cam = SquareSensor([0.0, 0.0, 10.0], [0.0, 0.0, 0.0], 11, 11, (-0.055, 0.055, -0.055, 0.055))
+    tel = Telescope([g], [], [cam])
+    v = 2.0
+    img = _image(kind, tel, BEAM, torch.tensor([v]), "parallel").reshape(11, 11)
+    total = v * math.pi * R_AP ** 2
+    tol = 1e-7 if kind == "oracle" else 2e-6  # the samples and weights are float32 inputs
+    assert abs(img[5, 5] - total) <= tol * total, (img[5, 5], total)
+    img[5, 5] = 0.0
+    assert np.all(img == 0.0)
+
+
+@pytest.mark.parametrize("kind", KINDS)
+def test_kat_shadow_masks(kind, request):
+    request.getfixturevalue("cuda" if kind == "gpu" else "built")
+    g = facet(curvature=0.0)
+    cam = SquareSensor([0.0, 0.0, 10.0], [0.0, 0.0, 0.0], 8, 8, (-0.6, 0.6, -0.6, 0.6))
+    tel = Telescope([g], obstructions(), [cam])
+    pts, vals, _ = _debug(kind, tel, BEAM, torch.ones(1), "parallel")
+    P = g.points.reshape(-1, 3).double().numpy()
+    shadow, edge = expected_shadow(P[:, 0], P[:, 1], SHADOW_BAND[kind])
+    got = vals == 0.0
+    assert shadow.sum() > 100 and (~shadow).sum() > 100
+    assert np.array_equal(got[~edge], shadow[~edge]), f"{(got != shadow)[~edge].sum()} shadow mismatches"
+    # unshadowed rays carry v * A / M
+    A = math.pi * R_AP ** 2
+    assert np.allclose(vals[~got], A / len(P), rtol=2e-6)
+
+
+def _hex_cell(centers, inradius, x, y):
+    """Containing hexagon (pointy-top, hex norm <= 1) of each point, -1 if none;
+    `edge` marks points within 1e-6 m (hex-norm units x inradius) of a border."""
+    d = np.stack([x[:, None] - centers[None, :, 0], y[:, None] - centers[None, :, 1]], -1)
+    ax, ay = np.abs(d[..., 0]), np.abs(d[..., 1])
+    hn = np.maximum(ax, 0.5 * ax + math.sqrt(3) / 2 * ay) / inradius
+    best = np.argmin(hn, axis=1)
+    hb = hn[np.arange(len(x)), best]
+    two = np.partition(hn, 1, axis=1)[:, :2]
+    edge = (np.abs(hb - 1.0) * inradius < 1e-6) | ((two[:, 1] - two[:, 0]) * inradius < 2e-6)
+    return np.where(hb <= 1.0, best, -1), edge
+
+
+@pytest.mark.parametrize("kind", KINDS)
+def test_kat_hex_binning(kind, request):
+    request.getfixturevalue("cuda" if kind == "gpu" else "built")
+    g = facet(curvature=0.0)
+    centers = W.hex_grid(400, 0.042)
+    cam = it.HexagonalSensor([0.0, 0.0, 1.0], [0.0, 0.0, 0.0], centers.astype(np.float32))
+    tel = Telescope([g], [], [cam])
+    pts, vals, pix = _debug(kind, tel, BEAM, torch.ones(1), "parallel")
+    P = g.points.reshape(-1, 3).double().numpy()
+    assert np.allclose(pts, P[:, :2], atol=2e-6)  # flat facet: straight up
+    want, edge = _hex_cell(centers.astype(np.float32).astype(np.float64), cam.hex_inradius, P[:, 0], P[:, 1])
+    assert (want >= 0).sum() > 1000 and (want < 0).sum() > 100
+    bad = (pix != want) & ~edge
+    assert not bad.any(), f"{bad.sum()} rays binned to the wrong hexagon"
+
+
+@pytest.mark.parametrize("kind", KINDS)
+def test_kat_square_binning_with_edge_band(kind, request):
+    request.getfixturevalue("cuda" if kind == "gpu" else "built")
+    g = facet(curvature=0.0)
+    ew = 0.004
+    cam = SquareSensor([0.0, 0.0, 1.0], [0.0, 0.0, 0.0], 20, 16, (-0.4, 0.4, -0.32, 0.32), edge_width=ew)
+    tel = Telescope([g], [], [cam])
+    pts, vals, pix = _debug(kind, tel, BEAM, torch.ones(1), "parallel")
+    P = g.points.reshape(-1, 3).double().numpy()
+    fx, fy = (P[:, 0] + 0.4) / 0.04, (P[:, 1] + 0.32) / 0.04
+    ix, iy = np.floor(fx), np.floor(fy)
+    inside = (ix >= 0) & (ix < 20) & (iy >= 0) & (iy < 16)
+    band = np.minimum(np.minimum(fx - ix, 1 - (fx - ix)), np.minimum(fy - iy, 1 - (fy - iy))) * 0.04
+    want = np.where(inside & (band >= ew), iy * 20 + ix, -1).astype(np.int64)
+    edge = (np.abs(band - ew) < 1e-6) | (np.abs(band) < 1e-6)
+    assert (want >= 0).sum() > 1000 and (want < 0).sum() > 100
+    bad = (pix != want) & ~edge
+    assert not bad.any(), f"{bad.sum()} rays binned to the wrong square pixel"

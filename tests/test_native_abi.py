@@ -15,20 +15,21 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def declared_symbols():
     src = open(os.path.join(ROOT, "include", "iactrace_gb300.h")).read()
-    return sorted(set(re.findall(r"^\s*(?:int|const char\*)\s+(iact_\w+)\s*\(", src, re.M)))
+    return sorted(set(re.findall(r"^\s*(?:int|void|const char\*)\s+(iact_\w+)\s*\(", src, re.M)))
 
 
 def test_exports_every_declared_symbol(built):
     lib = ctypes.CDLL(N.lib_path())
     syms = declared_symbols()
-    assert "iact_render" in syms and "iact_render_debug" in syms
+    assert "iact_render" in syms and "iact_render_debug" in syms and "iact_batch_destroy" in syms
+    assert sorted(N.EXPORTED) == [x for x in syms if x != "iact_render_noalloc"]
     for s in syms:
         assert hasattr(lib, s), f"{s} declared in include/iactrace_gb300.h but not exported"
 
 
 def test_layout_and_version(built):
     N.check_layout(built)
-    assert built.iact_abi_version() == 1
+    assert built.iact_abi_version() == 2
 
 
 def _square(n=4):
@@ -76,3 +77,53 @@ def test_render_without_device_fails_loudly(built):
     tel, src, val, st = W.plain_forward(n_samples=4, n_sources=1)
     with pytest.raises(RuntimeError):
         it.render(tel, src, val, st)
+
+
+def _fake_scene(F, M, n_cyl=0):
+    """Descriptor of F facets x M samples with dummy (never dereferenced) device pointers."""
+    sc = N.IactScene()
+    sc.n_facets, sc.n_samples = F, M
+    p = 0x10000
+    for name in ("facet_pos", "facet_rot", "facet_scale", "points", "normals", "delta", "weights"):
+        setattr(sc, name, p)
+    if n_cyl:
+        sc.n_cyl, sc.cyl = n_cyl, p
+    return sc
+
+
+def test_batch_planner_without_a_gpu(built):
+    """iact_batch_create plans on the host only: tiles, rays, classes and the
+    workspace size follow from the jobs; bad arguments are rejected."""
+    scenes = [_fake_scene(100, 256, 4), _fake_scene(37, 64), _fake_scene(5, 33)]
+    sn = _square(8)
+    S = [7, 1, 0]
+    jobs = (N.IactJob * 3)()
+    for i in range(3):
+        jobs[i].scene = ctypes.pointer(scenes[i])
+        jobs[i].sensor = ctypes.pointer(sn)
+        jobs[i].sources = jobs[i].values = 0x20000 if S[i] else None
+        jobs[i].n_sources = S[i]
+        jobs[i].out = 0x30000
+    h = ctypes.c_void_p()
+    assert built.iact_batch_create(jobs, 3, N.SRC_POINT, N.MODE_IMAGE, None, ctypes.byref(h)) == N.IACT_OK
+    info = (ctypes.c_int64 * 5)()
+    assert built.iact_batch_info(h, info, 5) == N.IACT_OK
+    assert info[0] == 3 and info[2] == 100 * 256 * 7 + 37 * 64 * 1
+    assert info[1] > 0 and info[4] == 1 and info[3] == 3  # prep, one render class, finish
+    size = ctypes.c_size_t(0)
+    assert built.iact_batch_workspace_size(h, ctypes.byref(size)) == N.IACT_OK
+    assert size.value >= (100 * 256 + 37 * 64 + 5 * 33) * 32 + 3 * 64 * 8
+    assert built.iact_batch_render(h, None) == N.IACT_E_INVALID  # not prepared: nothing queued
+    assert b"prepare" in built.iact_last_error()
+    built.iact_batch_destroy(h)
+    # rejected jobs
+    jobs[1].out = None
+    assert built.iact_batch_create(jobs, 3, N.SRC_POINT, N.MODE_IMAGE, None, ctypes.byref(h)) == N.IACT_E_INVALID
+    assert b"job 1" in built.iact_last_error()
+    jobs[1].out = 0x30000
+    assert built.iact_batch_create(jobs, 3, N.SRC_POINT, 9, None, ctypes.byref(h)) == N.IACT_E_INVALID
+    opts = N.IactOpts()
+    opts.block_threads = 100
+    assert built.iact_batch_create(jobs, 3, N.SRC_POINT, N.MODE_IMAGE, ctypes.byref(opts),
+                                   ctypes.byref(h)) == N.IACT_E_INVALID
+    assert built.iact_batch_create(jobs, -1, N.SRC_POINT, N.MODE_IMAGE, None, ctypes.byref(h)) == N.IACT_E_INVALID

@@ -284,3 +284,42 @@ def soft_base(sensor, pts):
     ri = np.where((dr > dq) & (dr > ds), -qi - si, ri)
     big = ~(x < 1e9)
     return {"base_q": np.where(big, 0, qi), "base_r": np.where(big, 0, ri)}
+
+
+def soft_hex_kink_pixels(sensor, pts, band=1e-6, wmin=1e-6):
+    """Pixel ids fed by rays whose soft-hex weights sit within `band` metres
+    of a kink of the hexagonal norm (|ux| = 0, |uy| = 0 or the two branches
+    of the max equal) on a tap of relative weight > wmin. The weights are not
+    differentiable there: float32 and float64 evaluations of the same ray
+    take opposite one-sided derivatives, so a gradient comparison must not
+    weight those pixels."""
+    if sensor["kind"] != "soft_hex":
+        return np.zeros(0, dtype=np.int64)
+    x, y = pts[:, 0].astype(np.float64), pts[:, 1].astype(np.float64)
+    ok = x < 1e9
+    base = soft_base(sensor, pts)
+    xs, ys = x - sensor["off_x"], y - sensor["off_y"]
+    xg, yg = sensor["gc"] * xs - sensor["gs"] * ys, sensor["gs"] * xs + sensor["gc"] * ys
+    ddx = xg - sensor["hex_sx"] * (base["base_q"] + base["base_r"] / 2)
+    ddy = yg - sensor["hex_sy"] * base["base_r"]
+    K = sensor["kernel_size"]
+    taps = [(q, rr) for q in range(-K, K + 1) for rr in range(-K, K + 1) if max(abs(q), abs(rr), abs(q + rr)) <= K]
+    table = np.asarray(sensor["table"])
+    near = np.zeros(x.shape, dtype=bool)
+    ws = []
+    for q, rr in taps:
+        ux = ddx - sensor["hex_sx"] * (q + rr / 2)
+        uy = ddy - sensor["hex_sy"] * rr
+        ax, ay = np.abs(ux), np.abs(uy)
+        hd = np.maximum(ax, 0.5 * ax + SQRT3_2 * ay) / sensor["inradius"]
+        w = np.exp(-0.5 * (hd / sensor["sigma"]) ** 2)
+        ws.append(w)
+        kink = np.minimum(np.minimum(ax, ay), np.abs(ax - (0.5 * ax + SQRT3_2 * ay)))
+        near |= ok & (kink < band) & (w > wmin * 1.0)
+    bad = []
+    for i in np.nonzero(near)[0]:
+        for q, rr in taps:
+            qi, ri = int(base["base_q"][i] + q) - sensor["q_min"], int(base["base_r"][i] + rr) - sensor["r_min"]
+            if 0 <= qi < table.shape[0] and 0 <= ri < table.shape[1] and table[qi, ri] >= 0:
+                bad.append(int(table[qi, ri]))
+    return np.unique(np.array(bad, dtype=np.int64))
