@@ -125,6 +125,50 @@ def workload_config(name, tel, S, mode, flush):
     return cfg, F * M * S
 
 
+def adjoint_kernel_seconds(tel, src, val, stype, mode, gout, flush_buf, steps):
+    """Event time of the adjoint kernel alone (iact_render_backward through
+    the C ABI, gradients w.r.t. facet rotations and positions, sources and
+    values), averaged over `steps` launches with the L2 flushed before each."""
+    import ctypes
+    from iactrace_gb300 import _native as N
+    from iactrace_gb300.core.render import source_code
+    from iactrace_gb300.core.scene import pack_scene
+    dev = src.device
+    lib = N.load()
+    ps = pack_scene(tel, dev)
+    sdesc, keep = tel.sensors[0].pack(dev)
+    S = src.shape[0]
+    ws = torch.empty(ps.workspace_bytes(sdesc, S, N.MODE_BACKWARD), dtype=torch.uint8, device=dev)
+    g = [torch.empty((ps.F, 3), device=dev), torch.empty((ps.F, 3), device=dev),
+         torch.empty((S, 3), device=dev), torch.empty(S, device=dev)]
+    nm = N.MODE_RESPONSE if mode == "response" else N.MODE_IMAGE
+    gout = gout.contiguous()
+    ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+    stream = torch.cuda.current_stream(dev)
+    ev[0].record(stream)
+    ev[1].record(stream)
+    o = N.IactOpts()
+    o.kernel_events[0], o.kernel_events[1] = ev[0].cuda_event, ev[1].cuda_event
+    code = source_code(stype)
+    no_src = code == N.SRC_EXTENDED
+
+    def call():
+        N.check(lib.iact_render_backward(ctypes.byref(ps.desc), ctypes.byref(sdesc), code, src.data_ptr(),
+                                         val.data_ptr(), S, nm, gout.data_ptr(), g[0].data_ptr(), g[1].data_ptr(),
+                                         None, None if no_src else g[2].data_ptr(), g[3].data_ptr(), None, None,
+                                         None, ws.data_ptr(), ws.numel(), ctypes.byref(o), stream.cuda_stream))
+
+    call()
+    tot = 0.0
+    for k in range(steps):
+        flush_buf.fill_(float(k))
+        call()
+        ev[1].synchronize()
+        tot += ev[0].elapsed_time(ev[1]) / 1e3
+    del keep
+    return tot / steps
+
+
 def fp32_peak_tflops(dev) -> float:
     """FP32 throughput of an FMA-chain probe kernel on this GPU (TFLOP/s)."""
     from iactrace_gb300 import _native as N
@@ -530,8 +574,11 @@ def main():
             fa_ev[k][1].record(stream)
         torch.cuda.synchronize(dev)
         fa_s = sum(a.elapsed_time(b) for a, b in fa_ev) / 1e3 / args.steps
+        adj_s = adjoint_kernel_seconds(tel, src, val, stype, mode, gout, flush_buf, args.steps)
         fwdadj = {"value": rays / fa_s, "unit": "rays/s", "ms_per_step": fa_s * 1e3,
                   "time_ratio_vs_fwd": fa_s / step_s,
+                  "adjoint_kernel_ms": adj_s * 1e3,
+                  "kernel_time_ratio_vs_fwd": (kern_s + adj_s) / kern_s,
                   "grads": "facet rotations and positions, sources, values"}
     except NotImplementedError as e:
         fwdadj = {"unavailable": str(e)}
