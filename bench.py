@@ -433,6 +433,42 @@ def run_batched(args, rank, world):
     fwd_adj()
     fa_steps = max(1, min(args.steps, 3))
     fa_s = timed(fwd_adj, fa_steps)
+
+    # forward + adjoint of every instance as two graph replays (iact_batch_backward)
+    bb = it.BatchRenderer(tels, srcs, vals, st, opts=b.opts, tune=False, backward=True,
+                          grads=("rot", "pos", "src", "val"))
+    gen = torch.Generator(device=dev).manual_seed(0)
+    for go in bb.grad_outs:
+        go.copy_(torch.randn(go.shape, device=dev, generator=gen))
+
+    def fwd_adj_batched():
+        bb()
+        bb.backward()
+
+    fwd_adj_batched()
+    fab_s = timed(fwd_adj_batched, fa_steps)
+    b_info = bb.info()
+    del bb
+
+    # the launch-bound regime: 64 small variants (1-64 sources, 100-300 facets)
+    st_tels, st_src, st_val, _ = W.ragged_batch(n_instances=64, seed=11, max_sources=64, max_facets=300)
+    st_src = [x.to(dev) for x in st_src]
+    st_val = [x.to(dev) for x in st_val]
+    st_rays = sum(len(t.mirror_groups[0]) * t.mirror_groups[0].n_samples * x.shape[0] for t, x in zip(st_tels, st_src))
+    sb = it.BatchRenderer(st_tels, st_src, st_val, st, tune=True)
+
+    def st_inst():
+        for t, x, v in zip(st_tels, st_src, st_val):
+            it.render(t, x, v, st)
+
+    for _ in range(args.warmup):
+        sb()
+        st_inst()
+    small = {"instances": 64, "sources_max": 64, "facets_min_max": [100, 300], "rays_per_step": st_rays}
+    small["batched_ms"] = timed(sb, args.steps) * 1e3
+    small["per_instance_ms"] = timed(st_inst, args.steps) * 1e3
+    small["batched_vs_per_instance"] = small["per_instance_ms"] / small["batched_ms"]
+    del sb
     clk = clocks.stop()
     peak = fp32_peak_tflops(dev)
     achieved = F_RAY["batched"] * rays / kern_s / 1e12
@@ -452,12 +488,17 @@ def run_batched(args, rank, world):
         "per_instance": {"value": rays / inst_s, "unit": "rays/s", "ms_per_step": inst_s * 1e3,
                          "launches_per_step": 3 * len(tels), "path": "render() per telescope, same stream"},
         "batched_vs_per_instance": inst_s / batch_s,
+        "small_instances": small,
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                      "traffic": None, "kernel": "k_batch_render", "kernel_ms": kern_s * 1e3,
                      "flops_per_ray": F_RAY["batched"],
                      "peak_source": "measured live: FP32 FMA-chain probe kernel (iact_probe_fma)"},
         "fwd_adjoint_per_instance": {"value": rays / fa_s, "unit": "rays/s", "ms_per_step": fa_s * 1e3,
                                      "time_ratio_vs_batched_fwd": fa_s / batch_s},
+        "fwd_adjoint_batched": {"value": rays / fab_s, "unit": "rays/s", "ms_per_step": fab_s * 1e3,
+                                "time_ratio_vs_batched_fwd": fab_s / batch_s,
+                                "vs_per_instance": fa_s / fab_s, "launches": b_info["launches"] +
+                                b_info["backward_launches"]},
         "autotune": {"knobs_block_tasks_hist": tune["knobs"] if tune else None,
                      "candidates_ms": tune["tried"] if tune else None, "setup_s": setup_s},
         "batch": info,

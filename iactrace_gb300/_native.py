@@ -38,6 +38,7 @@ SENSOR_HEX = 1
 SENSOR_SOFT_SQUARE = 2
 SENSOR_SOFT_HEX = 3
 FLAG_NO_CULL = 1
+FLAG_BATCH_BACKWARD = 2
 APERTURE_DISK = 0
 APERTURE_POLYGON = 1
 
@@ -94,7 +95,10 @@ class IactOpts(ctypes.Structure):
 class IactJob(ctypes.Structure):
     _fields_ = [("scene", ctypes.POINTER(IactScene)), ("sensor", ctypes.POINTER(IactSensor)),
                 ("sources", ctypes.c_void_p), ("values", ctypes.c_void_p), ("n_sources", _i),
-                ("seed", ctypes.c_uint32), ("out", ctypes.c_void_p)]
+                ("seed", ctypes.c_uint32), ("out", ctypes.c_void_p), ("grad_out", ctypes.c_void_p),
+                ("g_facet_rot", ctypes.c_void_p), ("g_facet_pos", ctypes.c_void_p), ("g_facet_scale", ctypes.c_void_p),
+                ("g_sources", ctypes.c_void_p), ("g_values", ctypes.c_void_p), ("g_mirror_rot", ctypes.c_void_p),
+                ("g_mirror_pos", ctypes.c_void_p), ("g_mirror_surface", ctypes.c_void_p)]
 
 
 class IactError(RuntimeError):
@@ -129,6 +133,7 @@ _SIGS = {
     "iact_batch_workspace_size": ([ctypes.c_void_p, ctypes.POINTER(ctypes.c_size_t)], ctypes.c_int),
     "iact_batch_prepare": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p], ctypes.c_int),
     "iact_batch_render": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "iact_batch_backward": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "iact_batch_info": ([ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64), _i], ctypes.c_int),
     "iact_batch_destroy": ([ctypes.c_void_p], None),
 }

@@ -10,6 +10,12 @@ that job up to FP64 summation order.
 Inputs stay bound to the batch: to render new parameters, write them into
 the batch's own tensors (``sources[i]``, ``values[i]``, ``facet_rotations[i]``
 ...) in place and call the batch again.
+
+With ``backward=True`` the batch also runs the adjoint of every job in one
+persistent launch (``iact_batch_backward``): write dL/d(out) into
+``grad_outs[i]`` and call ``backward()``; the gradients land in ``grads[i]``
+(facet rotations and positions, roughness scales, sources, values, stage
+mirrors, as requested).
 """
 from __future__ import annotations
 
@@ -32,8 +38,10 @@ class BatchRenderer:
     else the library defaults. graph: capture the launch in a CUDA graph.
     """
 
+    GRADS = ("rot", "pos", "scale", "src", "val", "mrot", "mpos", "msurf")
+
     def __init__(self, telescopes, sources, values, source_type="point", mode="image", sensor_idx=0, opts=None,
-                 seeds=None, graph=True, tune=True, device=None):
+                 seeds=None, graph=True, tune=True, device=None, backward=False, grads=("rot", "pos", "src", "val")):
         if not (len(telescopes) == len(sources) == len(values)):
             raise ValueError("telescopes, sources and values must have the same length")
         self.device = torch.device(device) if device is not None else _device()
@@ -77,12 +85,34 @@ class BatchRenderer:
             J.sources, J.values, J.n_sources = src.data_ptr(), val.data_ptr(), S
             J.seed = int(seeds[i]) & 0xFFFFFFFF if seeds is not None else 0
             J.out = out.data_ptr()
+        self.backward_enabled = bool(backward)
+        self.grad_outs, self.grads = [], []
+        if backward:
+            unknown = set(grads) - set(self.GRADS)
+            if unknown:
+                raise ValueError(f"unknown gradient names {sorted(unknown)}")
+            for i in range(n):
+                F, M, S, P, kind, nm = shapes[i]
+                go = torch.zeros_like(self.outs[i])
+                shp = {"rot": (F, 3), "pos": (F, 3), "scale": (F,), "src": (S, 3), "val": (S,), "mrot": (nm, 3),
+                       "mpos": (nm, 3), "msurf": (nm, 2 + N.IACT_MAX_ASPH)}
+                gi = {k: torch.zeros(shp[k], device=self.device) for k in grads
+                      if not (k == "src" and self.code == N.SRC_EXTENDED) and not (k[0] == "m" and nm == 0)}
+                self.grad_outs.append(go)
+                self.grads.append(gi)
+                J = self._jobs[i]
+                J.grad_out = go.data_ptr()
+                ptr = lambda k: gi[k].data_ptr() if k in gi else None
+                J.g_facet_rot, J.g_facet_pos, J.g_facet_scale = ptr("rot"), ptr("pos"), ptr("scale")
+                J.g_sources, J.g_values = ptr("src"), ptr("val")
+                J.g_mirror_rot, J.g_mirror_pos, J.g_mirror_surface = ptr("mrot"), ptr("mpos"), ptr("msurf")
         self.n_jobs = n
         self.rays = sum(F * M * S for F, M, S, *_ in shapes)
         self.signature = (self.mode, self.code, tuple(shapes))
         self._handle = None
         self._ws = None
         self._graph = None
+        self._bgraph = None
         if opts is None and tune:
             from .autotune import tune_batch
             opts = tune_batch(self)
@@ -94,6 +124,12 @@ class BatchRenderer:
     # ---------------------------------------------------------------- plumbing
     def _create(self, opts):
         h = ctypes.c_void_p()
+        if self.backward_enabled:
+            o = N.IactOpts()
+            if opts is not None:
+                ctypes.memmove(ctypes.addressof(o), ctypes.addressof(opts), ctypes.sizeof(o))
+            o.flags |= N.FLAG_BATCH_BACKWARD
+            opts = o
         N.check(self.lib.iact_batch_create(self._jobs, self.n_jobs, self.code, self.mode,
                                            ctypes.byref(opts) if opts is not None else None, ctypes.byref(h)))
         size = ctypes.c_size_t(0)
@@ -112,17 +148,42 @@ class BatchRenderer:
         stream = stream or torch.cuda.current_stream(self.device)
         N.check(self.lib.iact_batch_render(self._handle, stream.cuda_stream))
 
-    def capture(self):
-        """Capture the batch's launch sequence in a CUDA graph."""
+    def launch_backward(self, stream=None):
+        """Queue the adjoint of every job on `stream` (default: current stream)."""
+        if not self.backward_enabled:
+            raise RuntimeError("create the BatchRenderer with backward=True")
+        stream = stream or torch.cuda.current_stream(self.device)
+        N.check(self.lib.iact_batch_backward(self._handle, stream.cuda_stream))
+
+    def _capture(self, fn):
         side = torch.cuda.Stream(self.device)
         side.wait_stream(torch.cuda.current_stream(self.device))
         with torch.cuda.stream(side):
-            self.launch(side)  # first launch outside the capture
+            fn(side)  # first launch outside the capture
         torch.cuda.current_stream(self.device).wait_stream(side)
         g = torch.cuda.CUDAGraph()
         with torch.cuda.graph(g):
-            self.launch()
-        self._graph = g
+            fn(None)
+        return g
+
+    def capture(self):
+        """Capture the batch's launch sequences (forward, backward) in CUDA graphs."""
+        self._graph = self._capture(self.launch)
+        if self.backward_enabled:
+            self._bgraph = self._capture(self.launch_backward)
+
+    def backward(self, grad_outs=None):
+        """Adjoint of every job: dL/d(out_i) from `grad_outs` (copied into the
+        bound tensors) or from the bound ``grad_outs`` as they are; returns
+        the list of gradient dicts (owned by the batch)."""
+        if grad_outs is not None:
+            for dst, src in zip(self.grad_outs, grad_outs):
+                dst.copy_(src)
+        if self._bgraph is not None:
+            self._bgraph.replay()
+        else:
+            self.launch_backward()
+        return self.grads
 
     def __call__(self):
         """Render every job; returns the list of outputs (owned by the batch)."""
@@ -133,13 +194,15 @@ class BatchRenderer:
         return self.outs
 
     def info(self) -> dict:
-        v = (ctypes.c_int64 * 5)()
-        N.check(self.lib.iact_batch_info(self._handle, v, 5))
-        return {"jobs": v[0], "tiles": v[1], "rays": v[2], "launches": v[3], "classes": v[4]}
+        v = (ctypes.c_int64 * 7)()
+        N.check(self.lib.iact_batch_info(self._handle, v, 7))
+        return {"jobs": v[0], "tiles": v[1], "rays": v[2], "launches": v[3], "classes": v[4],
+                "adjoint_tiles": v[5], "backward_launches": v[6]}
 
     def release(self):
         if self._handle is not None:
             self._graph = None
+            self._bgraph = None
             self.lib.iact_batch_destroy(self._handle)
             self._handle = None
             self._ws = None

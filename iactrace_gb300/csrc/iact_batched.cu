@@ -23,36 +23,30 @@
 #include <string>
 #include <vector>
 
+#include "iact_batch.h"
 #include "iact_device.cuh"
 #include "iact_internal.h"
 #include "iact_render_impl.cuh"
 
 namespace iact {
 
-struct BatchJob {
-  RenderK rk;       // pointers resolved into the workspace
-  PrepK pk;
-  float* out;
-  long long n_out;  // out entries (P, or S*P)
-  int tile_begin;   // first tile of this job in its class's queue
-  int pad_;
-};
-
-struct BatchK {
-  const BatchJob* jobs;  // this class's jobs (largest first)
-  int n_jobs;
-  int n_tiles;
-  int* counter;
-  int tab_floats;   // table area (floats, multiple of 4)
-  int htab_elems;   // int16 hexagon lookup area (multiple of 8)
-  int hist_floats;  // FP32 histogram area; the tile's candidate masks follow it
-};
-
-__global__ void __launch_bounds__(256) k_batch_prep(const BatchJob* __restrict__ jobs) {
-  const PrepK& p = jobs[blockIdx.y].pk;
+// backward != 0: the backward prep (with roughness deltas where asked) and
+// zeroed gradient buckets
+__global__ void __launch_bounds__(256) k_batch_prep(const BatchJob* __restrict__ jobs, int backward) {
+  const BatchJob& J = jobs[blockIdx.y];
+  const PrepK& p = backward ? J.pkb : J.pk;
   if (blockIdx.x == 0) prep_tables(p);
   const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   prep_chunks(p, w, ((long long)gridDim.x * blockDim.x) >> 5);
+  if (backward)
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < J.gr.n_bucket;
+         i += (long long)gridDim.x * blockDim.x)
+      J.ak.gfacet[i] = 0.0;
+}
+
+int launch_batch_prep(const BatchJob* jobs, int n_jobs, int gx, int backward, cudaStream_t st) {
+  k_batch_prep<<<dim3(gx, n_jobs), 256, 0, st>>>(jobs, backward);
+  return check_cuda(cudaGetLastError(), "k_batch_prep launch");
 }
 
 template <int SRC, bool SOFT, int MODE, bool STAGES>
@@ -152,33 +146,6 @@ bool is_soft(const iact_sensor_t& s) { return s.type == IACT_SENSOR_SOFT_SQUARE 
 
 using namespace iact;
 
-struct iact_batch {
-  int src_type = 0, mode = 0, block = 256;
-  iact_opts_t opts;
-  std::vector<iact_scene_t> scenes;
-  std::vector<iact_sensor_t> sensors;
-  std::vector<iact_job_t> jobs;
-  // plan: job table position -> user's job index, per-position layout
-  std::vector<int> order;
-  std::vector<RenderK> rk;  // workspace offsets still relative (base 0)
-  std::vector<WsLayout> lay;
-  std::vector<size_t> region, acc_off;
-  struct Class {
-    int soft = 0, stages = 0;
-    int jb = 0, nj = 0, n_tiles = 0;
-    int tab_floats = 0, htab_elems = 0, hist_floats = 0;
-    size_t smem = 0;
-    int grid = 0;
-  };
-  std::vector<Class> classes;
-  size_t off_counter = 0, off_jobs = 0, off_acc = 0, acc_bytes = 0, total = 0;
-  long long tiles = 0, rays = 0, max_fm = 0, max_out = 0;  // max_fm: (facet, chunk) units
-  // prepare
-  char* ws = nullptr;
-  std::vector<BatchJob> table;
-  int prep_gx = 1, fin_gx = 1;
-};
-
 extern "C" {
 
 int iact_batch_create(const iact_job_t* jobs, int32_t n_jobs, int32_t source_type, int32_t mode,
@@ -204,13 +171,23 @@ int iact_batch_create(const iact_job_t* jobs, int32_t n_jobs, int32_t source_typ
     if (mode == IACT_MODE_RESPONSE && (long long)J.n_sources * J.sensor->n_pixels > 0x7fffffffLL)
       return set_error(IACT_E_UNSUPPORTED, at + "response matrix larger than 2^31 entries");
     if (!J.out && acc_elems(J.sensor, J.n_sources, mode) > 0) return set_error(IACT_E_INVALID, at + "out is NULL");
+    if (opts && (opts->flags & IACT_FLAG_BATCH_BACKWARD)) {
+      if (J.scene->n_stages > 2)
+        return set_error(IACT_E_UNSUPPORTED, at + "backward: at most 2 mirror stages after the primary");
+      if (source_type == IACT_SRC_EXTENDED && J.g_sources)
+        return set_error(IACT_E_UNSUPPORTED, at + "backward: no source gradients for extended sources");
+      if (!J.grad_out && acc_elems(J.sensor, J.n_sources, mode) > 0)
+        return set_error(IACT_E_INVALID, at + "backward: grad_out is NULL");
+    }
   }
+  const bool backward = opts && (opts->flags & IACT_FLAG_BATCH_BACKWARD);
 
   iact_batch* b = new (std::nothrow) iact_batch();
   if (!b) return set_error(IACT_E_INVALID, "iact_batch_create: out of host memory");
   b->src_type = source_type;
   b->mode = mode;
   b->block = block;
+  b->backward = backward;
   memset(&b->opts, 0, sizeof(b->opts));
   if (opts) b->opts = *opts;
   b->scenes.resize(n_jobs);
@@ -225,14 +202,27 @@ int iact_batch_create(const iact_job_t* jobs, int32_t n_jobs, int32_t source_typ
 
   // per-job tiles (workspace pointers relative to a zero base for now)
   std::vector<RenderK> rk(n_jobs);
+  std::vector<AdjK> ak(backward ? n_jobs : 0);
+  std::vector<size_t> a_smem(backward ? n_jobs : 0);
   std::vector<WsLayout> lay(n_jobs);
   for (int i = 0; i < n_jobs; ++i) {
-    lay[i] = workspace_layout(&b->scenes[i], 0, false);
+    // the backward layout holds the forward's arrays too (plus deltas and buckets)
+    lay[i] = backward ? workspace_for(&b->scenes[i], &b->sensors[i], jobs[i].n_sources, IACT_MODE_BACKWARD)
+                      : workspace_layout(&b->scenes[i], 0, false);
     rk[i] = base_params(&b->scenes[i], &b->sensors[i], lay[i], nullptr, jobs[i].sources, jobs[i].values,
                         jobs[i].n_sources);
     rk[i].seed = jobs[i].seed;
     if (opts && (opts->flags & IACT_FLAG_NO_CULL)) rk[i].n_words = 0;
-    int rc = plan_tiles(rk[i], mode, block, opts);
+    int rc = plan_tiles(rk[i], mode, block, opts, 0);
+    if (!rc && backward) {
+      iact_opts_t o;
+      memset(&o, 0, sizeof(o));
+      if (opts) o = *opts;
+      o.seed = jobs[i].seed;
+      ak[i] = adjoint_params(&b->scenes[i], &b->sensors[i], lay[i], nullptr, jobs[i].sources, jobs[i].values,
+                             jobs[i].grad_out, jobs[i].n_sources, jobs[i].g_facet_scale != nullptr, &o);
+      rc = plan_adjoint(ak[i], &b->sensors[i], block, a_smem[i], 0);
+    }
     if (rc) {
       delete b;
       return rc;
@@ -291,13 +281,35 @@ int iact_batch_create(const iact_job_t* jobs, int32_t n_jobs, int32_t source_typ
     C.htab_elems = (int)(htab_floor / sizeof(short));
     C.hist_floats = (int)(hist / sizeof(float));
     C.smem = tab_floor + htab_floor + hist + masks;
+    if (backward) {  // adjoint layout: tables | int16 hex table | stage-mirror sums | masks
+      size_t atab = 0, ahtab = 0, amir = 0, amask = 0;
+      long long at = 0;
+      for (int i : mem) {
+        const AdjK& a = ak[i];
+        atab = std::max(atab, sizeof(float) * (size_t)((a.n_table_floats + 3) & ~3));
+        if (a.hex_in_smem)
+          ahtab = std::max(ahtab, sizeof(short) * (((size_t)a.sn.table_q * a.sn.table_r + 7) & ~(size_t)7));
+        amir = std::max(amir, sizeof(float) * (size_t)a.n_mir * kMirGrad);
+        amask = std::max(amask, sizeof(uint32_t) * (size_t)a.n_words * a.SB * a.FC * a.CC);
+        at += a.n_tiles;
+      }
+      if (at > 0x7fffffffLL || atab + ahtab + amir + amask > budget) {
+        delete b;
+        return set_error(IACT_E_UNSUPPORTED, "iact_batch_create: backward plan does not fit");
+      }
+      C.a_tiles = (int)at;
+      C.a_tab_floats = (int)(atab / sizeof(float));
+      C.a_htab_elems = (int)(ahtab / sizeof(short));
+      C.a_mgrad_floats = (int)(amir / sizeof(float));
+      C.a_smem = atab + ahtab + amir + amask;
+    }
     b->classes.push_back(C);
   }
 
   // workspace: counters, job table, per-job tables and samples, accumulators
   size_t off = 0;
-  b->off_counter = off;
-  off = a256(off + 64 * 4);
+  b->off_counter = off;  // 64 B per class: 4 forward, 4 backward
+  off = a256(off + 64 * 8);
   b->off_jobs = off;
   off = a256(off + sizeof(BatchJob) * (size_t)std::max(n_jobs, 1));
   b->region.assign(n_jobs, 0);
@@ -318,11 +330,14 @@ int iact_batch_create(const iact_job_t* jobs, int32_t n_jobs, int32_t source_typ
   b->total = a256(off + acc);
   for (int i = 0; i < n_jobs; ++i) {
     b->tiles += rk[i].n_tiles;
+    if (backward) b->a_tiles += ak[i].n_tiles;
     b->rays += (long long)rk[i].S * rk[i].F * rk[i].M;
     b->max_fm = std::max(b->max_fm, (long long)rk[i].F * ((rk[i].M + 31) / 32));  // (facet, chunk) units
     b->max_out = std::max(b->max_out, (long long)acc_elems(&b->sensors[i], jobs[i].n_sources, mode));
+    b->max_fs = std::max(b->max_fs, (long long)std::max(std::max(rk[i].F, rk[i].S), b->scenes[i].n_mirrors));
   }
   b->rk = std::move(rk);
+  b->ak = std::move(ak);
   b->lay = std::move(lay);
   *out = b;
   return IACT_OK;
@@ -346,7 +361,7 @@ int iact_batch_prepare(iact_batch* b, void* workspace, size_t workspace_bytes, v
   std::vector<BatchJob> table(n_jobs);
   for (int ci = 0; ci < (int)b->classes.size(); ++ci) {
     const iact_batch::Class& C = b->classes[ci];
-    int tile = 0;
+    int tile = 0, atile = 0;
     for (int pos = C.jb; pos < C.jb + C.nj; ++pos) {
       const int i = b->order[pos];
       char* base = ws + b->region[pos];
@@ -364,6 +379,31 @@ int iact_batch_prepare(iact_batch* b, void* workspace, size_t workspace_bytes, v
       J.n_out = (long long)acc_elems(&b->sensors[i], b->jobs[i].n_sources, b->mode);
       J.tile_begin = tile;
       tile += J.rk.n_tiles;
+      if (b->backward) {
+        const iact_job_t& U = b->jobs[i];
+        const AdjK& a0 = b->ak[i];
+        AdjK& a = J.ak;
+        a = a0;
+        a.P4 = reinterpret_cast<const float4*>(base + b->lay[i].p4);
+        a.N4 = reinterpret_cast<const float4*>(base + b->lay[i].n4);
+        a.D4 = U.g_facet_scale ? reinterpret_cast<const float4*>(base + b->lay[i].d4) : nullptr;
+        a.B4 = b->lay[i].n_b4 ? reinterpret_cast<const float4*>(base + b->lay[i].b4) : nullptr;
+        a.tables = reinterpret_cast<const float*>(base + b->lay[i].tables);
+        a.counter = reinterpret_cast<int*>(base + b->lay[i].counter);
+        a.gfacet = reinterpret_cast<double*>(base + b->lay[i].acc);
+        a.gsrc = a.gfacet + (size_t)a.F * kFacetGrad;
+        a.gmir = a.gsrc + (size_t)a.S * 4;
+        J.pkb = prep_params(&b->scenes[i], b->lay[i], base, U.g_facet_scale != nullptr);
+        J.gr.g_rot = U.g_facet_rot; J.gr.g_pos = U.g_facet_pos; J.gr.g_scale = U.g_facet_scale;
+        J.gr.g_src = U.g_sources; J.gr.g_val = U.g_values;
+        J.gr.g_mrot = U.g_mirror_rot; J.gr.g_mpos = U.g_mirror_pos; J.gr.g_msurf = U.g_mirror_surface;
+        J.gr.facet_rot = b->scenes[i].facet_rot;
+        J.gr.mirrors = b->scenes[i].mirrors;
+        J.gr.F = a.F; J.gr.S = a.S; J.gr.n_mir = a.n_mir;
+        J.gr.n_bucket = (long long)a.F * kFacetGrad + (long long)a.S * 4 + (long long)a.n_mir * kMirGrad;
+        J.atile_begin = atile;
+        atile += a.n_tiles;
+      }
     }
   }
   int rc = IACT_OK;
@@ -380,7 +420,15 @@ int iact_batch_prepare(iact_batch* b, void* workspace, size_t workspace_bytes, v
     if (rc) return rc;
     if (per_sm < 1) return set_error(IACT_E_UNSUPPORTED, "batched render kernel does not fit on an SM");
     C.grid = std::max(1, std::min(C.n_tiles, per_sm * di.sm_count));
+    if (b->backward) {
+      per_sm = 0;
+      rc = resident_ctas(batch_adjoint_kernel(b->src_type, C.soft, b->mode, C.stages), b->block, C.a_smem, &per_sm);
+      if (rc) return rc;
+      if (per_sm < 1) return set_error(IACT_E_UNSUPPORTED, "batched adjoint kernel does not fit on an SM");
+      C.a_grid = std::max(1, std::min(C.a_tiles, per_sm * di.sm_count));
+    }
   }
+  b->afin_gx = (int)std::max<long long>(1, std::min<long long>((b->max_fs + 255) / 256, 1024));
   b->prep_gx = (int)std::max<long long>(1, std::min<long long>((b->max_fm + 7) / 8, 1024));  // 8 warps per block
   b->fin_gx = (int)std::max<long long>(1, std::min<long long>((b->max_out + 255) / 256, 1024));
   b->table = std::move(table);
@@ -403,8 +451,7 @@ int iact_batch_render(iact_batch* b, void* stream) {
     if (rc) return rc;
   }
   if (b->max_fm > 0) {
-    k_batch_prep<<<dim3(b->prep_gx, n_jobs), 256, 0, st>>>(jobs);
-    rc = check_cuda(cudaGetLastError(), "k_batch_prep launch");
+    rc = launch_batch_prep(jobs, n_jobs, b->prep_gx, 0, st);
     if (rc) return rc;
   }
   void* const* ev = b->opts.kernel_events;
@@ -434,10 +481,15 @@ int iact_batch_render(iact_batch* b, void* stream) {
 
 int iact_batch_info(const iact_batch* b, int64_t* out, int32_t n) {
   if (!b || !out) return set_error(IACT_E_INVALID, "iact_batch_info: NULL argument");
-  int launches = (b->max_fm > 0 ? 1 : 0) + (b->max_out > 0 ? 1 : 0);
+  int launches = (b->max_fm > 0 ? 1 : 0) + (b->max_out > 0 ? 1 : 0), alaunches = 0;
   for (const auto& C : b->classes) launches += C.n_tiles > 0 ? 1 : 0;
-  const int64_t v[5] = {(int64_t)b->jobs.size(), b->tiles, b->rays, launches, (int64_t)b->classes.size()};
-  for (int i = 0; i < n && i < 5; ++i) out[i] = v[i];
+  if (b->backward) {
+    alaunches = 2;  // prep (+ bucket zeroing), finish
+    for (const auto& C : b->classes) alaunches += C.a_tiles > 0 ? 1 : 0;
+  }
+  const int64_t v[7] = {(int64_t)b->jobs.size(), b->tiles, b->rays, launches, (int64_t)b->classes.size(),
+                        b->a_tiles, alaunches};
+  for (int i = 0; i < n && i < 7; ++i) out[i] = v[i];
   return IACT_OK;
 }
 

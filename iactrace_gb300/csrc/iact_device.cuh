@@ -25,7 +25,7 @@ constexpr int kBoxF = 6;    // min(3) max(3)
 constexpr int kSphF = 4;    // center(3) r*r
 constexpr int kOboxF = 15;  // center(3) half(3) R(9) row-major local->world
 constexpr int kTriF = 9;    // v0(3) e1(3) e2(3)
-constexpr int kMirF = 48;   // see MirRec
+constexpr int kMirF = 52;   // see MirRec
 
 // One stage >= 1 mirror, as laid out in shared memory (floats).
 struct MirRec {
@@ -44,6 +44,9 @@ struct MirRec {
   float k;          // 23  conic constant
   float asph[8];    // 24..31
   float vert[16];   // 32..47
+  float z0_hi;      // 48  sag at the offset (FP64 value as hi + lo floats)
+  float z0_lo;      // 49
+  float pad[2];     // 50..51
 };
 static_assert(sizeof(MirRec) == kMirF * sizeof(float), "MirRec layout");
 
@@ -454,9 +457,10 @@ __device__ __forceinline__ int bin_hex(const SensorK& s, const TT* table, float 
 }
 
 // ------------------------------------------------------- stage >= 1 mirrors
-// core/surfaces.py:25-39 _sag_raw and its r2-derivative, in FP64: the sag
-// root is the one place where the float32 chain cancels (ray origins several
-// metres from the surface against a 1e-6 residual tolerance).
+// core/surfaces.py:25-39 _sag_raw in FP64 (reference form; used once per
+// mirror for z0): the sag root is the one place where the float32 chain
+// cancels (ray origins several metres from the surface against a 1e-6
+// residual tolerance).
 __device__ __forceinline__ double sag_raw_d(const float* m, double r2) {
   double c = m[15], alpha = (1.0 + (double)m[23]) * c * c;
   double den = 1.0 + sqrt(1.0 - alpha * r2);
@@ -472,21 +476,60 @@ __device__ __forceinline__ double sag_raw_d(const float* m, double r2) {
   }
   return z;
 }
-__device__ __forceinline__ double sag_raw_dr2_d(const float* m, double r2) {
-  double c = m[15], alpha = (1.0 + (double)m[23]) * c * c;
-  double s = sqrt(1.0 - alpha * r2);
-  double den = 1.0 + s;
-  double dz = c / den + (r2 * c) * alpha / (2.0 * s * den * den);
-  int na = (int)m[19];
+// FP64 reciprocal and reciprocal square root: the hardware float32
+// approximations refined by two Newton-Raphson steps each (y' = y + y e,
+// e = 1 - x y, and y' = y + y e / 2, e = 1 - x y^2; the classic iterations,
+// e.g. Muller et al., Handbook of Floating-Point Arithmetic, ch. 5): each step
+// squares the relative error, 2e-7 -> 1e-13 -> below the double rounding.
+// Arguments must be normal float32 numbers (the callers guard the ranges).
+__device__ __forceinline__ double rcp_d(double x) {
+  double y = (double)rcp_a((float)x);
+  double e = fma(-x, y, 1.0);
+  y = fma(y, e, y);
+  e = fma(-x, y, 1.0);
+  return fma(y, e, y);
+}
+__device__ __forceinline__ double rsqrt_d(double x) {
+  float xf = (float)x, yf;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(yf) : "f"(xf));
+  double y = yf;
+  double e = fma(-x * y, y, 1.0);
+  y = fma(0.5 * y, e, y);
+  e = fma(-x * y, y, 1.0);
+  return fma(0.5 * y, e, y);
+}
+// sqrt(x) for x >= 0 (0 -> 0), NaN for x < 0 as the IEEE square root
+__device__ __forceinline__ double sqrt_d(double x) {
+  return x > 0.0 ? x * rsqrt_d(x) : (x == 0.0 ? 0.0 : __longlong_as_double(0x7ff8000000000000ll));
+}
+
+// core/surfaces.py:25-39 _sag_raw and its r2-derivative together (one square
+// root, one reciprocal): S = c r2 / (1 + q) + sum a_i r2^(2(i+1)),
+// dS/dr2 = c / (1 + q) + c alpha r2 / (2 q (1 + q)^2) + sum ..., q = sqrt(1 - alpha r2)
+__device__ __forceinline__ void sag_eval_d(const float* m, double r2, double& S, double& dS) {
+  const double c = m[15], alpha = (1.0 + (double)m[23]) * c * c;
+  const double qq = fma(-alpha, r2, 1.0);
+  const double rq = qq > 0.0 ? rsqrt_d(qq) : (qq == 0.0 ? __longlong_as_double(0x7ff0000000000000ll)
+                                                       : __longlong_as_double(0x7ff8000000000000ll));
+  const double q = qq > 0.0 ? qq * rq : (qq == 0.0 ? 0.0 : rq);
+  const double id = rcp_d(1.0 + q);
+  const double cid = c * id;
+  S = r2 * cid;
+  dS = cid + 0.5 * (r2 * alpha) * cid * id * rq;
+  const int na = (int)m[19];
   if (na > 0) {
-    double r4 = r2 * r2, pm1 = r2, sacc = 0.0;  // p*r2^(p-1), p = 2(i+1)
+    const double r4 = r2 * r2;
+    double p = r4, pm1 = r2, sa = 0.0, sd = 0.0;  // a_i r2^p, p a_i r2^(p-1), p = 2(i+1)
     for (int i = 0; i < na; ++i) {
-      sacc += (double)m[24 + i] * (double)(2 * (i + 1)) * pm1;
+      const double a = m[24 + i];
+      sa = fma(a, p, sa);
+      sd = fma(a * (double)(2 * (i + 1)), pm1, sd);
+      p *= r4;
       pm1 *= r4;
     }
-    dz += sacc;
+    S += sa;
+    dS += sd;
   }
-  return dz;
 }
 
 // core/intersections.py:229-285 intersect_conic (on the raw-frame origin)
@@ -500,8 +543,10 @@ __device__ __forceinline__ double conic_t(const float* m, double ox, double oy, 
   if (fabs(c) < 1e-12) return (fabs(dz) > 1e-10) ? -oz / dz : inf;
   double disc = B * B - 4.0 * A * C;
   if (disc < 0.0) return inf;
-  double sq = sqrt(disc);
-  double t1 = (-B - sq) / (2.0 * A + 1e-30), t2 = (-B + sq) / (2.0 * A + 1e-30);
+  double sq = sqrt_d(disc);
+  const double den = 2.0 * A + 1e-30;
+  const double iden = fabs(den) > 1e-37 ? rcp_d(den) : 1.0 / den;
+  double t1 = (-B - sq) * iden, t2 = (-B + sq) * iden;
   bool v1 = t1 > 1e-8, v2 = t2 > 1e-8;
   return (v1 && v2) ? fmin(t1, t2) : (v1 ? t1 : (v2 ? t2 : inf));
 }
@@ -509,37 +554,41 @@ __device__ __forceinline__ double conic_t(const float* m, double ox, double oy, 
 // core/surfaces.py:67-108 AsphericSurface.intersect + core/intersections.py:290-367
 // newton_raphson_intersect (10 steps, tol 1e-8, valid if t > 1e-8 and
 // |g| < 1e-6). Local frame in, local point and unit normal out; returns t or
-// +inf when invalid or outside the aperture (core/render.py:100-101).
+// +inf when invalid or outside the aperture (core/render.py:100-101). The
+// root is found in FP64 (the sag at z0, the conic start, the Newton steps,
+// the residual); the Newton step divides by a float32 reciprocal of g'
+// (it still converges to the FP64 root); the unit normal is float32.
 __device__ __forceinline__ float mirror_hit(const float* m, V3 o, V3 d, V3& pl, V3& nl) {
   const float inf = __int_as_float(0x7f800000);
-  double x0 = m[12], y0 = m[13];
-  double z0 = sag_raw_d(m, x0 * x0 + y0 * y0);
-  double ox = o.x, oy = o.y, oz = o.z, dx = d.x, dy = d.y, dz = d.z;
+  const double x0 = m[12], y0 = m[13];
+  const double z0 = (double)m[48] + (double)m[49];
+  const double ox = o.x, oy = o.y, oz = o.z, dx = d.x, dy = d.y, dz = d.z;
   double t = conic_t(m, ox + x0, oy + y0, oz + z0, dx, dy, dz);
   bool conv = false;
   for (int it = 0; it < 10; ++it) {
     if (!conv) {
-      double xs = ox + t * dx + x0, ys = oy + t * dy + y0;
-      double r2 = xs * xs + ys * ys;
-      double g = (oz + t * dz) - (sag_raw_d(m, r2) - z0);
-      double gd = sag_raw_dr2_d(m, r2);
-      double gp = dz - (gd * (2.0 * xs) * dx + gd * (2.0 * ys) * dy);
-      double gs = (fabs(gp) > 1e-12) ? gp : 1e-12;
+      const double xs = fma(t, dx, ox) + x0, ys = fma(t, dy, oy) + y0;
+      const double r2 = xs * xs + ys * ys;
+      double S, dS;
+      sag_eval_d(m, r2, S, dS);
+      const double g = fma(t, dz, oz) - (S - z0);
+      const double gp = dz - 2.0 * dS * (xs * dx + ys * dy);
+      const double gs = (fabs(gp) > 1e-12) ? gp : 1e-12;
       conv = fabs(g) < 1e-8;
-      t = t - g / gs;
+      t = t - g * (double)rcp_a((float)gs);
     }
   }
-  double xh = ox + t * dx, yh = oy + t * dy;
-  double xs = xh + x0, ys = yh + y0;
-  double r2 = xs * xs + ys * ys;
-  double zs = sag_raw_d(m, r2) - z0;
-  double res = fabs((oz + t * dz) - zs);
-  bool valid = (t > 1e-8) && (res < 1e-6);
-  double gd = sag_raw_dr2_d(m, r2);
-  double nx = -(gd * 2.0 * xs), ny = -(gd * 2.0 * ys);
-  double nn = sqrt(nx * nx + ny * ny + 1.0);
+  const double xh = fma(t, dx, ox), yh = fma(t, dy, oy);
+  const double xs = xh + x0, ys = yh + y0;
+  double S, dS;
+  sag_eval_d(m, xs * xs + ys * ys, S, dS);
+  const double zs = S - z0;
+  const double res = fabs(fma(t, dz, oz) - zs);
+  const bool valid = (t > 1e-8) && (res < 1e-6);
+  const float nx = (float)(-2.0 * dS * xs), ny = (float)(-2.0 * dS * ys);
+  const float inn = rsqrtf(fmaf(nx, nx, fmaf(ny, ny, 1.f)));
   pl = mk((float)xh, (float)yh, (float)zs);
-  nl = mk((float)(nx / nn), (float)(ny / nn), (float)(1.0 / nn));
+  nl = mk(nx * inn, ny * inn, inn);
   // telescope/mirrors.py:147-149 disk, :209-220 polygon check_aperture
   bool in_ap;
   if ((int)m[20] == IACT_APERTURE_DISK) {
@@ -608,15 +657,20 @@ struct SagD {
 __device__ __forceinline__ void sag_derivs(const float* m, double rho, SagD& o) {
   const double c = m[15], k = m[23];
   const double al = (1.0 + k) * c * c;
-  const double q = sqrt(1.0 - al * rho);
-  const double q3 = q * q * q, opq = 1.0 + q;
-  o.S = c * rho / opq;
-  o.Sr = c / (2.0 * q);
-  o.Srr = c * al / (4.0 * q3);
-  o.Sc = rho / opq + (1.0 + k) * c * c * rho * rho / (q * opq * opq);
-  o.Sk = c * c * c * rho * rho / (2.0 * q * opq * opq);
-  o.Src = 1.0 / (2.0 * q) + (1.0 + k) * c * c * rho / (2.0 * q3);
-  o.Srk = c * c * c * rho / (4.0 * q3);
+  const double qq = fma(-al, rho, 1.0);
+  // one reciprocal square root and one reciprocal (Newton-refined, FP64)
+  // replace the square root and the divisions of the closed forms
+  const double iq = qq > 0.0 ? rsqrt_d(qq) : (qq == 0.0 ? __longlong_as_double(0x7ff0000000000000ll)
+                                                       : __longlong_as_double(0x7ff8000000000000ll));
+  const double q = qq > 0.0 ? qq * iq : (qq == 0.0 ? 0.0 : iq);
+  const double iq3 = iq * iq * iq, iopq = rcp_d(1.0 + q), iopq2 = iopq * iopq;
+  o.S = c * rho * iopq;
+  o.Sr = 0.5 * c * iq;
+  o.Srr = 0.25 * c * al * iq3;
+  o.Sc = rho * iopq + al * rho * rho * iq * iopq2;
+  o.Sk = 0.5 * c * c * c * rho * rho * iq * iopq2;
+  o.Src = 0.5 * iq + 0.5 * al * rho * iq3;
+  o.Srk = 0.25 * c * c * c * rho * iq3;
   const int na = (int)m[19];
   for (int i = 0; i < 8; ++i) {
     o.Sa[i] = 0.0;

@@ -54,8 +54,9 @@ SensorK make_sensor(const iact_sensor_t* s);
 
 // Work-tile shape (sources x facets x 32-sample chunks) for a block of
 // `block` threads: fills p.SB, FC, CC, n_fchunk, n_cchunk, n_tiles from
-// p.F, p.M, p.S and the opts knobs.
-int plan_tiles(RenderK& p, int mode, int block, const iact_opts_t* opts);
+// p.F, p.M, p.S and the opts knobs; without explicit knobs the tile shrinks
+// (down to one task per warp) until there are at least `min_tiles`.
+int plan_tiles(RenderK& p, int mode, int block, const iact_opts_t* opts, long long min_tiles);
 // Shared-memory plan of one render: tables, int16 hex lookup table (if it
 // fits in half the budget) and FP32 histogram rows (if they fit). Floors let
 // a batch reserve the largest table sizes of all its jobs.

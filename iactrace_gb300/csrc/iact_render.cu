@@ -324,7 +324,7 @@ WsLayout workspace_for(const iact_scene_t* sc, const iact_sensor_t* sn, int S, i
   return workspace_layout(sc, acc_elems(sn, S, mode), false);
 }
 
-int plan_tiles(RenderK& p, int mode, int block, const iact_opts_t* opts) {
+int plan_tiles(RenderK& p, int mode, int block, const iact_opts_t* opts, long long min_tiles) {
   const int nw = block / 32;
   const int nch = (p.M + 31) / 32;
   const int S = p.S;
@@ -333,19 +333,25 @@ int plan_tiles(RenderK& p, int mode, int block, const iact_opts_t* opts) {
   int SB = (opts && opts->sources_per_cta > 0) ? opts->sources_per_cta
                                                : std::min(S, mode == IACT_MODE_RESPONSE ? std::max(1, nw / 2) : nw);
   SB = std::max(1, std::min(SB, S));
+  const bool fixed = opts && (opts->tasks_per_warp > 0 || opts->facets_per_tile > 0);
   const int tpw = (opts && opts->tasks_per_warp > 0) ? opts->tasks_per_warp : 48;
   // warp tasks (32 rays each) per tile; candidate masks stay within 16 KiB
-  const int target = std::max(1, std::min(nw * tpw, p.n_words ? 4096 / p.n_words : 1 << 30));
-  int CC = std::max(1, std::min(nch, std::max(1, target / SB)));
-  int FC = (opts && opts->facets_per_tile > 0) ? opts->facets_per_tile : std::max(1, target / (SB * CC));
-  FC = std::max(1, std::min(FC, p.F));
-  p.SB = SB; p.FC = FC; p.CC = CC;
-  p.n_fchunk = (p.F + FC - 1) / FC;
-  p.n_cchunk = (nch + CC - 1) / CC;
-  const long long tiles =
-      (S > 0 && p.F > 0 && p.M > 0) ? (long long)((S + SB - 1) / SB) * p.n_fchunk * p.n_cchunk : 0;
-  if (tiles > 0x7fffffffLL) return set_error(IACT_E_UNSUPPORTED, "too many work tiles");
-  p.n_tiles = (int)tiles;
+  int target = std::max(1, std::min(nw * tpw, p.n_words ? 4096 / p.n_words : 1 << 30));
+  for (;;) {
+    const int CC = std::max(1, std::min(nch, std::max(1, target / SB)));
+    int FC = (opts && opts->facets_per_tile > 0) ? opts->facets_per_tile : std::max(1, target / (SB * CC));
+    FC = std::max(1, std::min(FC, p.F));
+    p.SB = SB; p.FC = FC; p.CC = CC;
+    p.n_fchunk = (p.F + FC - 1) / FC;
+    p.n_cchunk = (nch + CC - 1) / CC;
+    const long long tiles =
+        (S > 0 && p.F > 0 && p.M > 0) ? (long long)((S + SB - 1) / SB) * p.n_fchunk * p.n_cchunk : 0;
+    if (tiles > 0x7fffffffLL) return set_error(IACT_E_UNSUPPORTED, "too many work tiles");
+    p.n_tiles = (int)tiles;
+    // small launches: halve the tile until the GPU holds enough of them to balance
+    if (fixed || tiles == 0 || tiles >= min_tiles || target <= nw) break;
+    target = std::max(nw, target / 2);
+  }
   return IACT_OK;
 }
 
@@ -392,9 +398,9 @@ int launch_render(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type,
   if (opts && (opts->flags & IACT_FLAG_NO_CULL)) p.n_words = 0;
   int block = (opts && opts->block_threads > 0) ? opts->block_threads : 256;
   if (block % 32 || block > 256) return set_error(IACT_E_INVALID, "opts.block_threads must be a multiple of 32, <= 256");
-  rc = plan_tiles(p, mode, block, opts);
-  if (rc) return rc;
   DevInfo di = device_info();
+  rc = plan_tiles(p, mode, block, opts, 8LL * std::max(di.sm_count, 1));
+  if (rc) return rc;
   const size_t mask_bytes = sizeof(uint32_t) * (size_t)p.n_words * p.SB * p.FC * p.CC;
   const size_t budget = (size_t)std::min(di.smem_optin > 0 ? di.smem_optin : 49152, 200 * 1024) - mask_bytes;
   SmemPlan sp;

@@ -136,6 +136,9 @@ typedef struct {
  * bounding volume comes near the rays' common bundle (exact: identical
  * shadow masks); this flag tests every primitive on every ray instead. */
 #define IACT_FLAG_NO_CULL 1
+/* iact_batch_create: also plan iact_batch_backward (workspace for the
+ * gradient buckets of every job) */
+#define IACT_FLAG_BATCH_BACKWARD 2
 
 /* Optional launch knobs; NULL or zeros select the built-in defaults. */
 typedef struct {
@@ -251,6 +254,18 @@ typedef struct {
   int32_t n_sources;
   uint32_t seed;               /* jitter stream of EXTENDED sources         */
   float* out;                  /* device [P] (IMAGE) or [S,P] (RESPONSE)    */
+  /* iact_batch_backward only (batches created with IACT_FLAG_BATCH_BACKWARD):
+   * dL/d(out) in, gradients out as in iact_render_backward; outputs may be
+   * NULL */
+  const float* grad_out;
+  float* g_facet_rot;
+  float* g_facet_pos;
+  float* g_facet_scale;
+  float* g_sources;
+  float* g_values;
+  float* g_mirror_rot;
+  float* g_mirror_pos;
+  float* g_mirror_surface;
 } iact_job_t;
 
 typedef struct iact_batch iact_batch;
@@ -272,8 +287,15 @@ int iact_batch_prepare(iact_batch* batch, void* workspace, size_t workspace_byte
  * captured in a CUDA graph and replayed. Job arrays (samples, facet
  * parameters, sources, values) are read when the kernels run. */
 int iact_batch_render(iact_batch* batch, void* stream);
+/* Adjoint of iact_batch_render for every job of a batch created with
+ * IACT_FLAG_BATCH_BACKWARD: reads each job's grad_out, writes its gradient
+ * outputs (as iact_render_backward, same limits). Recomputes the forward
+ * paths; one persistent launch per template class over all jobs' adjoint
+ * tiles; capture-safe like iact_batch_render. */
+int iact_batch_backward(iact_batch* batch, void* stream);
 /* out[0] jobs, out[1] work tiles, out[2] rays, out[3] kernel launches per
- * iact_batch_render, out[4] template classes used */
+ * iact_batch_render, out[4] template classes used, out[5] adjoint tiles,
+ * out[6] kernel launches per iact_batch_backward */
 int iact_batch_info(const iact_batch* batch, int64_t* out, int32_t n);
 void iact_batch_destroy(iact_batch* batch);
 

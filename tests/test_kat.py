@@ -94,7 +94,9 @@ def test_kat_flux_and_focus(kind, request):
     v = 2.0
     img = _image(kind, tel, BEAM, torch.tensor([v]), "parallel").reshape(11, 11)
     total = v * math.pi * R_AP ** 2
-    tol = 1e-7 if kind == "oracle" else 2e-6  # the samples and weights are float32 inputs
+    # oracle: float32 inputs (samples, weights); GPU: plus float32 shared-memory
+    # sums of 4000 equal rays into one pixel (the image tolerance, 1e-5)
+    tol = 1e-7 if kind == "oracle" else 1e-5
     assert abs(img[5, 5] - total) <= tol * total, (img[5, 5], total)
     img[5, 5] = 0.0
     assert np.all(img == 0.0)

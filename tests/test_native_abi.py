@@ -115,7 +115,28 @@ def test_batch_planner_without_a_gpu(built):
     assert size.value >= (100 * 256 + 37 * 64 + 5 * 33) * 32 + 3 * 64 * 8
     assert built.iact_batch_render(h, None) == N.IACT_E_INVALID  # not prepared: nothing queued
     assert b"prepare" in built.iact_last_error()
+    assert built.iact_batch_backward(h, None) == N.IACT_E_INVALID  # created without the backward flag
     built.iact_batch_destroy(h)
+    # with the backward plan: every non-empty job needs dL/d(out)
+    opts = N.IactOpts()
+    opts.flags = N.FLAG_BATCH_BACKWARD
+    assert built.iact_batch_create(jobs, 3, N.SRC_POINT, N.MODE_IMAGE, ctypes.byref(opts),
+                                   ctypes.byref(h)) == N.IACT_E_INVALID
+    assert b"grad_out" in built.iact_last_error()
+    for i in range(3):
+        jobs[i].grad_out = 0x40000
+        jobs[i].g_facet_rot = 0x50000
+    assert built.iact_batch_create(jobs, 3, N.SRC_POINT, N.MODE_IMAGE, ctypes.byref(opts), ctypes.byref(h)) == 0
+    info7 = (ctypes.c_int64 * 7)()
+    assert built.iact_batch_info(h, info7, 7) == N.IACT_OK
+    assert info7[5] > 0 and info7[6] == 3  # prep + one adjoint class + finish
+    size_b = ctypes.c_size_t(0)
+    assert built.iact_batch_workspace_size(h, ctypes.byref(size_b)) == N.IACT_OK
+    assert size_b.value > size.value  # + roughness deltas and gradient buckets
+    built.iact_batch_destroy(h)
+    for i in range(3):
+        jobs[i].grad_out = None
+        jobs[i].g_facet_rot = None
     # rejected jobs
     jobs[1].out = None
     assert built.iact_batch_create(jobs, 3, N.SRC_POINT, N.MODE_IMAGE, None, ctypes.byref(h)) == N.IACT_E_INVALID
