@@ -341,7 +341,7 @@ def run_batched(args, rank, world):
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
     torch.cuda.set_device(dev)
     N.load(build_if_missing=True)
-    tels, srcs_h, vals_h, st = W.ragged_batch()
+    tels, srcs_h, vals_h, st = W.ragged_batch(n_instances=args.instances, max_sources=args.max_sources)
     srcs = [s.to(dev) for s in srcs_h]
     vals = [v.to(dev) for v in vals_h]
     F = [len(t.mirror_groups[0]) for t in tels]
@@ -351,7 +351,7 @@ def run_batched(args, rank, world):
     stream = torch.cuda.current_stream(dev)
     flush_buf = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     t0 = time.perf_counter()
-    b = it.BatchRenderer(tels, srcs, vals, st, tune=True)
+    b = it.BatchRenderer(tels, srcs, vals, st, tune=not args.no_tune)
     setup_s = time.perf_counter() - t0
     tune = AT.last_result(b)
     info = b.info()
@@ -479,7 +479,7 @@ def run_batched(args, rank, world):
         "unit": "rays/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": batch_s * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded Davies-Cotton variants and sources)",
-        "config": {"workload": "ragged_batch_64_dc_variants_hex960_2048", "instances": len(tels),
+        "config": {"workload": f"ragged_batch_{len(tels)}_dc_variants_hex960_2048", "instances": len(tels),
                    "facets_min_max": [min(F), max(F)], "sources_min_max": [min(S), max(S)],
                    "samples_per_facet": M, "rays_per_step": rays, "output": "64 images fp32",
                    "l2": "flushed before each step (256 MiB write)"},
@@ -526,6 +526,9 @@ def main():
     ap.add_argument("--workload", default="response",
                     choices=["response", "plain", "cassegrain", "alignment", "batched"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--instances", type=int, default=64, help="batched workload: telescope variants")
+    ap.add_argument("--max-sources", type=int, default=4096, help="batched workload: largest source count")
+    ap.add_argument("--no-tune", action="store_true", help="batched workload: library defaults, no autotuner")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = _env_rank()

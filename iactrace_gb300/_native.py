@@ -101,6 +101,13 @@ class IactJob(ctypes.Structure):
                 ("g_mirror_pos", ctypes.c_void_p), ("g_mirror_surface", ctypes.c_void_p)]
 
 
+class IactSampler(ctypes.Structure):
+    _fields_ = [("n_facets", _i), ("n_samples", _i), ("aperture", _i), ("n_vert", _i),
+                ("curvature", _f), ("conic", _f), ("n_asph", _i), ("asph", _f * IACT_MAX_ASPH),
+                ("offsets", ctypes.c_void_p), ("radii", ctypes.c_void_p), ("vertices", ctypes.c_void_p),
+                ("seed", ctypes.c_uint32)]
+
+
 class IactError(RuntimeError):
     def __init__(self, code: int, msg: str):
         super().__init__(f"iactrace_gb300 error {code}: {msg}")
@@ -136,6 +143,8 @@ _SIGS = {
     "iact_batch_backward": ([ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
     "iact_batch_info": ([ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64), _i], ctypes.c_int),
     "iact_batch_destroy": ([ctypes.c_void_p], None),
+    "iact_sample_facets": ([ctypes.POINTER(IactSampler), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                            ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
 }
 
 # symbols declared by include/iactrace_gb300.h that bindings resolve

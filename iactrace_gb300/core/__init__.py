@@ -1,6 +1,6 @@
 from .apertures import Aperture, DiskAperture, PolygonAperture
 from .batch import BatchRenderer
-from .integrators import Integrator, MCIntegrator
+from .integrators import DeviceIntegrator, Integrator, MCIntegrator
 from .obstructions import (Box, BoxGroup, Cylinder, CylinderGroup, Obstruction, ObstructionGroup, OrientedBox,
                            OrientedBoxGroup, Sphere, SphereGroup, Triangle, TriangleGroup, group_obstructions)
 from .reflection import compute_perturbation_delta, reflect
@@ -9,7 +9,7 @@ from .surfaces import AsphericSurface
 from .transforms import euler_to_matrix, look_at_euler, look_at_rotation
 
 __all__ = [
-    "AsphericSurface", "Aperture", "DiskAperture", "PolygonAperture", "Integrator", "MCIntegrator",
+    "AsphericSurface", "Aperture", "DiskAperture", "PolygonAperture", "Integrator", "MCIntegrator", "DeviceIntegrator",
     "compute_perturbation_delta", "reflect", "euler_to_matrix", "look_at_rotation", "look_at_euler",
     "render", "render_debug", "render_response_matrix", "BatchRenderer",
     "Obstruction", "ObstructionGroup", "Cylinder", "CylinderGroup", "Box", "BoxGroup", "Sphere", "SphereGroup",

@@ -2,15 +2,20 @@
 
 ``MCIntegrator.sample_group`` fills a stage-0 mirror group with local sample
 points, unit normals, unit-sigma roughness deltas and weights
-``cos_z / area * n_samples`` (core/integrators.py:97-187).
+``cos_z / area * n_samples`` (core/integrators.py:97-187), on the host.
+``DeviceIntegrator`` draws the same distribution on the GPU
+(``iact_sample_facets``): counter-based Philox variates keyed by (seed,
+facet, sample), FP64 arithmetic, float32 arrays left on the device.
 """
 from __future__ import annotations
 
+import ctypes
 import math
 from abc import ABC, abstractmethod
 
 import torch
 
+from .. import _native as N
 from ..utils import keys as _keys
 from ..utils.sampling import sample_disk, sample_polygon
 from .reflection import compute_perturbation_delta
@@ -68,3 +73,57 @@ class MCIntegrator(Integrator):
         x, y = verts[..., 0], verts[..., 1]
         area = 0.5 * torch.abs(torch.sum(x * torch.roll(y, -1, -1) - torch.roll(x, -1, -1) * y, -1))
         return self._finish(group, params["surface"], xy, params["offsets"].double(), area, gen)
+
+
+def sampler_desc(group, key, n_samples: int, device):
+    """The iact_sampler_t of a stage-0 group and its arrays on `device`
+    (returns the descriptor and the tensors it points at)."""
+    params = group.get_sampling_params()
+    surf = params["surface"]
+    d = N.IactSampler()
+    d.n_facets, d.n_samples = len(group), int(n_samples)
+    d.curvature, d.conic = float(surf.curvature), float(surf.conic)
+    a = surf.aspheric.reshape(-1).tolist()
+    if len(a) > N.IACT_MAX_ASPH:
+        raise ValueError(f"at most {N.IACT_MAX_ASPH} aspheric coefficients")
+    d.n_asph = len(a)
+    for i, v in enumerate(a):
+        d.asph[i] = float(v)
+    keep = [params["offsets"].reshape(-1, 2).to(device=device, dtype=torch.float32).contiguous()]
+    d.offsets = keep[0].data_ptr()
+    if params["type"] == "disk":
+        d.aperture = N.APERTURE_DISK
+        keep.append(params["radii"].reshape(-1).to(device=device, dtype=torch.float32).contiguous())
+        d.radii = keep[-1].data_ptr()
+    else:
+        d.aperture = N.APERTURE_POLYGON
+        v = params["vertices"].to(device=device, dtype=torch.float32).contiguous()
+        if v.shape[1] > N.IACT_MAX_POLY:
+            raise ValueError(f"polygon apertures have at most {N.IACT_MAX_POLY} vertices")
+        d.n_vert = int(v.shape[1])
+        keep.append(v)
+        d.vertices = v.data_ptr()
+    d.seed = _keys.as_key(key).value & 0xFFFFFFFF
+    return d, keep
+
+
+class DeviceIntegrator(Integrator):
+    """MCIntegrator on the GPU: same aperture, surface, roughness-delta and
+    weight construction (core/integrators.py:97-187), variates from the
+    counter-based stream of iact_sample_facets (reproducible on any host)."""
+
+    def __init__(self, n_samples: int = 128, device=None):
+        self.n_samples = int(n_samples)
+        self.device = device
+
+    def sample_group(self, group, key):
+        dev = torch.device(self.device) if self.device is not None else torch.device("cuda", torch.cuda.current_device())
+        d, keep = sampler_desc(group, key, self.n_samples, dev)
+        F, M = len(group), self.n_samples
+        pts, nrm, dlt = (torch.empty((F, M, 3), device=dev) for _ in range(3))
+        w = torch.empty((F, M, 1), device=dev)
+        lib = N.load()
+        N.check(lib.iact_sample_facets(ctypes.byref(d), pts.data_ptr(), nrm.data_ptr(), dlt.data_ptr(), w.data_ptr(),
+                                       torch.cuda.current_stream(dev).cuda_stream))
+        del keep
+        return group.with_samples(pts, nrm, dlt, w)

@@ -29,6 +29,8 @@
  *                             (no dedicated reference function)
  *   iact_batch_*           <- a Python loop (or jax.vmap) of Telescope.__call__
  *                             over telescope variants (no reference function)
+ *   iact_sample_facets     <- core/integrators.py:97-187 MCIntegrator.sample_group
+ *                             (counter-based streams instead of threefry)
  */
 #ifndef IACTRACE_GB300_H
 #define IACTRACE_GB300_H
@@ -298,6 +300,33 @@ int iact_batch_backward(iact_batch* batch, void* stream);
  * out[6] kernel launches per iact_batch_backward */
 int iact_batch_info(const iact_batch* batch, int64_t* out, int32_t n);
 void iact_batch_destroy(iact_batch* batch);
+
+/* ---- Monte-Carlo facet sampling on the device -----------------------------
+ * One stage-0 mirror group (shared aspheric surface, per-facet disk radius or
+ * convex polygon and offset) sampled as core/integrators.py:97-187
+ * MCIntegrator.sample_group does: uniform points on the aperture
+ * (utils/sampling.py:8-67: r = sqrt(u) disk, or an area-weighted fan
+ * triangle of the polygon), lifted to the surface (core/surfaces.py:41-65),
+ * unit normals, unit-sigma roughness deltas in the tangent plane
+ * (core/reflection.py:22-49) and weights cos_z / area * n_samples. The
+ * variates come from Philox4x32-10 keyed by (seed, facet, sample), so any
+ * host can replay them; the arithmetic is FP64, stored as float32. */
+typedef struct {
+  int32_t n_facets, n_samples;
+  int32_t aperture;           /* IACT_APERTURE_DISK or IACT_APERTURE_POLYGON */
+  int32_t n_vert;             /* polygon vertices, 3..IACT_MAX_POLY          */
+  float curvature, conic;
+  int32_t n_asph;
+  float asph[IACT_MAX_ASPH];
+  const float* offsets;       /* device [F,2]                                */
+  const float* radii;         /* device [F] (disk)                           */
+  const float* vertices;      /* device [F, n_vert, 2] (polygon, convex)     */
+  uint32_t seed;
+} iact_sampler_t;
+
+/* points, normals, delta: device [F, M, 3]; weights: device [F, M] */
+int iact_sample_facets(const iact_sampler_t* sampler, float* points, float* normals,
+                       float* delta, float* weights, void* stream);
 
 #ifdef __cplusplus
 }

@@ -48,6 +48,8 @@ def load():
             getattr(lib, name).argtypes = [vp, vp, i, vp, vp, i, vp, vp, vp, vp, vp, u]
             getattr(lib, name).restype = i
         lib.oracle_transform_f64.argtypes = [vp, vp, vp, vp]
+        lib.oracle_sample_facets.argtypes = [vp, vp, vp, vp, vp]
+        lib.oracle_sample_facets.restype = i
         lib.oracle_max_threads.restype = i
         _lib = lib
     return _lib
@@ -117,3 +119,17 @@ def render_debug(tel, sources, values, source_type="point", sensor_idx=0, dtype=
 
 def max_threads() -> int:
     return int(load().oracle_max_threads())
+
+
+def sample_facets(sampler_desc, F: int, M: int):
+    """Replay of iact_sample_facets on host arrays (the descriptor's array
+    pointers must be host pointers): points, normals, delta [F, M, 3] and
+    weights [F, M], float64."""
+    lib = load()
+    pts, nrm, dlt = (np.zeros((F, M, 3)) for _ in range(3))
+    wts = np.zeros((F, M))
+    rc = lib.oracle_sample_facets(ctypes.addressof(sampler_desc), pts.ctypes.data, nrm.ctypes.data,
+                                  dlt.ctypes.data, wts.ctypes.data)
+    if rc:
+        raise RuntimeError(f"oracle_sample_facets failed ({rc})")
+    return pts, nrm, dlt, wts

@@ -1,0 +1,127 @@
+"""On-device Monte-Carlo facet sampling (iact_sample_facets, DeviceIntegrator).
+
+* replay: the FP64 oracle (oracle_sample_facets) replays the same
+  counter-based variates; the device arrays equal it to float32 rounding;
+* distribution: the samples follow MCIntegrator's (the reference's)
+  distribution: uniform on the disk / polygon, normals of the surface,
+  unit-normal roughness coefficients, weights cos_z / area * n_samples;
+* use: a render of device-sampled facets agrees with the same render of
+  host-sampled facets within Monte-Carlo noise.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+import pytest
+import torch
+
+import iactrace_gb300 as it
+from iactrace_gb300 import Mirror, Telescope, workloads as W
+from iactrace_gb300.core import AsphericSurface, DiskAperture, PolygonAperture
+from iactrace_gb300.core.integrators import sampler_desc
+from iactrace_gb300.telescope.mirrors import group_mirrors
+
+
+
+
+def _groups():
+    surf = AsphericSurface(0.05, -1.05, [1e-4, -2e-6])
+    disk = [Mirror([x, y, 0.0], [0.0, 0.0, 0.0], surf, DiskAperture(r), optical_stage=0, offset=[x, y])
+            for x, y, r in ((0.0, 0.0, 0.6), (1.2, 0.3, 0.5), (-2.0, 1.5, 0.45))]
+    hexv = W.hex_vertices(0.9)
+    poly = [Mirror([x, y, 0.0], [0.0, 0.0, 0.0], surf, PolygonAperture(hexv), optical_stage=0, offset=[x, y])
+            for x, y in W.hex_grid(7, 0.92)]
+    return group_mirrors(disk)[0], group_mirrors(poly)[0]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("which", [0, 1])
+def test_device_samples_replay_on_the_oracle(cuda, which):
+    import oracle.oracle as O
+    g = _groups()[which]
+    M = 2048
+    dev = it.DeviceIntegrator(M).sample_group(g, 7)
+    d, keep = sampler_desc(g, 7, M, "cpu")
+    pts, nrm, dlt, wts = O.sample_facets(d, len(g), M)
+    del keep
+    assert np.abs(dev.points.cpu().double().numpy() - pts).max() < 1e-6
+    assert np.abs(dev.normals.cpu().double().numpy() - nrm).max() < 1e-6
+    assert np.abs(dev.perturbation_delta.cpu().double().numpy() - dlt).max() < 2e-5  # |delta| up to ~6
+    assert np.abs(dev.weights.cpu().double().numpy()[..., 0] / wts - 1).max() < 1e-6
+
+
+@pytest.mark.gpu
+def test_device_samples_distribution(cuda):
+    disk, poly = _groups()
+    M = 20000
+    d = it.DeviceIntegrator(M).sample_group(disk, 11)
+    xy = d.points[..., :2].cpu().double().numpy()
+    for f, R in enumerate((0.6, 0.5, 0.45)):
+        r2 = (xy[f] ** 2).sum(-1) / R ** 2
+        assert r2.max() <= 1.0 + 1e-6
+        assert abs(r2.mean() - 0.5) < 0.01  # uniform on the disk: E[r^2] = R^2 / 2
+        ang = np.arctan2(xy[f, :, 1], xy[f, :, 0])
+        hist = np.histogram(ang, bins=8, range=(-math.pi, math.pi))[0] / M
+        assert np.abs(hist - 1 / 8).max() < 0.01
+    dl = d.perturbation_delta.cpu().double().numpy().reshape(-1, 3)
+    n = d.normals.cpu().double().numpy().reshape(-1, 3)
+    assert np.abs((dl * n).sum(-1)).max() < 1e-5  # tangent to the surface
+    th2 = (dl ** 2).sum(-1)  # theta1^2 + theta2^2 ~ chi2(2): mean 2
+    assert abs(th2.mean() - 2.0) < 0.05
+    # weights: cos_z / (pi R^2) * M, so sum over a facet's samples of 1/w * n_z = area
+    w = d.weights.cpu().double().numpy()[..., 0]
+    for f, R in enumerate((0.6, 0.5, 0.45)):
+        assert np.allclose(n.reshape(3, M, 3)[f, :, 2] / w[f] * M, math.pi * R ** 2, rtol=1e-6)
+    # polygon: uniform over the hexagon (each of the 4 fan triangles gets its area share)
+    p = it.DeviceIntegrator(M).sample_group(poly, 12)
+    xy = p.points[0, :, :2].cpu().double().numpy()
+    v = np.array(W.hex_vertices(0.9))
+    cnt = np.zeros(4)
+    for t in range(4):
+        a, b, c = v[0], v[t + 1], v[t + 2]
+        den = (b[1] - c[1]) * (a[0] - c[0]) + (c[0] - b[0]) * (a[1] - c[1])
+        l1 = ((b[1] - c[1]) * (xy[:, 0] - c[0]) + (c[0] - b[0]) * (xy[:, 1] - c[1])) / den
+        l2 = ((c[1] - a[1]) * (xy[:, 0] - c[0]) + (a[0] - c[0]) * (xy[:, 1] - c[1])) / den
+        cnt[t] = ((l1 >= -1e-9) & (l2 >= -1e-9) & (1 - l1 - l2 >= -1e-9)).sum()
+    assert cnt.sum() >= M - 5
+    assert np.allclose(cnt / M, [1 / 6, 1 / 3, 1 / 3, 1 / 6], atol=0.012)
+
+
+@pytest.mark.gpu
+def test_render_with_device_sampled_facets(cuda):
+    groups, obst = W.davies_cotton(n_samples=4, seed=3)
+    g = groups[0]
+    host = it.MCIntegrator(512).sample_group(g, 5)
+    devg = it.DeviceIntegrator(512).sample_group(g, 5)
+    cam = W.hex_camera(960)
+    src = W.point_sources_disk(8, 2.0, 4)
+    val = torch.ones(8)
+    a = it.render(Telescope([host], obst, [cam]), src, val, "point").double()
+    b = it.render(Telescope([devg], obst, [cam]), src, val, "point").double()
+    # same total flux and image within Monte-Carlo noise (2 x 194560 rays per image)
+    assert abs(float(a.sum() / b.sum()) - 1) < 0.01
+    assert float((a - b).norm() / a.norm()) < 0.05
+
+
+@pytest.mark.parametrize("which", [0, 1])
+def test_oracle_sampler_distribution_on_cpu(built, which):
+    """The checker itself (CPU replay) follows the integrator's distribution."""
+    import oracle.oracle as O
+    g = _groups()[which]
+    M = 20000
+    d, keep = sampler_desc(g, 3, M, "cpu")
+    pts, nrm, dlt, wts = O.sample_facets(d, len(g), M)
+    del keep
+    # the surface: z = sag(x + ox, y + oy) - sag(ox, oy), normal ~ (-dz/dx, -dz/dy, 1)
+    surf = g.get_surface()
+    off = g.offsets.double().numpy()
+    for f in range(len(g)):
+        x = torch.as_tensor(pts[f, :50, 0]); y = torch.as_tensor(pts[f, :50, 1])
+        z = surf.sag(x, y, torch.as_tensor(off[f])).numpy()
+        assert np.abs(z - pts[f, :50, 2]).max() < 1e-9  # descriptor carries float32 surface constants
+    assert np.abs(np.linalg.norm(nrm, axis=-1) - 1).max() < 1e-12
+    assert abs((dlt ** 2).sum(-1).mean() - 2.0) < 0.05
+    if which == 0:
+        r2 = (pts[0, :, :2] ** 2).sum(-1) / 0.6 ** 2
+        assert abs(r2.mean() - 0.5) < 0.01 and r2.max() <= 1.0
