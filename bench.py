@@ -156,7 +156,7 @@ def adjoint_kernel_seconds(tel, src, val, stype, mode, gout, flush_buf, steps):
         N.check(lib.iact_render_backward(ctypes.byref(ps.desc), ctypes.byref(sdesc), code, src.data_ptr(),
                                          val.data_ptr(), S, nm, gout.data_ptr(), g[0].data_ptr(), g[1].data_ptr(),
                                          None, None if no_src else g[2].data_ptr(), g[3].data_ptr(), None, None,
-                                         None, ws.data_ptr(), ws.numel(), ctypes.byref(o), stream.cuda_stream))
+                                         None, None, ws.data_ptr(), ws.numel(), ctypes.byref(o), stream.cuda_stream))
 
     call()
     tot = 0.0

@@ -18,7 +18,7 @@ import torch
 from .. import _native as N
 from ..utils import keys as _keys
 from ..utils.sampling import sample_disk, sample_polygon
-from .reflection import compute_perturbation_delta
+from .reflection import compute_perturbation_delta, perturbation_delta_from_normals
 
 
 class Integrator(ABC):
@@ -82,8 +82,9 @@ def sampler_desc(group, key, n_samples: int, device):
     surf = params["surface"]
     d = N.IactSampler()
     d.n_facets, d.n_samples = len(group), int(n_samples)
-    d.curvature, d.conic = float(surf.curvature), float(surf.conic)
-    a = surf.aspheric.reshape(-1).tolist()
+    value = lambda x: float(x.detach()) if isinstance(x, torch.Tensor) else float(x)
+    d.curvature, d.conic = value(surf.curvature), value(surf.conic)
+    a = surf.aspheric.detach().reshape(-1).tolist()
     if len(a) > N.IACT_MAX_ASPH:
         raise ValueError(f"at most {N.IACT_MAX_ASPH} aspheric coefficients")
     d.n_asph = len(a)
@@ -126,4 +127,36 @@ class DeviceIntegrator(Integrator):
         N.check(lib.iact_sample_facets(ctypes.byref(d), pts.data_ptr(), nrm.data_ptr(), dlt.data_ptr(), w.data_ptr(),
                                        torch.cuda.current_stream(dev).cuda_stream))
         del keep
+        surf = group.get_surface()
+        params = [surf.curvature, surf.conic, surf.aspheric]
+        if any(isinstance(t, torch.Tensor) and t.requires_grad for t in params):
+            pts, nrm, dlt, w = self._differentiable(group, surf, pts, nrm, dlt, w)
         return group.with_samples(pts, nrm, dlt, w)
+
+    def _differentiable(self, group, surf, pts, nrm, dlt, w):
+        """The sample arrays as functions of the surface parameters (FP64
+        torch restatement of the kernel's mapping, core/surfaces.py:41-65 and
+        core/reflection.py:22-49): the aperture positions and the roughness
+        coefficients do not depend on the surface; points, normals, deltas
+        and weights do (resampling gradients)."""
+        dev = pts.device
+        xy = pts[..., :2].double()
+        n0 = nrm.double()
+        # the roughness coefficients of the drawn deltas in their tangent basis
+        ref_z = torch.tensor([0.0, 0.0, 1.0], dtype=torch.float64, device=dev)
+        ref_x = torch.tensor([1.0, 0.0, 0.0], dtype=torch.float64, device=dev)
+        ref = torch.where(n0[..., 2:3].abs() > 0.9, ref_x, ref_z)
+        t1 = torch.linalg.cross(n0, ref.expand_as(n0))
+        t1 = t1 / torch.linalg.norm(t1, dim=-1, keepdim=True)
+        t2 = torch.linalg.cross(n0, t1)
+        d0 = dlt.double()
+        th1, th2 = (d0 * t1).sum(-1), (d0 * t2).sum(-1)
+        s64 = type(surf)(surf.curvature if not isinstance(surf.curvature, torch.Tensor) else surf.curvature.double(),
+                         surf.conic if not isinstance(surf.conic, torch.Tensor) else surf.conic.double(),
+                         surf.aspheric.double())
+        off = group.offsets.reshape(-1, 1, 2).to(device=dev, dtype=torch.float64)
+        p, n = s64.point_and_normal(xy, off)
+        dl = perturbation_delta_from_normals(n, th1, th2)
+        area = (n0[..., 2] / w[..., 0].double() * self.n_samples).detach()  # per facet: pi R^2 or polygon area
+        ww = n[..., 2:3] / area[..., None] * self.n_samples
+        return p.float(), n.float(), dl.float(), ww.float()

@@ -13,8 +13,8 @@ def reflect(d, n):
 def perturbation_delta_from_normals(normals, theta1, theta2):
     """core/reflection.py:22-49 with the two N(0,1) draws given: tangent basis
     from cross(n, ref) with ref = x if |n_z| > 0.9 else z."""
-    ref_z = torch.tensor([0.0, 0.0, 1.0], dtype=normals.dtype)
-    ref_x = torch.tensor([1.0, 0.0, 0.0], dtype=normals.dtype)
+    ref_z = torch.tensor([0.0, 0.0, 1.0], dtype=normals.dtype, device=normals.device)
+    ref_x = torch.tensor([1.0, 0.0, 0.0], dtype=normals.dtype, device=normals.device)
     dot_z = torch.abs(torch.sum(normals * ref_z, dim=-1, keepdim=True))
     ref = torch.where(dot_z > 0.9, ref_x, ref_z)
     t1 = torch.linalg.cross(normals, ref.expand_as(normals))

@@ -67,17 +67,38 @@ def _desc_with(ps, rot, pos, scale):
     return d
 
 
+def _sample_grads(gs, rot, scale, nrm, dlt, wts):
+    """Local-frame gradients of the primary sample arrays from the adjoint's
+    per-sample world sums gs [F, M, 7] = (dL/dp_world, dL/dn'_world,
+    dL/d(1/w)): p_world = R p + pos; n' = R m / |m|, m = n + s delta
+    (telescope/mirrors.py:64-79); value = v (-c) / w."""
+    from .transforms import euler_to_matrix
+    g = gs.double()
+    R = euler_to_matrix(rot.double())  # (F, 3, 3)
+    a, b, giw = g[..., 0:3], g[..., 3:6], g[..., 6]
+    gp = torch.einsum("fji,fmj->fmi", R, a)  # R^T a
+    bl = torch.einsum("fji,fmj->fmi", R, b)
+    m = nrm.double() + scale.double()[:, None, None] * dlt.double()
+    mn = torch.linalg.norm(m, dim=-1, keepdim=True)
+    u = m / mn
+    gm = (bl - (bl * u).sum(-1, keepdim=True) * u) / mn
+    w = wts.double()
+    return gp, gm, scale.double()[:, None, None] * gm, -giw / (w * w)
+
+
 class RenderFunction(torch.autograd.Function):
     """iact_render forward, iact_render_backward (recompute-based adjoint) backward.
 
     Differentiable inputs: concatenated stage-0 facet rotations (F,3, degrees),
-    positions (F,3), perturbation scales (F,), sources (S,3), values (S,), and
+    positions (F,3), perturbation scales (F,), sources (S,3), values (S,),
     per stage mirror rotations (n,3), positions (n,3) and surface parameters
-    (n, 10: curvature, conic, 8 aspheric coefficients).
+    (n, 10: curvature, conic, 8 aspheric coefficients), and the primary sample
+    arrays (points, normals, deltas (F,M,3), weights (F,M)) when they carry
+    gradients (resampled with differentiable surface parameters).
     """
 
     @staticmethod
-    def forward(ctx, meta, rot, pos, scale, src, val, mrot, mpos, msurf):
+    def forward(ctx, meta, rot, pos, scale, src, val, mrot, mpos, msurf, spts, snrm, sdlt, swts):
         ps, sensor, code, mode, shape, opts = meta
         device = src.device
         sdesc, keep = sensor.pack(device)
@@ -86,17 +107,19 @@ class RenderFunction(torch.autograd.Function):
         out = _forward(ps, _desc_with(ps, rot_, pos_, scale_), sdesc, code, src_, val_, mode, shape, opts, device)
         ctx.meta = meta
         ctx.n_mir = mrot.shape[0]
-        ctx.save_for_backward(rot_, pos_, scale_, src_, val_)
+        ctx.save_for_backward(rot_, pos_, scale_, src_, val_, snrm.detach(), sdlt.detach(), swts.detach())
         del keep
         return out
 
     @staticmethod
     def backward(ctx, gout):
         ps, sensor, code, mode, shape, opts = ctx.meta
-        rot, pos, scale, src, val = ctx.saved_tensors
+        rot, pos, scale, src, val, snrm, sdlt, swts = ctx.saved_tensors
         device = src.device
         sdesc, keep = sensor.pack(device)
         need = ctx.needs_input_grad
+        need_s = any(need[9:13])
+        gsamp = torch.empty((ps.F, ps.M, 7), device=device) if need_s and ps.F * ps.M else None
         g = [torch.empty_like(t) if need[i + 1] else None for i, t in enumerate((rot, pos, scale, src, val))]
         nm = ctx.n_mir
         gm = [torch.empty(sh, device=device) if need[6 + i] and nm else None
@@ -111,13 +134,18 @@ class RenderFunction(torch.autograd.Function):
         N.check(N.load().iact_render_backward(
             ctypes.byref(_desc_with(ps, rot, pos, scale)), ctypes.byref(sdesc), code, src.data_ptr(),
             val.data_ptr(), int(src.shape[0]), mode, gout.data_ptr(), ptr(g[0]), ptr(g[1]), ptr(g[2]),
-            ptr(g[3]), ptr(g[4]), ptr(gm[0]), ptr(gm[1]), ptr(gm[2]), ws.data_ptr(), ws.numel(),
+            ptr(g[3]), ptr(g[4]), ptr(gm[0]), ptr(gm[1]), ptr(gm[2]), ptr(gsamp), ws.data_ptr(), ws.numel(),
             ctypes.byref(opts) if opts is not None else None, stream))
         del keep
         gm = [x if x is not None or not need[6 + i] else torch.zeros((0,) + ((3,) if i < 2 else (10,)),
                                                                       device=device)
               for i, x in enumerate(gm)]
-        return (None, *g, *gm)
+        gs = [None] * 4
+        if gsamp is not None:
+            gs = [x.to(t.dtype) if need[9 + i] else None
+                  for i, (x, t) in enumerate(zip(_sample_grads(gsamp, rot, scale, snrm, sdlt, swts),
+                                                 (snrm, snrm, sdlt, swts)))]
+        return (None, *g, *gm, *gs)
 
 
 def _as_t(x, device):
@@ -145,6 +173,15 @@ def _stage_params(tel, device):
     return torch.cat(rots), torch.cat(poss), torch.cat(surfs)
 
 
+def primary_samples(tel, device):
+    """Concatenated stage-0 sample arrays: points, normals, deltas (F,M,3)
+    and weights (F,M), float32 on `device`, differentiable."""
+    prim = stages_of(tel).get(0, [])
+    cat = lambda name: torch.cat([getattr(g, name) for g in prim]).to(device=device, dtype=torch.float32)
+    pts, nrm, dlt, w = cat("points"), cat("normals"), cat("perturbation_delta"), cat("weights")
+    return pts, nrm, dlt, w.reshape(w.shape[0], w.shape[1])
+
+
 def _needs_grad(tel, src, val):
     if not torch.is_grad_enabled():
         return False
@@ -153,6 +190,8 @@ def _needs_grad(tel, src, val):
     for stage, groups in stages_of(tel).items():
         for g in groups:
             ts = [g.rotations, g.positions, g.perturbation_scale, g.aspheric, g.curvature, g.conic]
+            if stage == 0:
+                ts += [g.points, g.normals, g.perturbation_delta, g.weights]
             if any(isinstance(t, torch.Tensor) and t.requires_grad for t in ts):
                 return True
     return False
@@ -185,8 +224,14 @@ def _launch(tel, sources, values, source_type, sensor_idx, mode, opts=None, seed
         if ps.n_stages > 2:
             raise NotImplementedError("gradients through more than two mirror stages are not available")
         mrot, mpos, msurf = _stage_params(tel, device)
+        prim = stages_of(tel).get(0, [])
+        if any(t.requires_grad for g in prim for t in (g.points, g.normals, g.perturbation_delta, g.weights)):
+            spts, snrm, sdlt, swts = primary_samples(tel, device)
+        else:  # sample arrays are constants: nothing to carry
+            spts = snrm = sdlt = torch.zeros((0, 0, 3), device=device)
+            swts = torch.zeros((0, 0), device=device)
         return RenderFunction.apply((ps, sensor, code, mode, shape, opts), rot, pos, scale, src, val,
-                                    mrot, mpos, msurf)
+                                    mrot, mpos, msurf, spts, snrm, sdlt, swts)
     ps = pack_scene(tel, device)
     sdesc, keep = sensor.pack(device)
     out = _forward(ps, ps.desc, sdesc, code, src, val, mode, shape, opts, device)

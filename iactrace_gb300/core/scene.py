@@ -46,7 +46,7 @@ def _mirror_records(stage_groups) -> np.ndarray:
                 m.pos[:] = g.positions[i].detach().cpu().tolist()
                 m.rot[:] = g.rotations[i].detach().cpu().tolist()
                 m.offset[:] = g.offsets[i].detach().cpu().tolist()
-                m.curvature, m.conic = float(g.curvature), float(g.conic)
+                m.curvature, m.conic = _value(g.curvature), _value(g.conic)
                 for k, a in enumerate(asph):
                     m.asph[k] = a
                 if polygon:
@@ -139,6 +139,10 @@ def primary_params(tel, device):
     return cat("rotations", 3), cat("positions", 3), cat("perturbation_scale", 0)
 
 
+def _value(x) -> float:
+    return float(x.detach()) if isinstance(x, torch.Tensor) else float(x)
+
+
 def _fingerprint(tel):
     """Identity of everything packed once (not the per-facet transforms)."""
     fp = []
@@ -149,7 +153,7 @@ def _fingerprint(tel):
             t = getattr(g, name, None)
             if t is not None:
                 fp.append((id(t), t._version))
-        fp.append((g.optical_stage, float(g.curvature), float(g.conic), len(g)))
+        fp.append((g.optical_stage, _value(g.curvature), _value(g.conic), len(g)))
     for g in (tel.obstruction_groups or []):
         fp.append(id(g))
     return tuple(fp)

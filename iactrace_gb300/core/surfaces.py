@@ -27,15 +27,17 @@ class AsphericSurface:
         return AsphericSurface(float(s["curvature"]), float(s["conic"]), s.get("aspheric", []) or [])
 
     def key(self):
-        return (float(self.curvature), float(self.conic), tuple(float(a) for a in self.aspheric.tolist()))
+        v = lambda x: float(x.detach()) if isinstance(x, torch.Tensor) else float(x)
+        return (v(self.curvature), v(self.conic), tuple(float(a) for a in self.aspheric.detach().tolist()))
 
     def _sag_raw(self, x, y):
         """core/surfaces.py:25-39 (aspheric term i multiplies r2**(2(i+1)))."""
         r2 = x * x + y * y
         c, k = self.curvature, self.conic
         z = r2 * c / (1 + torch.sqrt(1 - (1 + k) * c * c * r2))
-        for i, a in enumerate(self.aspheric.to(r2.dtype).tolist()):
-            z = z + a * r2 ** (2 * (i + 1))
+        a = self.aspheric.to(device=r2.device, dtype=r2.dtype)
+        for i in range(a.shape[0]):  # tensor ops: the coefficients may carry gradients
+            z = z + a[i] * r2 ** (2 * (i + 1))
         return z
 
     def _sag_raw_dr2(self, r2):
@@ -44,9 +46,10 @@ class AsphericSurface:
         s = torch.sqrt(1 - alpha * r2)
         den = 1 + s
         dz = c / den + (r2 * c) * alpha / (2 * s * den * den)
-        for i, a in enumerate(self.aspheric.to(r2.dtype).tolist()):
+        a = self.aspheric.to(device=r2.device, dtype=r2.dtype)
+        for i in range(a.shape[0]):
             p = 2 * (i + 1)
-            dz = dz + a * p * r2 ** (p - 1)
+            dz = dz + a[i] * p * r2 ** (p - 1)
         return dz
 
     def sag(self, x, y, offset):

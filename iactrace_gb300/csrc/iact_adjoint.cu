@@ -166,7 +166,7 @@ int plan_adjoint(AdjK& p, const iact_sensor_t* sn, int block, size_t& smem, long
 int launch_backward(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type, const float* sources,
                     const float* values, int S, int mode, const float* grad_out, float* g_rot, float* g_pos,
                     float* g_scale, float* g_src, float* g_val, float* g_mrot, float* g_mpos, float* g_msurf,
-                    void* ws, size_t ws_bytes, const iact_opts_t* opts, cudaStream_t st) {
+                    float* g_samples, void* ws, size_t ws_bytes, const iact_opts_t* opts, cudaStream_t st) {
   (void)ws_bytes;
   const int F = sc->n_facets;
   const WsLayout L = workspace_for(sc, sn, S, IACT_MODE_BACKWARD);
@@ -178,12 +178,18 @@ int launch_backward(const iact_scene_t* sc, const iact_sensor_t* sn, int src_typ
   const size_t nacc = (size_t)F * kFacetGrad + (size_t)S * 4 + (size_t)n_mir * kMirGrad;
   int rc = check_cuda(cudaMemsetAsync(gfacet, 0, nacc * sizeof(double), st), "zero gradient buckets");
   if (rc) return rc;
+  const size_t nsamp = (size_t)F * std::max(sc->n_samples, 0) * 7;
+  if (g_samples && nsamp) {
+    rc = check_cuda(cudaMemsetAsync(g_samples, 0, nsamp * sizeof(float), st), "zero sample gradients");
+    if (rc) return rc;
+  }
   if (S > 0 && F > 0 && sc->n_samples > 0) {
     rc = check_cuda(cudaMemsetAsync(w + L.counter, 0, 64, st), "reset tile counter");
     if (rc) return rc;
     rc = launch_prep(sc, L, w, st, g_scale != nullptr);
     if (rc) return rc;
     AdjK p = adjoint_params(sc, sn, L, w, sources, values, grad_out, S, g_scale != nullptr, opts);
+    p.gsamp = g_samples;
     const int block = (opts && opts->block_threads > 0) ? opts->block_threads : 256;
     size_t smem = 0;
     rc = plan_adjoint(p, sn, block, smem, 8LL * std::max(device_info().sm_count, 1));

@@ -33,6 +33,7 @@ struct AdjK {
   uint32_t seed;  // jitter stream of extended sources
   const float4* B4;  // per (facet, chunk) bundle bounds (culling on)
   int n_words;       // 32-bit candidate-mask words per task; 0 = no culling
+  float* gsamp;      // optional [F*M, 7]: per sample dL/d(world point, perturbed normal, 1/weight)
 };
 
 // Per-lane running sums of one (facet, source) stream of rays.
@@ -434,6 +435,12 @@ __device__ __forceinline__ void adjoint_tile(const AdjK& p, const Obst& ob, cons
         }
         acc.gsrc[0] += gsrc.x; acc.gsrc[1] += gsrc.y; acc.gsrc[2] += gsrc.z;
         acc.gv += gv0 * -c * iw;
+        if (p.gsamp) {  // per-sample sums over the sources (resampling gradients)
+          float* gs = p.gsamp + si * 7;
+          atomicAdd(gs + 0, a.x); atomicAdd(gs + 1, a.y); atomicAdd(gs + 2, a.z);
+          atomicAdd(gs + 3, b.x); atomicAdd(gs + 4, b.y); atomicAdd(gs + 5, b.z);
+          atomicAdd(gs + 6, gv0 * v * -c);
+        }
       }
     }
     if (++cl == CCc) {

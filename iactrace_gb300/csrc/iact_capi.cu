@@ -169,8 +169,8 @@ int iact_render_backward(const iact_scene_t* scene, const iact_sensor_t* sensor,
                          const float* sources, const float* values, int32_t n_sources, int32_t mode,
                          const float* grad_out, float* g_facet_rot, float* g_facet_pos, float* g_facet_scale,
                          float* g_sources, float* g_values, float* g_mirror_rot, float* g_mirror_pos,
-                         float* g_mirror_surface, void* workspace, size_t workspace_bytes, const iact_opts_t* opts,
-                         void* stream) {
+                         float* g_mirror_surface, float* g_samples, void* workspace, size_t workspace_bytes,
+                         const iact_opts_t* opts, void* stream) {
   if (mode != IACT_MODE_IMAGE && mode != IACT_MODE_RESPONSE)
     return set_error(IACT_E_INVALID, "mode must be IACT_MODE_IMAGE or IACT_MODE_RESPONSE");
   int rc = check_common(scene, sensor, source_type, sources, values, n_sources, IACT_MODE_BACKWARD, workspace,
@@ -183,7 +183,8 @@ int iact_render_backward(const iact_scene_t* scene, const iact_sensor_t* sensor,
   if (!grad_out && acc_elems(sensor, n_sources, mode) > 0) return set_error(IACT_E_INVALID, "grad_out is NULL");
   return launch_backward(scene, sensor, source_type, sources, values, n_sources, mode, grad_out, g_facet_rot,
                          g_facet_pos, g_facet_scale, g_sources, g_values, g_mirror_rot, g_mirror_pos,
-                         g_mirror_surface, workspace, workspace_bytes, opts, static_cast<cudaStream_t>(stream));
+                         g_mirror_surface, g_samples, workspace, workspace_bytes, opts,
+                         static_cast<cudaStream_t>(stream));
 }
 
 }  // extern "C"

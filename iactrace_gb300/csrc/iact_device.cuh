@@ -242,7 +242,7 @@ struct Bundle {
 // radius `rad` around `q` can lie from a ray origin, plus the margin
 __device__ __forceinline__ float bundle_reach(const Bundle& b, V3 q, float rad) {
   V3 w = q - b.c;
-  const float T = sqrtf(dot(w, w)) + rad + b.R0;
+  const float T = sqrt_a(dot(w, w)) * 1.00001f + rad + b.R0;
   return b.R0 + T * b.dlt + 2e-3f + 1e-4f * T;
 }
 
@@ -275,7 +275,7 @@ __device__ __forceinline__ bool capsule_may_hit(const Bundle& b, V3 p1, V3 ax, f
     V3 q = w0 - s * ax;
     best = fminf(best, dot(q, q));
   }
-  const float t = (bb * e - d) / den, s = e + t * bb;
+  const float t = (bb * e - d) * rcp_a(den), s = e + t * bb;
   if (t >= 0.f && s >= 0.f && s <= h) {
     V3 q = w0 + t * b.u - s * ax;
     best = fminf(best, dot(q, q));
@@ -287,7 +287,7 @@ __device__ __forceinline__ bool capsule_may_hit(const Bundle& b, V3 p1, V3 ax, f
 __device__ __forceinline__ bool aabb_may_hit(const Bundle& b, const float* bx) {
   const V3 lo = mk(bx[0], bx[1], bx[2]), hi = mk(bx[3], bx[4], bx[5]);
   const V3 ctr = 0.5f * (lo + hi), half = 0.5f * (hi - lo);
-  const float g = bundle_reach(b, ctr, sqrtf(dot(half, half)));
+  const float g = bundle_reach(b, ctr, sqrt_a(dot(half, half)) * 1.00001f);
   float t0 = 0.f, t1 = 3.0e38f;
   const float cc[3] = {b.c.x, b.c.y, b.c.z}, uu[3] = {b.u.x, b.u.y, b.u.z};
 #pragma unroll
@@ -296,7 +296,7 @@ __device__ __forceinline__ bool aabb_may_hit(const Bundle& b, const float* bx) {
     if (fabsf(uu[a]) < 1e-20f) {
       if (cc[a] < l || cc[a] > hgh) return false;
     } else {
-      const float inv = 1.f / uu[a];
+      const float inv = rcp_a(uu[a]);
       const float ta = (l - cc[a]) * inv, tb = (hgh - cc[a]) * inv;
       t0 = fmaxf(t0, fminf(ta, tb));
       t1 = fminf(t1, fmaxf(ta, tb));
@@ -310,26 +310,26 @@ __device__ __forceinline__ bool aabb_may_hit(const Bundle& b, const float* bx) {
 __device__ __forceinline__ bool prim_may_hit(const Obst& ob, int k, const Bundle& b) {
   if (k < ob.n_cyl) {
     const float* c = ob.cyl + k * kCylF;
-    return capsule_may_hit(b, mk(c[0], c[1], c[2]), mk(c[3], c[4], c[5]), c[6], sqrtf(c[7]));
+    return capsule_may_hit(b, mk(c[0], c[1], c[2]), mk(c[3], c[4], c[5]), c[6], sqrt_a(c[7]) * 1.00001f);
   }
   k -= ob.n_cyl;
   if (k < ob.n_box) return aabb_may_hit(b, ob.box + k * kBoxF);
   k -= ob.n_box;
   if (k < ob.n_sph) {
     const float* s = ob.sph + k * kSphF;
-    return sphere_may_hit(b, mk(s[0], s[1], s[2]), sqrtf(s[3]));
+    return sphere_may_hit(b, mk(s[0], s[1], s[2]), sqrt_a(s[3]) * 1.00001f);
   }
   k -= ob.n_sph;
   if (k < ob.n_obox) {
     const float* o = ob.obox + k * kOboxF;
-    return sphere_may_hit(b, mk(o[0], o[1], o[2]), sqrtf(o[3] * o[3] + o[4] * o[4] + o[5] * o[5]));
+    return sphere_may_hit(b, mk(o[0], o[1], o[2]), sqrt_a(o[3] * o[3] + o[4] * o[4] + o[5] * o[5]) * 1.00001f);
   }
   k -= ob.n_obox;
   const float* t = ob.tri + k * kTriF;
   const V3 v0 = mk(t[0], t[1], t[2]), e1 = mk(t[3], t[4], t[5]), e2 = mk(t[6], t[7], t[8]);
   const V3 g = v0 + (1.f / 3.f) * (e1 + e2);
   V3 a = v0 - g, bq = (v0 + e1) - g, cq = (v0 + e2) - g;
-  const float rad = sqrtf(fmaxf(fmaxf(dot(a, a), dot(bq, bq)), dot(cq, cq)));
+  const float rad = sqrt_a(fmaxf(fmaxf(dot(a, a), dot(bq, bq)), dot(cq, cq))) * 1.00001f;
   return sphere_may_hit(b, g, rad);
 }
 

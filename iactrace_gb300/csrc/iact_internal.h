@@ -83,6 +83,6 @@ int launch_probe_fma(float* out, int blocks, int iters, cudaStream_t stream);
 int launch_backward(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type, const float* sources,
                     const float* values, int S, int mode, const float* grad_out, float* g_rot, float* g_pos,
                     float* g_scale, float* g_src, float* g_val, float* g_mrot, float* g_mpos, float* g_msurf,
-                    void* ws, size_t ws_bytes, const iact_opts_t* opts, cudaStream_t stream);
+                    float* g_samples, void* ws, size_t ws_bytes, const iact_opts_t* opts, cudaStream_t stream);
 
 }  // namespace iact

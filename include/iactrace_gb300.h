@@ -218,9 +218,12 @@ int iact_render_debug(const iact_scene_t* scene, const iact_sensor_t* sensor,
  * mirror stages after the primary: given grad_out = dL/d(out), writes
  * dL/d(facet rotations) [F,3] (per degree), dL/d(facet positions) [F,3],
  * dL/d(facet perturbation scales) [F], dL/d(sources) [S,3], dL/d(values)
- * [S], and per stage mirror dL/d(rotation) [n_mirrors,3], dL/d(position)
- * [n_mirrors,3] and dL/d(curvature, conic, aspheric[8]) [n_mirrors,10];
- * any output may be NULL. Each
+ * [S], per stage mirror dL/d(rotation) [n_mirrors,3], dL/d(position)
+ * [n_mirrors,3] and dL/d(curvature, conic, aspheric[8]) [n_mirrors,10], and
+ * per primary sample (g_samples [F*M,7]) dL/d(world point) (3), dL/d(unit
+ * perturbed world normal) (3) and dL/d(1/weight) (1), summed over the
+ * sources, for gradients that flow through the sample arrays (primary
+ * surface parameters via resampling); any output may be NULL. Each
  * ray's forward path is recomputed, nothing is stored between the calls.
  * Pixel ids and shadow masks carry no gradient (as under jax.grad); soft
  * sensors also pass gradients through the sensor-plane position. Workspace:
@@ -233,9 +236,9 @@ int iact_render_backward(const iact_scene_t* scene, const iact_sensor_t* sensor,
                          float* g_facet_pos, float* g_facet_scale,
                          float* g_sources, float* g_values,
                          float* g_mirror_rot, float* g_mirror_pos,
-                         float* g_mirror_surface, void* workspace,
-                         size_t workspace_bytes, const iact_opts_t* opts,
-                         void* stream);
+                         float* g_mirror_surface, float* g_samples,
+                         void* workspace, size_t workspace_bytes,
+                         const iact_opts_t* opts, void* stream);
 
 /* ---- Batched persistent render -------------------------------------------
  * Many telescope variants and source sets of uneven size in one persistent

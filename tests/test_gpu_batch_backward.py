@@ -2,7 +2,10 @@
 against the single-scene adjoint of every job (iact_render_backward through
 torch.autograd, itself checked against the FP64 twin and finite
 differences). Same rays, same buckets; only the FP64 summation order of the
-warp flushes differs: relative L2 per gradient block <= SAME_TOL."""
+warp flushes differs: relative L2 per gradient block <= SAME_TOL; the
+stage-mirror blocks go through FP32 shared-memory partial sums whose
+grouping follows the tiling (which differs between a batch and a single
+launch), so they are held to the gradient tolerance MIRROR_TOL."""
 from __future__ import annotations
 
 import numpy as np
@@ -16,6 +19,7 @@ from test_gpu_adjoint import gpu_grads
 from test_gpu_batch import _mixed_jobs
 
 SAME_TOL = 1e-5
+MIRROR_TOL = 1e-4
 
 pytestmark = pytest.mark.gpu
 
@@ -47,12 +51,12 @@ def test_batch_backward_equals_single_backward(cuda, mode):
                 e = _rel(res[i][k].cpu().numpy(), ref[k])
                 assert e <= SAME_TOL, f"replay {rep} job {i} d/d{k}: relative L2 {e:.3g}"
             if "mrot0" in ref:
-                assert _rel(res[i]["mrot"].cpu().numpy(), ref["mrot0"]) <= SAME_TOL
-                assert _rel(res[i]["mpos"].cpu().numpy(), ref["mpos0"]) <= SAME_TOL
+                assert _rel(res[i]["mrot"].cpu().numpy(), ref["mrot0"]) <= MIRROR_TOL
+                assert _rel(res[i]["mpos"].cpu().numpy(), ref["mpos0"]) <= MIRROR_TOL
                 ms = res[i]["msurf"].cpu().numpy()[0]
-                assert _rel(ms[0], ref["mc0"]) <= SAME_TOL and _rel(ms[1], ref["mk0"]) <= SAME_TOL
+                assert _rel(ms[0], ref["mc0"]) <= MIRROR_TOL and _rel(ms[1], ref["mk0"]) <= MIRROR_TOL
                 na = ref["masph0"].size
-                assert _rel(ms[2:2 + na], ref["masph0"]) <= SAME_TOL
+                assert _rel(ms[2:2 + na], ref["masph0"]) <= MIRROR_TOL
 
 
 def test_batch_backward_extended_soft_hex(cuda):
