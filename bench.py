@@ -229,7 +229,7 @@ def run_reference(args, rank, world):
     t = time.perf_counter()
     O.render(tel, src[:n], val[:n], stype, 0, mode=omode, dtype="f32", threads=threads)
     rate = n * F * M / max(time.perf_counter() - t, 1e-9)
-    budget = 150.0 / max(1, args.steps + args.warmup)
+    budget = args.cpu_budget / max(1, args.steps + args.warmup)
     ns = int(max(1, min(src.shape[0], rate * budget / (F * M))))
     for _ in range(args.warmup):
         O.render(tel, src[:ns], val[:ns], stype, 0, mode=omode, dtype="f32", threads=threads)
@@ -259,7 +259,7 @@ def run_reference_batched(args, world):
     tels, srcs, vals, st = W.ragged_batch()
     threads = os.cpu_count() or 1
     M = tels[0].mirror_groups[0].n_samples
-    budget = 150.0 / max(1, args.steps + args.warmup)
+    budget = args.cpu_budget / max(1, args.steps + args.warmup)
 
     def step():
         rays, t0, k = 0, time.perf_counter(), 0
@@ -529,6 +529,8 @@ def main():
     ap.add_argument("--instances", type=int, default=64, help="batched workload: telescope variants")
     ap.add_argument("--max-sources", type=int, default=4096, help="batched workload: largest source count")
     ap.add_argument("--no-tune", action="store_true", help="batched workload: library defaults, no autotuner")
+    ap.add_argument("--cpu-budget", type=float, default=150.0,
+                    help="--impl reference: seconds of CPU work over all steps")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = _env_rank()

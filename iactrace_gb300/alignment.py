@@ -18,6 +18,7 @@ error is reported beside the loss but is not expected to fall with it.
 from __future__ import annotations
 
 import math
+import os
 import time
 
 import numpy as np
@@ -89,16 +90,38 @@ def rms_tilt_error_mrad(rot, truth) -> float:
     return float(torch.sqrt((d * d).mean()) * math.pi / 180.0 * 1e3)
 
 
-def run(prob, steps: int = 200, lr: float = 2e-3, log_every: int = 0):
-    """Adam on the facet tips and tilts (degrees). Returns the history."""
+def run(prob, steps: int = 200, lr: float = 2e-3, log_every: int = 0, checkpoint: str | None = None,
+        checkpoint_every: int = 50):
+    """Adam on the facet tips and tilts (degrees). Returns the history.
+
+    checkpoint: a file; if it exists the run resumes from it (tilt offsets,
+    Adam moments, step count, history) and continues up to `steps` in
+    total; the state is saved there every `checkpoint_every` steps and at
+    the end."""
     tel, src, val, target = prob["telescope"], prob["sources"], prob["values"], prob["target"]
     base = prob["nominal"]
     delta = torch.zeros((base.shape[0], 2), device=base.device, requires_grad=True)
     opt = torch.optim.Adam([delta], lr=lr)
     pad = torch.zeros((base.shape[0], 1), device=base.device)
     hist = {"loss": [], "rms_mrad": [], "step_ms": []}
+    start = 0
+    if checkpoint is not None and os.path.exists(checkpoint):
+        st = torch.load(checkpoint, map_location=base.device, weights_only=False)
+        with torch.no_grad():
+            delta.copy_(st["delta"])
+        opt.load_state_dict(st["adam"])
+        hist = st["history"]
+        start = int(st["step"])
+
+    def save(step):
+        if checkpoint is not None:
+            tmp = checkpoint + ".tmp"
+            torch.save({"delta": delta.detach().clone(), "adam": opt.state_dict(), "history": hist, "step": step},
+                       tmp)
+            os.replace(tmp, checkpoint)
+
     scale = float(target.pow(2).sum())
-    for it in range(steps):
+    for it in range(start, steps):
         t0 = time.perf_counter()
         opt.zero_grad(set_to_none=True)
         rot = base + torch.cat([delta, pad], 1)
@@ -112,4 +135,7 @@ def run(prob, steps: int = 200, lr: float = 2e-3, log_every: int = 0):
         hist["rms_mrad"].append(rms_tilt_error_mrad(rot, prob["truth"]))
         if log_every and (it % log_every == 0 or it == steps - 1):
             print(f"step {it:4d} loss {hist['loss'][-1]:.4e} rms tilt error {hist['rms_mrad'][-1]:.3f} mrad")
+        if checkpoint is not None and (it + 1) % checkpoint_every == 0:
+            save(it + 1)
+    save(max(start, steps))
     return hist

@@ -10,7 +10,7 @@ any group is hit (core/render.py:38-40).
 from __future__ import annotations
 
 import ctypes
-from collections import defaultdict
+from collections import OrderedDict, defaultdict
 
 import numpy as np
 import torch
@@ -64,6 +64,13 @@ def _mirror_records(stage_groups) -> np.ndarray:
     return np.frombuffer(b"".join(recs), dtype=np.uint8) if recs else np.zeros(0, np.uint8)
 
 
+def _require_finite(what: str, t: torch.Tensor) -> None:
+    """Host-side input validation at pack time (once per scene): the kernels
+    do not check their tables, so NaN / Inf never reach them."""
+    if t.numel() and not bool(torch.isfinite(t).all()):
+        raise ValueError(f"{what} contains NaN or Inf")
+
+
 class PackedScene:
     """Device-resident tables + the iact_scene_t that points at them.
 
@@ -86,6 +93,8 @@ class PackedScene:
         d.n_facets, d.n_samples = self.F, self.M
         if self.F and self.M:
             cat = lambda name: torch.cat([getattr(g, name).detach().float() for g in prim])
+            for name in ("points", "normals", "perturbation_delta", "weights"):
+                _require_finite(f"primary {name}", cat(name))
             self.points = _f32(cat("points"), device)
             self.normals = _f32(cat("normals"), device)
             self.delta = _f32(cat("perturbation_delta"), device)
@@ -94,6 +103,9 @@ class PackedScene:
                 setattr(d, name, getattr(self, name).data_ptr())
         later = [(s, gs) for s, gs in st.items() if s != 0]
         recs = _mirror_records(later)
+        if len(recs) and not np.isfinite(recs.view(np.float32)).all():
+            # the records are float32 fields and int32 counts; counts are finite as floats too
+            raise ValueError("stage-mirror parameters contain NaN or Inf")
         self.n_mirrors = len(recs) // ctypes.sizeof(N.IactMirror)
         self.mirrors = torch.from_numpy(recs.copy()).to(device) if self.n_mirrors else None
         d.n_mirrors = self.n_mirrors
@@ -102,7 +114,9 @@ class PackedScene:
         d.mirrors = self.mirrors.data_ptr() if self.n_mirrors else None
         kinds = defaultdict(list)
         for g in (tel.obstruction_groups or []):
-            kinds[g.kind].append(g.table().float())
+            t = g.table().float()
+            _require_finite(f"{g.kind} obstruction table", t)
+            kinds[g.kind].append(t)
         self.obst = {}
         for kind in ("cyl", "box", "sph", "obox", "tri"):
             if kinds[kind]:
@@ -159,6 +173,23 @@ def _fingerprint(tel):
     return tuple(fp)
 
 
+# Packed scenes shared by telescopes built from the same sample arrays, stage
+# mirrors and obstructions (an optimiser's functional updates of the facet
+# transforms create a new Telescope per step). The entries keep their source
+# tensors alive, so the ids in the fingerprint cannot be reused while cached.
+_SHARED = OrderedDict()
+_SHARED_MAX = 16
+
+
+def _sources(tel):
+    out = []
+    for g in tel.mirror_groups:
+        names = ("points", "normals", "perturbation_delta", "weights") if g.optical_stage == 0 else \
+            ("positions", "rotations", "offsets", "aspheric")
+        out += [getattr(g, n, None) for n in names]
+    return out + list(tel.obstruction_groups or [])
+
+
 def pack_scene(tel, device, facets=None) -> PackedScene:
     """Packed tables of `tel` on `device` (cached while the sample arrays,
     stage mirrors and obstructions are unchanged), with the current facet
@@ -170,7 +201,15 @@ def pack_scene(tel, device, facets=None) -> PackedScene:
     if hit is not None and hit[0] == fp:
         ps = hit[1]
     else:
-        ps = PackedScene(tel, device)
+        shared = _SHARED.get((key, fp))
+        if shared is not None:
+            _SHARED.move_to_end((key, fp))
+            ps = shared[1]
+        else:
+            ps = PackedScene(tel, device)
+            _SHARED[(key, fp)] = (_sources(tel), ps)
+            while len(_SHARED) > _SHARED_MAX:
+                _SHARED.popitem(last=False)
         cache[key] = (fp, ps)
     if facets is None:
         # device copies of the facet transforms, reused while the source

@@ -64,3 +64,16 @@ def test_alignment_reduces_image_loss(cuda):
     assert hist["loss"][-1] < 0.3 * hist["loss"][0], hist["loss"][::8]
     assert min(hist["loss"][:5]) < hist["loss"][0], hist["loss"][:5]
     print("rms tilt error (mrad)", hist["rms_mrad"][::8])
+
+
+def test_alignment_checkpoint_resume(cuda, tmp_path):
+    """An interrupted run resumed from its checkpoint continues where it
+    stopped: same steps, Adam state carried over, history appended."""
+    ck = str(tmp_path / "align.pt")
+    pb = _problem(n_facets=37, n_samples=16, n_sources=16, n_pixels=400)
+    full = A.run(pb, steps=12, lr=4e-3)
+    A.run(pb, steps=6, lr=4e-3, checkpoint=ck, checkpoint_every=3)
+    resumed = A.run(pb, steps=12, lr=4e-3, checkpoint=ck)
+    assert len(resumed["loss"]) == 12
+    # the first six steps are the interrupted run's; the rest continue it
+    assert np.allclose(resumed["loss"], full["loss"], rtol=1e-3)
