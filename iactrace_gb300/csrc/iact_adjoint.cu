@@ -36,7 +36,7 @@
 namespace iact {
 
 template <int SRC, bool SOFT, int MODE, bool STAGES>
-__global__ void __launch_bounds__(256) k_adjoint(const AdjK p) {
+__global__ void __launch_bounds__(256, STAGES ? 2 : (SOFT ? 3 : 4)) k_adjoint(const AdjK p) {
   extern __shared__ __align__(16) float smem[];
   __shared__ int s_tile;
   const int tab_n = (p.n_table_floats + 3) & ~3;

@@ -23,7 +23,7 @@
 namespace iact {
 
 template <int SRC, bool SOFT, int MODE, bool STAGES>
-__global__ void __launch_bounds__(256) k_batch_adjoint(const BatchK b) {
+__global__ void __launch_bounds__(256, STAGES ? 2 : (SOFT ? 3 : 4)) k_batch_adjoint(const BatchK b) {
   extern __shared__ __align__(16) float smem[];
   __shared__ __align__(16) AdjK s_a;
   __shared__ int s_tile, s_job, s_begin;
