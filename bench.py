@@ -305,14 +305,14 @@ def run_alignment(args, rank, world):
     M = pb["telescope"].mirror_groups[0].n_samples
     S = pb["sources"].shape[0]
     rays = F * M * S
-    A.run(pb, steps=args.warmup)  # warm-up
+    A.run(pb, steps=args.warmup, graph=True)  # warm-up
     clocks = ClockSampler(torch.cuda.current_device())
     clocks.start()
     time.sleep(0.3)
     steps = max(args.steps, 200)
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
-    hist = A.run(pb, steps=steps)
+    hist = A.run(pb, steps=steps, graph=True)
     torch.cuda.synchronize(dev)
     dt = (time.perf_counter() - t0) / steps
     clk = clocks.stop()
@@ -324,7 +324,8 @@ def run_alignment(args, rank, world):
             "data": "synthetic (seeded dish, sources and misalignment)",
             "config": {"workload": "alignment_dish28m_876facets_hex2048_extended256", "facets": F,
                        "samples_per_facet": M, "sources": S, "parameters": 2 * F, "rays_per_step": rays,
-                       "timing": "host wall clock per Adam step incl. synchronize (forward, adjoint, optimiser)"},
+                       "timing": "host wall clock per Adam step incl. synchronize (forward, adjoint, optimiser; "
+                                 "3 eager steps, then the step replayed as one CUDA graph)"},
             "alignment": {"loss_first": hist["loss"][0], "loss_last": hist["loss"][-1],
                           "rms_tilt_error_mrad_first": hist["rms_mrad"][0],
                           "rms_tilt_error_mrad_last": hist["rms_mrad"][-1], "adam_steps": steps},

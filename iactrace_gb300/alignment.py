@@ -91,17 +91,23 @@ def rms_tilt_error_mrad(rot, truth) -> float:
 
 
 def run(prob, steps: int = 200, lr: float = 2e-3, log_every: int = 0, checkpoint: str | None = None,
-        checkpoint_every: int = 50):
+        checkpoint_every: int = 50, graph: bool = False):
     """Adam on the facet tips and tilts (degrees). Returns the history.
 
     checkpoint: a file; if it exists the run resumes from it (tilt offsets,
     Adam moments, step count, history) and continues up to `steps` in
     total; the state is saved there every `checkpoint_every` steps and at
-    the end."""
+    the end. graph: after three eager steps, the whole Adam step (render,
+    loss, adjoint, optimiser) is captured in a CUDA graph and replayed."""
     tel, src, val, target = prob["telescope"], prob["sources"], prob["values"], prob["target"]
     base = prob["nominal"]
+    # the facet positions and roughness scales stay fixed: keep them on the
+    # device (no per-step host copies, and nothing to copy inside a graph)
+    g0 = tel.mirror_groups[0]
+    g0 = g0.replace(positions=g0.positions.to(base.device), perturbation_scale=g0.perturbation_scale.to(base.device))
+    tel = Telescope([g0] + list(tel.mirror_groups[1:]), tel.obstruction_groups, tel.sensors, name=tel.name)
     delta = torch.zeros((base.shape[0], 2), device=base.device, requires_grad=True)
-    opt = torch.optim.Adam([delta], lr=lr)
+    opt = torch.optim.Adam([delta], lr=lr, capturable=graph)
     pad = torch.zeros((base.shape[0], 1), device=base.device)
     hist = {"loss": [], "rms_mrad": [], "step_ms": []}
     start = 0
@@ -121,14 +127,16 @@ def run(prob, steps: int = 200, lr: float = 2e-3, log_every: int = 0, checkpoint
             os.replace(tmp, checkpoint)
 
     scale = float(target.pow(2).sum())
-    for it in range(start, steps):
-        t0 = time.perf_counter()
-        opt.zero_grad(set_to_none=True)
+
+    def body():
         rot = base + torch.cat([delta, pad], 1)
         img = render(tel.set_mirror_rotations(0, rot), src, val, "extended", seed=prob["seed"])
         loss = (img - target).pow(2).sum() / scale
         loss.backward()
         opt.step()
+        return loss, rot
+
+    def record(it, t0, loss, rot):
         torch.cuda.synchronize()
         hist["step_ms"].append((time.perf_counter() - t0) * 1e3)
         hist["loss"].append(float(loss.detach()))
@@ -137,5 +145,37 @@ def run(prob, steps: int = 200, lr: float = 2e-3, log_every: int = 0, checkpoint
             print(f"step {it:4d} loss {hist['loss'][-1]:.4e} rms tilt error {hist['rms_mrad'][-1]:.3f} mrad")
         if checkpoint is not None and (it + 1) % checkpoint_every == 0:
             save(it + 1)
+
+    it = start
+    n_eager = steps if not graph else min(steps, start + 3)
+    side = torch.cuda.Stream(base.device) if graph else None
+    if graph:  # eager steps on a side stream warm up the allocator, autograd and Adam state
+        side.wait_stream(torch.cuda.current_stream(base.device))
+    with torch.cuda.stream(side) if graph else _nullctx():
+        while it < n_eager:
+            t0 = time.perf_counter()
+            opt.zero_grad(set_to_none=True)
+            loss, rot = body()
+            record(it, t0, loss, rot)
+            it += 1
+    if graph and it < steps:
+        torch.cuda.current_stream(base.device).wait_stream(side)
+        g = torch.cuda.CUDAGraph()
+        opt.zero_grad(set_to_none=True)
+        with torch.cuda.graph(g):
+            s_loss, s_rot = body()
+        while it < steps:
+            t0 = time.perf_counter()
+            g.replay()
+            record(it, t0, s_loss, s_rot)
+            it += 1
     save(max(start, steps))
     return hist
+
+
+class _nullctx:
+    def __enter__(self):
+        return None
+
+    def __exit__(self, *a):
+        return False

@@ -77,3 +77,12 @@ def test_alignment_checkpoint_resume(cuda, tmp_path):
     assert len(resumed["loss"]) == 12
     # the first six steps are the interrupted run's; the rest continue it
     assert np.allclose(resumed["loss"], full["loss"], rtol=1e-3)
+
+
+def test_alignment_graph_replay_matches_eager(cuda):
+    """The whole Adam step captured in a CUDA graph follows the eager run."""
+    pb = _problem(n_facets=37, n_samples=16, n_sources=16, n_pixels=400)
+    eager = A.run(pb, steps=10, lr=4e-3)
+    graph = A.run(pb, steps=10, lr=4e-3, graph=True)
+    assert np.allclose(graph["loss"], eager["loss"], rtol=1e-3), (graph["loss"], eager["loss"])
+    assert np.allclose(graph["rms_mrad"], eager["rms_mrad"], rtol=1e-3)
