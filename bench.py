@@ -316,6 +316,25 @@ def run_alignment(args, rank, world):
     torch.cuda.synchronize(dev)
     dt = (time.perf_counter() - t0) / steps
     clk = clocks.stop()
+    # kernel time of one forward render and one adjoint of the same problem (CUDA events)
+    import iactrace_gb300 as it
+    from iactrace_gb300 import _native as N
+    tel, src, val = pb["telescope"], pb["sources"], pb["values"]
+    ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+    stream = torch.cuda.current_stream(dev)
+    ev[0].record(stream)
+    ev[1].record(stream)
+    o = N.IactOpts()
+    o.kernel_events[0], o.kernel_events[1] = ev[0].cuda_event, ev[1].cuda_event
+    o.seed = pb["seed"]
+    flush_buf = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    fw = []
+    for k in range(5):
+        flush_buf.fill_(float(k))
+        out = it.render(tel, src, val, "extended", opts=o, seed=pb["seed"])
+        ev[1].synchronize()
+        fw.append(ev[0].elapsed_time(ev[1]))
+    adj_s = adjoint_kernel_seconds(tel, src, val, "extended", "image", torch.ones_like(out), flush_buf, 5)
     if rank == 0:
         print(json.dumps({
             "metric": METRIC + " [alignment: Adam step = fwd + adjoint]", "value": rays / dt, "unit": "rays/s",
@@ -326,6 +345,8 @@ def run_alignment(args, rank, world):
                        "samples_per_facet": M, "sources": S, "parameters": 2 * F, "rays_per_step": rays,
                        "timing": "host wall clock per Adam step incl. synchronize (forward, adjoint, optimiser; "
                                  "3 eager steps, then the step replayed as one CUDA graph)"},
+            "kernels": {"render_ms": sorted(fw)[2], "adjoint_ms": adj_s * 1e3,
+                        "kernel_time_ratio_vs_fwd": (sorted(fw)[2] + adj_s * 1e3) / sorted(fw)[2]},
             "alignment": {"loss_first": hist["loss"][0], "loss_last": hist["loss"][-1],
                           "rms_tilt_error_mrad_first": hist["rms_mrad"][0],
                           "rms_tilt_error_mrad_last": hist["rms_mrad"][-1], "adam_steps": steps},

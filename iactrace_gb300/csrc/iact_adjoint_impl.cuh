@@ -133,7 +133,13 @@ __device__ __forceinline__ void soft_hex_bwd(const SensorK& s, const TT* table, 
   const int p0 = hex_lookup(s, table, qi, ri);
   const float g0 = p0 >= 0 ? g[rowbase + p0] : 0.f;
   float W = 0.f, sgw = 0.f, dWx = 0.f, dWy = 0.f, sgdx = 0.f, sgdy = 0.f;  // d/d(grid x, grid y)
+  // lookup-table index of the base hexagon; interior rings are at fixed offsets
+  const float qx = qi - (float)s.q_min, rx = ri - (float)s.r_min;
+  const bool inner = (qx >= (float)K) & (qx < (float)(s.table_q - K)) & (rx >= (float)K) & (rx < (float)(s.table_r - K));
+  const int base = inner ? (int)qx * s.table_r + (int)rx : 0;
+#pragma unroll 3
   for (int q = -K; q <= K; ++q)
+#pragma unroll 3
     for (int r = -K; r <= K; ++r) {
       if (max(max(abs(q), abs(r)), abs(q + r)) > K) continue;
       float ux = ddx - s.hex_sx * ((float)q + 0.5f * (float)r), uy = ddy - s.hex_sy * (float)r;
@@ -147,7 +153,13 @@ __device__ __forceinline__ void soft_hex_bwd(const SensorK& s, const TT* table, 
       float dhy = (first ? 0.f : 0.8660254037844386f) * (uy >= 0.f ? 1.f : -1.f) * s.inv_inr;
       float dwda = -w * a * isg;  // dw/dhd
       float wx = dwda * dhx, wy = dwda * dhy;
-      int p = hex_lookup(s, table, qi + (float)q, ri + (float)r);
+      int p;
+      if (inner) {
+        p = (int)table[base + q * s.table_r + r];
+        p = p >= 0 ? p : -1;
+      } else {
+        p = hex_lookup(s, table, qi + (float)q, ri + (float)r);
+      }
       float dg = (p >= 0 ? g[rowbase + p] : 0.f) - g0;
       W += w; sgw += dg * w; dWx += wx; dWy += wy; sgdx += dg * wx; sgdy += dg * wy;
     }
@@ -288,8 +300,8 @@ __device__ __forceinline__ void adjoint_tile(const AdjK& p, const Obst& ob, cons
   const int s0 = sblk * p.SB, f0 = fc * p.FC, c0 = cc * p.CC;
   const int SBc = min(p.SB, p.S - s0), FCc = min(p.FC, p.F - f0), CCc = min(p.CC, nch - c0);
   const int T = SBc * FCc * CCc;
-  if (p.n_words) tile_masks<SRC>(p.B4, p.sources, p.M, p.n_words, ob, s0, f0, c0, FCc, CCc, T, tmask);
   const int tb = (warp * T) / nw, te = ((warp + 1) * T) / nw;
+  if (p.n_words) warp_masks<SRC>(p.B4, p.sources, p.M, p.n_words, ob, s0, f0, c0, FCc, CCc, tb, te, tmask);
   int sl = tb / (FCc * CCc);
   int fl = (tb - sl * FCc * CCc) / CCc;
   int cl = tb - sl * FCc * CCc - fl * CCc;

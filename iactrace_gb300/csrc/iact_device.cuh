@@ -383,6 +383,7 @@ struct SensorK {
   int q_min, r_min, table_q, table_r;
   float sigma;
   int kernel_size;
+  float hex_lim2;  // (inradius * edge_threshold - 1e-5)^2: points this close to a cell centre bin to that cell
 };
 
 // core/intersections.py:6-41 intersect_plane -> local (x, y) or (1e10, 1e10)
@@ -400,12 +401,13 @@ __device__ __forceinline__ void plane_hit(const SensorK& s, V3 o, V3 d, float& x
 
 // sensors/square.py:66-91 SquareSensor.accumulate: pixel id or -1
 __device__ __forceinline__ int bin_square(const SensorK& s, float x, float y) {
-  float xc = (x - s.x0) * s.inv_dx, yc = (y - s.y0) * s.inv_dy;
-  float xf = floorf(xc), yf = floorf(yc);
+  // explicit roundings (no contraction): every kernel bins a point identically
+  const float xc = __fmul_rn(__fsub_rn(x, s.x0), s.inv_dx), yc = __fmul_rn(__fsub_rn(y, s.y0), s.inv_dy);
+  const float xf = floorf(xc), yf = floorf(yc);
   // compare in float: out-of-range and NaN fail, as the int32 cast would
   bool valid = (xf >= 0.f) && (xf < (float)s.width) && (yf >= 0.f) && (yf < (float)s.height);
-  float fx = xc - xf, fy = yc - yf;
-  float dist = fminf(fminf(fx, 1.f - fx) * s.dx, fminf(fy, 1.f - fy) * s.dy);
+  const float fx = __fsub_rn(xc, xf), fy = __fsub_rn(yc, yf);
+  const float dist = fminf(__fmul_rn(fminf(fx, __fsub_rn(1.f, fx)), s.dx), __fmul_rn(fminf(fy, __fsub_rn(1.f, fy)), s.dy));
   valid = valid && !(dist < s.edge_width);
   return valid ? (int)yf * s.width + (int)xf : -1;
 }
@@ -413,20 +415,19 @@ __device__ __forceinline__ int bin_square(const SensorK& s, float x, float y) {
 // sensors/hexagonal.py:16-23 _rotate and :26-29 _cartesian_to_axial, :32-39 _axial_round
 __device__ __forceinline__ void hex_axial(const SensorK& s, float x, float y, float& xg, float& yg,
                                           float& qi, float& ri) {
-  const float SQRT3_3 = 0.5773502691896257f;
-  float xs = x - s.off_x, ys = y - s.off_y;
-  xg = s.gc * xs - s.gs * ys;
-  yg = s.gs * xs + s.gc * ys;
-  (void)SQRT3_3;
-  float q = fmaf(s.hq_x, xg, -s.hq_y * yg);  // (sqrt(3)/3 x - y/3) / size
-  float r = s.hr_y * yg;                      // (2 y / 3) / size
-  float sv = -q - r;
+  // explicit roundings (no contraction): every kernel bins a point identically
+  const float xs = __fsub_rn(x, s.off_x), ys = __fsub_rn(y, s.off_y);
+  xg = __fsub_rn(__fmul_rn(s.gc, xs), __fmul_rn(s.gs, ys));
+  yg = __fadd_rn(__fmul_rn(s.gs, xs), __fmul_rn(s.gc, ys));
+  const float q = __fsub_rn(__fmul_rn(s.hq_x, xg), __fmul_rn(s.hq_y, yg));  // (sqrt(3)/3 x - y/3) / size
+  const float r = __fmul_rn(s.hr_y, yg);                                     // (2 y / 3) / size
+  const float sv = __fsub_rn(-q, r);
   qi = rintf(q);
   ri = rintf(r);
-  float si = rintf(sv);
-  float dq = fabsf(qi - q), dr = fabsf(ri - r), ds = fabsf(si - sv);
-  if ((dq > dr) && (dq > ds)) qi = -ri - si;
-  if ((dr > dq) && (dr > ds)) ri = -qi - si;
+  const float si = rintf(sv);
+  const float dq = fabsf(__fsub_rn(qi, q)), dr = fabsf(__fsub_rn(ri, r)), ds = fabsf(__fsub_rn(si, sv));
+  if ((dq > dr) && (dq > ds)) qi = __fsub_rn(-ri, si);
+  if ((dr > dq) && (dr > ds)) ri = __fsub_rn(-qi, si);
 }
 
 // sensors/hexagonal.py:155-172 _lookup_pixels over a table in shared memory
@@ -440,8 +441,14 @@ __device__ __forceinline__ int hex_lookup(const SensorK& s, const TT* table, flo
 
 // sensors/hexagonal.py:42-47 _hex_norm
 __device__ __forceinline__ float hex_norm(float x, float y, float inv_inr) {
-  float ax = fabsf(x), ay = fabsf(y);
-  return fmaxf(ax, 0.5f * ax + 0.8660254037844386f * ay) * inv_inr;
+  const float ax = fabsf(x), ay = fabsf(y);
+  return __fmul_rn(fmaxf(ax, __fadd_rn(__fmul_rn(0.5f, ax), __fmul_rn(0.8660254037844386f, ay))), inv_inr);
+}
+
+// lattice centre of axial cell (qi, ri) in the grid frame
+__device__ __forceinline__ void hex_centre(const SensorK& s, float qi, float ri, float& cx, float& cy) {
+  cx = __fmul_rn(s.hex_sx, __fadd_rn(qi, __fmul_rn(0.5f, ri)));
+  cy = __fmul_rn(s.hex_sy, ri);
 }
 
 // sensors/hexagonal.py:174-194 HexagonalSensor.accumulate: pixel id or -1
@@ -450,9 +457,40 @@ __device__ __forceinline__ int bin_hex(const SensorK& s, const TT* table, float 
   float xg, yg, qi, ri;
   hex_axial(s, x, y, xg, yg, qi, ri);
   int p = hex_lookup(s, table, qi, ri);
-  float hcx = s.hex_sx * (qi + 0.5f * ri);
-  float hcy = s.hex_sy * ri;
-  float hd = hex_norm(xg - hcx, yg - hcy, s.inv_inr);
+  float hcx, hcy;
+  hex_centre(s, qi, ri, hcx, hcy);
+  float hd = hex_norm(__fsub_rn(xg, hcx), __fsub_rn(yg, hcy), s.inv_inr);
+  return (hd > s.edge_threshold) ? -1 : p;
+}
+
+// The last hexagon a lane binned into: its centre (grid frame) and pixel id.
+struct HexCache {
+  float cx, cy;
+  int pid;
+};
+
+// bin_hex with a one-cell cache: a point within inradius * edge_threshold
+// - 1e-5 m of the cached cell's centre lies inside that cell (the hexagonal
+// norm never exceeds the Euclidean one over the inradius) and outside the
+// edge band, so the reference's rounding, lookup and edge test give the
+// cached id; the 1e-5 m margin covers their float32 rounding. Otherwise the
+// full path runs and refills the cache.
+template <typename TT>
+__device__ __forceinline__ int bin_hex_cached(const SensorK& s, const TT* table, float x, float y, HexCache& hc) {
+  const float xs = __fsub_rn(x, s.off_x), ys = __fsub_rn(y, s.off_y);
+  const float xg = __fsub_rn(__fmul_rn(s.gc, xs), __fmul_rn(s.gs, ys));
+  const float yg = __fadd_rn(__fmul_rn(s.gs, xs), __fmul_rn(s.gc, ys));
+  const float ex = xg - hc.cx, ey = yg - hc.cy;
+  if (ex * ex + ey * ey < s.hex_lim2) return hc.pid;
+  float xg2, yg2, qi, ri;
+  hex_axial(s, x, y, xg2, yg2, qi, ri);
+  const int p = hex_lookup(s, table, qi, ri);
+  float hcx, hcy;
+  hex_centre(s, qi, ri, hcx, hcy);
+  const float hd = hex_norm(__fsub_rn(xg2, hcx), __fsub_rn(yg2, hcy), s.inv_inr);
+  hc.cx = hcx;
+  hc.cy = hcy;
+  hc.pid = p;
   return (hd > s.edge_threshold) ? -1 : p;
 }
 

@@ -177,6 +177,8 @@ SensorK make_sensor(const iact_sensor_t* s) {
     k.hr_y = (float)(2.0 / (3.0 * sz));
   }
   k.inv_inr = s->inradius > 0.f ? (float)(1.0 / (double)s->inradius) : 0.f;
+  const double lim = (double)s->inradius * s->edge_threshold - 1e-5;
+  k.hex_lim2 = lim > 0.0 ? (float)(lim * lim) : -1.f;  // -1: the cache never hits
   return k;
 }
 

@@ -231,6 +231,9 @@ __device__ __forceinline__ void splat_square(const SensorK& s, const Sink& sink,
 }
 
 // sensors/hexagonal.py:264-315 DifferentiableHexagonalSensor.accumulate
+// (all lanes call; inactive lanes pass ok = false). The tap weights of the
+// one-ring kernel (kernel_size 1, the reference default) stay in registers
+// between the normalisation and the deposit; larger kernels recompute them.
 template <typename TT>
 __device__ __forceinline__ void splat_hex(const SensorK& s, const TT* table, const Sink& sink,
                                           int rowbase, bool ok, float x, float y, float v) {
@@ -240,6 +243,34 @@ __device__ __forceinline__ void splat_hex(const SensorK& s, const TT* table, con
   float ddx = xg - s.hex_sx * (qi + 0.5f * ri), ddy = yg - s.hex_sy * ri;
   const int K = s.kernel_size;
   const float inv_sig = 1.f / s.sigma;
+  if (K == 1) {
+    constexpr int dq[7] = {-1, -1, 0, 0, 0, 1, 1}, dr[7] = {0, 1, -1, 0, 1, -1, 0};  // the ring in (q, r) order
+    float w[7], tot = 0.f;
+#pragma unroll
+    for (int j = 0; j < 7; ++j) {
+      const float a = hex_norm(ddx - s.hex_sx * ((float)dq[j] + 0.5f * (float)dr[j]),
+                               ddy - s.hex_sy * (float)dr[j], s.inv_inr) * inv_sig;
+      w[j] = expf(-0.5f * (a * a));
+      tot += w[j];
+    }
+    const float scale = ok ? v / tot : 0.f;
+    // lookup-table index of the base hexagon; the ring is at fixed offsets
+    const float qx = qi - (float)s.q_min, rx = ri - (float)s.r_min;
+    const bool inner = ok && (qx >= 1.f) & (qx < (float)(s.table_q - 1)) & (rx >= 1.f) & (rx < (float)(s.table_r - 1));
+    const int base = inner ? (int)qx * s.table_r + (int)rx : 0;
+#pragma unroll
+    for (int j = 0; j < 7; ++j) {
+      int p;
+      if (inner) {
+        p = (int)table[base + dq[j] * s.table_r + dr[j]];
+        p = p >= 0 ? p : -1;
+      } else {
+        p = ok ? hex_lookup(s, table, qi + (float)dq[j], ri + (float)dr[j]) : -1;
+      }
+      warp_add(sink, p >= 0 ? rowbase + p : -1, w[j] * scale);
+    }
+    return;
+  }
   float tot = 0.f;
   for (int q = -K; q <= K; ++q)
     for (int r = -K; r <= K; ++r) {
@@ -342,17 +373,19 @@ __device__ __forceinline__ void bundle_axis(V3 src, float sigma, V3 c, float R0,
   }
 }
 
-// CTA-collective: candidate masks of the T tasks (source sl, facet fl,
-// chunk cl; chunk fastest) of a tile starting at (s0, f0, c0) into
-// mask[T * nw]. One thread step per (task, 32-primitive word): the task's
-// bundle is decoded once and its word assembled in a register.
+// Warp-collective: candidate masks of the warp's tasks [tb, te) (source sl,
+// facet fl, chunk cl of a tile starting at (s0, f0, c0); chunk fastest) into
+// mask[t * nw + w]. One lane per (task, 32-primitive word): the task's
+// bundle is decoded once and its word assembled in a register; no
+// CTA-wide barrier (each warp reads only its own tasks' masks).
 template <int SRC>
-__device__ __forceinline__ void tile_masks(const float4* B4, const float* sources, int M, int nw, const Obst& ob,
-                                           int s0, int f0, int c0, int FCc, int CCc, int T, uint32_t* mask) {
+__device__ __forceinline__ void warp_masks(const float4* B4, const float* sources, int M, int nw, const Obst& ob,
+                                           int s0, int f0, int c0, int FCc, int CCc, int tb, int te,
+                                           uint32_t* mask) {
   const int np = ob.n_cyl + ob.n_box + ob.n_sph + ob.n_obox + ob.n_tri;
   const int nch = (M + 31) >> 5;
   constexpr int SS = (SRC == IACT_SRC_EXTENDED) ? 4 : 3;
-  for (int i = threadIdx.x; i < T * nw; i += blockDim.x) {
+  for (int i = tb * nw + (threadIdx.x & 31); i < te * nw; i += 32) {
     const int t = i / nw, w = i - t * nw;
     const int sl = t / (FCc * CCc), rem = t - sl * FCc * CCc;
     const int fl = rem / CCc, cl = rem - fl * CCc;
@@ -369,7 +402,7 @@ __device__ __forceinline__ void tile_masks(const float4* B4, const float* source
       if (prim_may_hit(ob, k, bd)) word |= 1u << (k & 31);
     mask[i] = word;
   }
-  __syncthreads();
+  __syncwarp();
 }
 
 template <int SRC, bool SOFT, int MODE, bool STAGES>
@@ -386,9 +419,10 @@ __device__ __forceinline__ void render_tile(const RenderK& p, const Obst& ob, co
 
   int rl_key = -1;  // run-length merged hit of this lane (hard sensors)
   float rl_val = 0.f;
+  HexCache hc = {3.0e38f, 3.0e38f, -1};  // last hexagon of this lane (hard hex sensors)
   const int T = SBc * FCc * CCc;
-  if (p.n_words) tile_masks<SRC>(p.B4, p.sources, p.M, p.n_words, ob, s0, f0, c0, FCc, CCc, T, tmask);
   const int tb = (warp * T) / nw, te = ((warp + 1) * T) / nw;
+  if (p.n_words) warp_masks<SRC>(p.B4, p.sources, p.M, p.n_words, ob, s0, f0, c0, FCc, CCc, tb, te, tmask);
   // task t = (source sl, facet fl, chunk cl), chunk fastest; decoded once
   int sl = tb / (FCc * CCc);
   int fl = (tb - sl * FCc * CCc) / CCc;
@@ -418,8 +452,10 @@ __device__ __forceinline__ void render_tile(const RenderK& p, const Obst& ob, co
       else if (p.hex_in_smem) splat_hex(p.sn, htab, sink, rowbase, act, x, y, val);
       else splat_hex(p.sn, p.hex_table, sink, rowbase, act, x, y, val);
     } else if (act) {
-      const int pix = (p.sn.type == IACT_SENSOR_SQUARE) ? bin_square(p.sn, x, y)
-                      : (p.hex_in_smem ? bin_hex(p.sn, htab, x, y) : bin_hex(p.sn, p.hex_table, x, y));
+      const int pix = (p.sn.type == IACT_SENSOR_SQUARE)
+                          ? bin_square(p.sn, x, y)
+                          : (p.hex_in_smem ? bin_hex_cached(p.sn, htab, x, y, hc)
+                                           : bin_hex_cached(p.sn, p.hex_table, x, y, hc));
       if ((pix >= 0) & (val != 0.f)) {
         const int key = rowbase + pix;
         if (key == rl_key) {
