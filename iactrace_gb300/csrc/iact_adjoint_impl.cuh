@@ -217,23 +217,23 @@ __device__ __forceinline__ void stage_bwd(const float* m, const StageRec& R, V3&
   const float ndg = dot(R.nl, gnl);
   const V3 gN = R.nl.z * (gnl - ndg * R.nl);
   // surface derivatives at the hit and at the facet offset (z0)
-  const double x0 = m[12], y0 = m[13];
-  const double Xs = (double)R.pl.x + x0, Ys = (double)R.pl.y + y0;
+  const float x0 = m[12], y0 = m[13];
+  const float Xs = R.pl.x + x0, Ys = R.pl.y + y0;
   SagD D, D0;
   sag_derivs(m, Xs * Xs + Ys * Ys, D);
-  if (x0 != 0.0 || y0 != 0.0) {
+  if (x0 != 0.f || y0 != 0.f) {
     sag_derivs(m, x0 * x0 + y0 * y0, D0);
   } else {  // no offset: z0 = 0 for every parameter value
-    D0.S = D0.Sr = D0.Srr = D0.Sc = D0.Sk = D0.Src = D0.Srk = 0.0;
+    D0.S = D0.Sr = D0.Srr = D0.Sc = D0.Sk = D0.Src = D0.Srk = 0.f;
 #pragma unroll
-    for (int i = 0; i < 8; ++i) D0.Sa[i] = D0.Sra[i] = 0.0;
+    for (int i = 0; i < 8; ++i) D0.Sa[i] = D0.Sra[i] = 0.f;
   }
-  const double sX = 2.0 * Xs * D.Sr, sY = 2.0 * Ys * D.Sr;
-  const double sXX = 2.0 * D.Sr + 4.0 * Xs * Xs * D.Srr, sXY = 4.0 * Xs * Ys * D.Srr, sYY = 2.0 * D.Sr + 4.0 * Ys * Ys * D.Srr;
-  double gX = -(gN.x * sXX + gN.y * sXY), gY = -(gN.x * sXY + gN.y * sYY);
-  const double wN = -(2.0 * Xs * gN.x + 2.0 * Ys * gN.y);  // dL/dS_rho through the normal
-  double gth_c = wN * D.Src, gth_k = wN * D.Srk;
-  double gth_a[8];
+  const float sX = 2.f * Xs * D.Sr, sY = 2.f * Ys * D.Sr;
+  const float sXX = 2.f * D.Sr + 4.f * Xs * Xs * D.Srr, sXY = 4.f * Xs * Ys * D.Srr, sYY = 2.f * D.Sr + 4.f * Ys * Ys * D.Srr;
+  float gX = -(gN.x * sXX + gN.y * sXY), gY = -(gN.x * sXY + gN.y * sYY);
+  const float wN = -(2.f * Xs * gN.x + 2.f * Ys * gN.y);  // dL/dS_rho through the normal
+  float gth_c = wN * D.Src, gth_k = wN * D.Srk;
+  float gth_a[8];
 #pragma unroll
   for (int i = 0; i < 8; ++i) gth_a[i] = wN * D.Sra[i];
   // pl = (X, Y, S(rho) - S(rho0))
@@ -245,14 +245,14 @@ __device__ __forceinline__ void stage_bwd(const float* m, const StageRec& R, V3&
   for (int i = 0; i < 8; ++i) gth_a[i] += gpl.z * (D.Sa[i] - D0.Sa[i]);
   // X = ol_x + t dl_x, Y = ol_y + t dl_y ; t implicit
   const V3 ol = rtmul(Rj, R.o - Pj), dl = rtmul(Rj, R.r);
-  V3 gol = mk((float)gX, (float)gY, 0.f);
-  V3 gdl = mk((float)(R.t * gX), (float)(R.t * gY), 0.f);
-  const double gt = gX * dl.x + gY * dl.y;
-  const double Gt = -sX * dl.x - sY * dl.y + dl.z;
-  const double lam = gt * rcp_d(Gt);
-  const V3 Nv = mk((float)-sX, (float)-sY, 1.f);
-  gol = gol - (float)lam * Nv;
-  gdl = gdl - (float)(lam * R.t) * Nv;
+  V3 gol = mk(gX, gY, 0.f);
+  V3 gdl = mk(R.t * gX, R.t * gY, 0.f);
+  const float gt = gX * dl.x + gY * dl.y;
+  const float Gt = -sX * dl.x - sY * dl.y + dl.z;
+  const float lam = gt / Gt;
+  const V3 Nv = mk(-sX, -sY, 1.f);
+  gol = gol - lam * Nv;
+  gdl = gdl - (lam * R.t) * Nv;
   gth_c += lam * (D.Sc - D0.Sc);
   gth_k += lam * (D.Sk - D0.Sk);
 #pragma unroll
@@ -271,10 +271,10 @@ __device__ __forceinline__ void stage_bwd(const float* m, const StageRec& R, V3&
 #pragma unroll
   for (int i = 0; i < 9; ++i) g[i] = gR[i];
   g[9] = gP.x; g[10] = gP.y; g[11] = gP.z;
-  g[12] = (float)gth_c;
-  g[13] = (float)gth_k;
+  g[12] = gth_c;
+  g[13] = gth_k;
 #pragma unroll
-  for (int i = 0; i < 8; ++i) g[14 + i] = (float)gth_a[i];
+  for (int i = 0; i < 8; ++i) g[14 + i] = gth_a[i];
 }
 
 // One work tile (source block, facet chunk, 32-sample chunk) of the

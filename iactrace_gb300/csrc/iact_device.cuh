@@ -25,7 +25,7 @@ constexpr int kBoxF = 6;    // min(3) max(3)
 constexpr int kSphF = 4;    // center(3) r*r
 constexpr int kOboxF = 15;  // center(3) half(3) R(9) row-major local->world
 constexpr int kTriF = 9;    // v0(3) e1(3) e2(3)
-constexpr int kMirF = 52;   // see MirRec
+constexpr int kMirF = 56;   // see MirRec
 
 // One stage >= 1 mirror, as laid out in shared memory (floats).
 struct MirRec {
@@ -44,11 +44,17 @@ struct MirRec {
   float k;          // 23  conic constant
   float asph[8];    // 24..31
   float vert[16];   // 32..47
-  float z0_hi;      // 48  sag at the offset (FP64 value as hi + lo floats)
-  float z0_lo;      // 49
-  float pad[2];     // 50..51
+  double z0;        // 48..49 sag at the offset (FP64)
+  double c_d;       // 50..51 curvature (FP64)
+  double alpha_d;   // 52..53 (1+k) c c (FP64)
+  double kp1_d;     // 54..55 1 + conic (FP64)
 };
 static_assert(sizeof(MirRec) == kMirF * sizeof(float), "MirRec layout");
+// FP64 fields of a mirror record (records start on 16-byte boundaries)
+enum MirD { kMirZ0 = 0, kMirC = 1, kMirAlpha = 2, kMirKp1 = 3 };
+__host__ __device__ __forceinline__ double mir_d(const float* m, MirD f) {
+  return reinterpret_cast<const double*>(m + 48)[f];
+}
 
 // Hardware approximations (PTX rcp.approx / sqrt.approx, <= 1 ulp-ish).
 // Used where the value only feeds a hit/miss comparison or a sensor-plane
@@ -515,26 +521,23 @@ __device__ __forceinline__ double sag_raw_d(const float* m, double r2) {
   return z;
 }
 // FP64 reciprocal and reciprocal square root: the hardware float32
-// approximations refined by two Newton-Raphson steps each (y' = y + y e,
+// approximations (relative error below 2^-22.9, plus 2^-24 from rounding the
+// argument to float32) refined by one Newton-Raphson step each (y' = y + y e,
 // e = 1 - x y, and y' = y + y e / 2, e = 1 - x y^2; the classic iterations,
-// e.g. Muller et al., Handbook of Floating-Point Arithmetic, ch. 5): each step
-// squares the relative error, 2e-7 -> 1e-13 -> below the double rounding.
+// e.g. Muller et al., Handbook of Floating-Point Arithmetic, ch. 5). A step
+// maps a relative error eps to eps^2 (reciprocal) and 1.5 eps^2 (reciprocal
+// square root): about 4e-14 here, which sets the sag to 1e-14 m at metre
+// scale, six orders below the 1e-8 Newton tolerance and the float32 outputs.
 // Arguments must be normal float32 numbers (the callers guard the ranges).
 __device__ __forceinline__ double rcp_d(double x) {
-  double y = (double)rcp_a((float)x);
-  double e = fma(-x, y, 1.0);
-  y = fma(y, e, y);
-  e = fma(-x, y, 1.0);
-  return fma(y, e, y);
+  const double y = (double)rcp_a((float)x);
+  return fma(y, fma(-x, y, 1.0), y);
 }
 __device__ __forceinline__ double rsqrt_d(double x) {
   float xf = (float)x, yf;
   asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(yf) : "f"(xf));
-  double y = yf;
-  double e = fma(-x * y, y, 1.0);
-  y = fma(0.5 * y, e, y);
-  e = fma(-x * y, y, 1.0);
-  return fma(0.5 * y, e, y);
+  const double y = yf;
+  return fma(0.5 * y, fma(-x * y, y, 1.0), y);
 }
 // sqrt(x) for x >= 0 (0 -> 0), NaN for x < 0 as the IEEE square root
 __device__ __forceinline__ double sqrt_d(double x) {
@@ -545,7 +548,7 @@ __device__ __forceinline__ double sqrt_d(double x) {
 // root, one reciprocal): S = c r2 / (1 + q) + sum a_i r2^(2(i+1)),
 // dS/dr2 = c / (1 + q) + c alpha r2 / (2 q (1 + q)^2) + sum ..., q = sqrt(1 - alpha r2)
 __device__ __forceinline__ void sag_eval_d(const float* m, double r2, double& S, double& dS) {
-  const double c = m[15], alpha = (1.0 + (double)m[23]) * c * c;
+  const double c = mir_d(m, kMirC), alpha = mir_d(m, kMirAlpha);
   const double qq = fma(-alpha, r2, 1.0);
   const double rq = qq > 0.0 ? rsqrt_d(qq) : (qq == 0.0 ? __longlong_as_double(0x7ff0000000000000ll)
                                                        : __longlong_as_double(0x7ff8000000000000ll));
@@ -573,7 +576,7 @@ __device__ __forceinline__ void sag_eval_d(const float* m, double r2, double& S,
 // core/intersections.py:229-285 intersect_conic (on the raw-frame origin)
 __device__ __forceinline__ double conic_t(const float* m, double ox, double oy, double oz, double dx,
                                           double dy, double dz) {
-  double c = m[15], kp = 1.0 + (double)m[23];
+  const double c = mir_d(m, kMirC), kp = mir_d(m, kMirKp1);
   double A = c * (dx * dx + dy * dy + kp * dz * dz);
   double B = 2.0 * (c * (ox * dx + oy * dy + kp * oz * dz) - dz);
   double C = c * (ox * ox + oy * oy + kp * oz * oz) - 2.0 * oz;
@@ -596,33 +599,45 @@ __device__ __forceinline__ double conic_t(const float* m, double ox, double oy, 
 // root is found in FP64 (the sag at z0, the conic start, the Newton steps,
 // the residual); the Newton step divides by a float32 reciprocal of g'
 // (it still converges to the FP64 root); the unit normal is float32.
+// As in the reference, the step taken at the first evaluation with
+// |g| < 1e-8 is still applied. When that last step is below 1e-7 the
+// residual at the returned t is second order in it (far below 1e-6, so the
+// hit is valid) and the sag there is the last evaluation's S moved to first
+// order, S + S'(r2 - r2_last); otherwise (no convergence, or a large last
+// step at a grazing ray) the surface is evaluated again at t.
 __device__ __forceinline__ float mirror_hit(const float* m, V3 o, V3 d, V3& pl, V3& nl) {
   const float inf = __int_as_float(0x7f800000);
   const double x0 = m[12], y0 = m[13];
-  const double z0 = (double)m[48] + (double)m[49];
+  const double z0 = mir_d(m, kMirZ0);
   const double ox = o.x, oy = o.y, oz = o.z, dx = d.x, dy = d.y, dz = d.z;
   double t = conic_t(m, ox + x0, oy + y0, oz + z0, dx, dy, dz);
   bool conv = false;
+  double S = 0.0, dS = 0.0, r2e = 0.0, step = 0.0;
   for (int it = 0; it < 10; ++it) {
     if (!conv) {
       const double xs = fma(t, dx, ox) + x0, ys = fma(t, dy, oy) + y0;
-      const double r2 = xs * xs + ys * ys;
-      double S, dS;
-      sag_eval_d(m, r2, S, dS);
+      r2e = xs * xs + ys * ys;
+      sag_eval_d(m, r2e, S, dS);
       const double g = fma(t, dz, oz) - (S - z0);
       const double gp = dz - 2.0 * dS * (xs * dx + ys * dy);
       const double gs = (fabs(gp) > 1e-12) ? gp : 1e-12;
       conv = fabs(g) < 1e-8;
-      t = t - g * (double)rcp_a((float)gs);
+      step = g * (double)rcp_a((float)gs);
+      t = t - step;
     }
   }
   const double xh = fma(t, dx, ox), yh = fma(t, dy, oy);
   const double xs = xh + x0, ys = yh + y0;
-  double S, dS;
-  sag_eval_d(m, xs * xs + ys * ys, S, dS);
+  const double r2 = xs * xs + ys * ys;
+  bool valid;
+  if (conv && fabs(step) < 1e-7) {
+    S = fma(dS, r2 - r2e, S);
+    valid = t > 1e-8;
+  } else {
+    sag_eval_d(m, r2, S, dS);
+    valid = (t > 1e-8) && (fabs(fma(t, dz, oz) - (S - z0)) < 1e-6);
+  }
   const double zs = S - z0;
-  const double res = fabs(fma(t, dz, oz) - zs);
-  const bool valid = (t > 1e-8) && (res < 1e-6);
   const float nx = (float)(-2.0 * dS * xs), ny = (float)(-2.0 * dS * ys);
   const float inn = rsqrtf(fmaf(nx, nx, fmaf(ny, ny, 1.f)));
   pl = mk((float)xh, (float)yh, (float)zs);
@@ -687,41 +702,41 @@ namespace iact {
 //   S_c = rho/(1+q) + (1+k) c^2 rho^2 / (q (1+q)^2),  S_k = c^3 rho^2 / (2 q (1+q)^2)
 //   S_rho,c = 1/(2q) + (1+k) c^2 rho / (2 q^3),       S_rho,k = c^3 rho / (4 q^3)
 //   S_a_i = rho^p_i,  S_rho,a_i = p_i rho^(p_i - 1)
+// float32: these are derivatives at a known hit, sums of positive-scale
+// terms without the cancellation of the root's residual (the root itself is
+// FP64, mirror_hit).
 struct SagD {
-  double S, Sr, Srr, Sc, Sk, Src, Srk;
-  double Sa[8], Sra[8];
+  float S, Sr, Srr, Sc, Sk, Src, Srk;
+  float Sa[8], Sra[8];
 };
 
-__device__ __forceinline__ void sag_derivs(const float* m, double rho, SagD& o) {
-  const double c = m[15], k = m[23];
-  const double al = (1.0 + k) * c * c;
-  const double qq = fma(-al, rho, 1.0);
-  // one reciprocal square root and one reciprocal (Newton-refined, FP64)
-  // replace the square root and the divisions of the closed forms
-  const double iq = qq > 0.0 ? rsqrt_d(qq) : (qq == 0.0 ? __longlong_as_double(0x7ff0000000000000ll)
-                                                       : __longlong_as_double(0x7ff8000000000000ll));
-  const double q = qq > 0.0 ? qq * iq : (qq == 0.0 ? 0.0 : iq);
-  const double iq3 = iq * iq * iq, iopq = rcp_d(1.0 + q), iopq2 = iopq * iopq;
+__device__ __forceinline__ void sag_derivs(const float* m, float rho, SagD& o) {
+  const float c = m[15], al = m[17];
+  const float qq = fmaf(-al, rho, 1.f);
+  const float iq = qq > 0.f ? rsqrtf(qq) : (qq == 0.f ? __int_as_float(0x7f800000) : __int_as_float(0x7fc00000));
+  const float q = qq > 0.f ? qq * iq : (qq == 0.f ? 0.f : iq);
+  const float iq3 = iq * iq * iq, iopq = 1.f / (1.f + q), iopq2 = iopq * iopq;
   o.S = c * rho * iopq;
-  o.Sr = 0.5 * c * iq;
-  o.Srr = 0.25 * c * al * iq3;
+  o.Sr = 0.5f * c * iq;
+  o.Srr = 0.25f * c * al * iq3;
   o.Sc = rho * iopq + al * rho * rho * iq * iopq2;
-  o.Sk = 0.5 * c * c * c * rho * rho * iq * iopq2;
-  o.Src = 0.5 * iq + 0.5 * al * rho * iq3;
-  o.Srk = 0.25 * c * c * c * rho * iq3;
+  o.Sk = 0.5f * c * c * c * rho * rho * iq * iopq2;
+  o.Src = 0.5f * iq + 0.5f * al * rho * iq3;
+  o.Srk = 0.25f * c * c * c * rho * iq3;
   const int na = (int)m[19];
+#pragma unroll
   for (int i = 0; i < 8; ++i) {
-    o.Sa[i] = 0.0;
-    o.Sra[i] = 0.0;
+    o.Sa[i] = 0.f;
+    o.Sra[i] = 0.f;
   }
-  double rp = rho * rho;  // rho^p, p = 2
-  double rpm1 = rho;      // rho^(p-1)
-  double rpm2 = 1.0;      // rho^(p-2)
+  float rp = rho * rho;  // rho^p, p = 2
+  float rpm1 = rho;      // rho^(p-1)
+  float rpm2 = 1.f;      // rho^(p-2)
   for (int i = 0; i < na; ++i) {
-    const double p = 2.0 * (i + 1), a = m[24 + i];
+    const float p = 2.f * (i + 1), a = m[24 + i];
     o.S += a * rp;
     o.Sr += a * p * rpm1;
-    o.Srr += a * p * (p - 1.0) * rpm2;
+    o.Srr += a * p * (p - 1.f) * rpm2;
     o.Sa[i] = rp;
     o.Sra[i] = p * rpm1;
     rp *= rho * rho;
