@@ -544,103 +544,126 @@ __device__ __forceinline__ double sqrt_d(double x) {
   return x > 0.0 ? x * rsqrt_d(x) : (x == 0.0 ? 0.0 : __longlong_as_double(0x7ff8000000000000ll));
 }
 
-// core/surfaces.py:25-39 _sag_raw and its r2-derivative together (one square
-// root, one reciprocal): S = c r2 / (1 + q) + sum a_i r2^(2(i+1)),
-// dS/dr2 = c / (1 + q) + c alpha r2 / (2 q (1 + q)^2) + sum ..., q = sqrt(1 - alpha r2)
-__device__ __forceinline__ void sag_eval_d(const float* m, double r2, double& S, double& dS) {
+// core/surfaces.py:25-39 _sag_raw on the Newton path: S in FP64, dS/dr2 in
+// float32 (it only scales the Newton step and sets the float32 normal).
+// One square root and one reciprocal, FP64 by one Newton-Raphson step from
+// the float32 approximations (rsqrt_d, rcp_d); outside the conic's domain
+// (1 - alpha r2 < 0) S is NaN and at its edge (= 0) the IEEE limits.
+__device__ __forceinline__ double sag_s_d(const float* m, double r2, float& dS) {
   const double c = mir_d(m, kMirC), alpha = mir_d(m, kMirAlpha);
   const double qq = fma(-alpha, r2, 1.0);
   const double rq = qq > 0.0 ? rsqrt_d(qq) : (qq == 0.0 ? __longlong_as_double(0x7ff0000000000000ll)
                                                        : __longlong_as_double(0x7ff8000000000000ll));
   const double q = qq > 0.0 ? qq * rq : (qq == 0.0 ? 0.0 : rq);
   const double id = rcp_d(1.0 + q);
-  const double cid = c * id;
-  S = r2 * cid;
-  dS = cid + 0.5 * (r2 * alpha) * cid * id * rq;
+  double S = r2 * (c * id);
+  const float cf = m[15], idf = (float)id, r2f = (float)r2;
+  float d = cf * idf + 0.5f * (r2f * m[17]) * cf * idf * idf * (float)rq;
   const int na = (int)m[19];
   if (na > 0) {
     const double r4 = r2 * r2;
-    double p = r4, pm1 = r2, sa = 0.0, sd = 0.0;  // a_i r2^p, p a_i r2^(p-1), p = 2(i+1)
+    const float r4f = r2f * r2f;
+    double p = r4, sa = 0.0;  // a_i r2^p, p = 2(i+1)
+    float pm1 = r2f, sd = 0.f;  // p a_i r2^(p-1)
     for (int i = 0; i < na; ++i) {
-      const double a = m[24 + i];
-      sa = fma(a, p, sa);
-      sd = fma(a * (double)(2 * (i + 1)), pm1, sd);
+      const float a = m[24 + i];
+      sa = fma((double)a, p, sa);
+      sd = fmaf(a * (float)(2 * (i + 1)), pm1, sd);
       p *= r4;
-      pm1 *= r4;
+      pm1 *= r4f;
     }
     S += sa;
-    dS += sd;
+    d += sd;
   }
+  dS = d;
+  return S;
 }
 
-// core/intersections.py:229-285 intersect_conic (on the raw-frame origin)
-__device__ __forceinline__ double conic_t(const float* m, double ox, double oy, double oz, double dx,
-                                          double dy, double dz) {
-  const double c = mir_d(m, kMirC), kp = mir_d(m, kMirKp1);
-  double A = c * (dx * dx + dy * dy + kp * dz * dz);
-  double B = 2.0 * (c * (ox * dx + oy * dy + kp * oz * dz) - dz);
-  double C = c * (ox * ox + oy * oy + kp * oz * oz) - 2.0 * oz;
-  const double inf = __longlong_as_double(0x7ff0000000000000ll);
-  if (fabs(c) < 1e-12) return (fabs(dz) > 1e-10) ? -oz / dz : inf;
-  double disc = B * B - 4.0 * A * C;
-  if (disc < 0.0) return inf;
-  double sq = sqrt_d(disc);
-  const double den = 2.0 * A + 1e-30;
-  const double iden = fabs(den) > 1e-37 ? rcp_d(den) : 1.0 / den;
-  double t1 = (-B - sq) * iden, t2 = (-B + sq) * iden;
-  bool v1 = t1 > 1e-8, v2 = t2 > 1e-8;
-  return (v1 && v2) ? fmin(t1, t2) : (v1 ? t1 : (v2 ? t2 : inf));
+// core/intersections.py:229-285 intersect_conic, on the raw-frame origin:
+// the roots in float32 by the cancellation-free form (q = -(B + sign(B)
+// sqrt(disc)) / 2, roots q / A and C / q), the smallest above 1e-8, then one
+// FP64 Newton step on the conic's implicit function
+// Q(t) = c (x^2 + y^2 + (1+k) z^2) - 2 z, which squares the float32 root's
+// error: the FP64 conic root. +inf (or NaN) when the ray misses the conic.
+__device__ __forceinline__ double conic_start(const float* m, float oxf, float oyf, float ozf, V3 d, double ox,
+                                              double oy, double oz) {
+  const float inf = __int_as_float(0x7f800000);
+  const float c = m[15], kp = m[16];
+  float t;
+  if (fabsf(c) < 1e-12f) {  // plane
+    t = (fabsf(d.z) > 1e-10f) ? -ozf * rcp_a(d.z) : inf;
+  } else {
+    const float A = c * (d.x * d.x + d.y * d.y + kp * d.z * d.z);
+    const float B = 2.f * (c * (oxf * d.x + oyf * d.y + kp * ozf * d.z) - d.z);
+    const float C = c * (oxf * oxf + oyf * oyf + kp * ozf * ozf) - 2.f * ozf;
+    const float disc = B * B - 4.f * A * C;
+    const float qv = -0.5f * (B + copysignf(sqrtf(fmaxf(disc, 0.f)), B));
+    const float t1 = qv * rcp_a(A), t2 = C * rcp_a(qv);
+    const bool v1 = t1 > 1e-8f, v2 = t2 > 1e-8f;
+    t = (disc < 0.f) ? inf : ((v1 && v2) ? fminf(t1, t2) : (v1 ? t1 : (v2 ? t2 : inf)));
+  }
+  if (!(t < inf)) return (double)t;
+  const double td = t;
+  const double x = fma(td, (double)d.x, ox), y = fma(td, (double)d.y, oy), z = fma(td, (double)d.z, oz);
+  const double Q = mir_d(m, kMirC) * fma(x, x, fma(y, y, mir_d(m, kMirKp1) * z * z)) - 2.0 * z;
+  const float xf = fmaf(t, d.x, oxf), yf = fmaf(t, d.y, oyf), zf = fmaf(t, d.z, ozf);
+  const float Qp = 2.f * (c * (xf * d.x + yf * d.y + kp * zf * d.z) - d.z);
+  return (fabsf(Qp) > 1e-12f) ? td - Q * (double)rcp_a(Qp) : td;
 }
 
 // core/surfaces.py:67-108 AsphericSurface.intersect + core/intersections.py:290-367
 // newton_raphson_intersect (10 steps, tol 1e-8, valid if t > 1e-8 and
 // |g| < 1e-6). Local frame in, local point and unit normal out; returns t or
-// +inf when invalid or outside the aperture (core/render.py:100-101). The
-// root is found in FP64 (the sag at z0, the conic start, the Newton steps,
-// the residual); the Newton step divides by a float32 reciprocal of g'
-// (it still converges to the FP64 root); the unit normal is float32.
-// As in the reference, the step taken at the first evaluation with
-// |g| < 1e-8 is still applied. When that last step is below 1e-7 the
-// residual at the returned t is second order in it (far below 1e-6, so the
-// hit is valid) and the sag there is the last evaluation's S moved to first
-// order, S + S'(r2 - r2_last); otherwise (no convergence, or a large last
-// step at a grazing ray) the surface is evaluated again at t.
+// +inf when invalid or outside the aperture (core/render.py:100-101).
+// The root is FP64: the conic start (conic_start), the residual g and the
+// sag; g' is float32 (it only scales the step: the iteration still
+// converges to the FP64 root) and so is the unit normal. As in the
+// reference, the step taken at the first evaluation with |g| < 1e-8 is still
+// applied; when that step is below 1e-7 the residual at the returned t is
+// second order in it (far below 1e-6: valid) and the sag there is the last
+// evaluation's moved to first order, S + S'(r2 - r2_last); otherwise (no
+// convergence, or a large last step at a grazing ray) the surface is
+// evaluated again at t. A NaN start or residual stays NaN through every
+// later step in the reference: the ray is invalid and the iteration stops.
 __device__ __forceinline__ float mirror_hit(const float* m, V3 o, V3 d, V3& pl, V3& nl) {
   const float inf = __int_as_float(0x7f800000);
-  const double x0 = m[12], y0 = m[13];
-  const double z0 = mir_d(m, kMirZ0);
-  const double ox = o.x, oy = o.y, oz = o.z, dx = d.x, dy = d.y, dz = d.z;
-  double t = conic_t(m, ox + x0, oy + y0, oz + z0, dx, dy, dz);
+  const double x0 = m[12], y0 = m[13], z0 = mir_d(m, kMirZ0);
+  // origin in the raw surface frame (core/surfaces.py:86-91)
+  const double ox = (double)o.x + x0, oy = (double)o.y + y0, oz = (double)o.z + z0;
+  const double dx = d.x, dy = d.y, dz = d.z;
+  double t = conic_start(m, o.x + m[12], o.y + m[13], o.z + (float)z0, d, ox, oy, oz);
+  bool live = fabs(t) <= 1.79e308;  // finite
   bool conv = false;
-  double S = 0.0, dS = 0.0, r2e = 0.0, step = 0.0;
-  for (int it = 0; it < 10; ++it) {
-    if (!conv) {
-      const double xs = fma(t, dx, ox) + x0, ys = fma(t, dy, oy) + y0;
-      r2e = xs * xs + ys * ys;
-      sag_eval_d(m, r2e, S, dS);
-      const double g = fma(t, dz, oz) - (S - z0);
-      const double gp = dz - 2.0 * dS * (xs * dx + ys * dy);
-      const double gs = (fabs(gp) > 1e-12) ? gp : 1e-12;
-      conv = fabs(g) < 1e-8;
-      step = g * (double)rcp_a((float)gs);
-      t = t - step;
-    }
+  double S = 0.0, r2e = 0.0, step = 0.0;
+  float dS = 0.f;
+  for (int it = 0; it < 10 && live && !conv; ++it) {
+    const double xs = fma(t, dx, ox), ys = fma(t, dy, oy);
+    r2e = fma(xs, xs, ys * ys);
+    S = sag_s_d(m, r2e, dS);
+    const double g = fma(t, dz, oz) - S;
+    const float gp = d.z - 2.f * dS * ((float)xs * d.x + (float)ys * d.y);
+    const float gs = (fabsf(gp) > 1e-12f) ? gp : 1e-12f;
+    conv = fabs(g) < 1e-8;
+    live = !isnan(g);
+    step = g * (double)rcp_a(gs);
+    t = t - step;
   }
-  const double xh = fma(t, dx, ox), yh = fma(t, dy, oy);
-  const double xs = xh + x0, ys = yh + y0;
-  const double r2 = xs * xs + ys * ys;
+  const double xs = fma(t, dx, ox), ys = fma(t, dy, oy);
+  const double r2 = fma(xs, xs, ys * ys);
   bool valid;
-  if (conv && fabs(step) < 1e-7) {
-    S = fma(dS, r2 - r2e, S);
+  if (!live) {
+    valid = false;
+  } else if (conv && fabs(step) < 1e-7) {
+    S = fma((double)dS, r2 - r2e, S);
     valid = t > 1e-8;
   } else {
-    sag_eval_d(m, r2, S, dS);
-    valid = (t > 1e-8) && (fabs(fma(t, dz, oz) - (S - z0)) < 1e-6);
+    S = sag_s_d(m, r2, dS);
+    valid = (t > 1e-8) && (fabs(fma(t, dz, oz) - S) < 1e-6);
   }
-  const double zs = S - z0;
-  const float nx = (float)(-2.0 * dS * xs), ny = (float)(-2.0 * dS * ys);
+  const float xsf = (float)xs, ysf = (float)ys;
+  const float nx = -2.f * dS * xsf, ny = -2.f * dS * ysf;
   const float inn = rsqrtf(fmaf(nx, nx, fmaf(ny, ny, 1.f)));
-  pl = mk((float)xh, (float)yh, (float)zs);
+  pl = mk((float)(xs - x0), (float)(ys - y0), (float)(S - z0));
   nl = mk(nx * inn, ny * inn, inn);
   // telescope/mirrors.py:147-149 disk, :209-220 polygon check_aperture
   bool in_ap;
