@@ -32,7 +32,7 @@ struct MirRec {
   float R[9];       // 0..8  local->world rotation
   float pos[3];     // 9..11
   float off[2];     // 12..13
-  float unused14;   // 14
+  float z0f;        // 14  z0 rounded to float32
   float c;          // 15  curvature
   float kp1;        // 16  1 + conic (float32)
   float alpha;      // 17  (1+k) c c (float32)
@@ -544,120 +544,180 @@ __device__ __forceinline__ double sqrt_d(double x) {
   return x > 0.0 ? x * rsqrt_d(x) : (x == 0.0 ? 0.0 : __longlong_as_double(0x7ff8000000000000ll));
 }
 
-// core/surfaces.py:25-39 _sag_raw on the Newton path: S in FP64, dS/dr2 in
-// float32 (it only scales the Newton step and sets the float32 normal).
-// One square root and one reciprocal, FP64 by one Newton-Raphson step from
-// the float32 approximations (rsqrt_d, rcp_d); outside the conic's domain
-// (1 - alpha r2 < 0) S is NaN and at its edge (= 0) the IEEE limits.
-__device__ __forceinline__ double sag_s_d(const float* m, double r2, float& dS) {
-  const double c = mir_d(m, kMirC), alpha = mir_d(m, kMirAlpha);
-  const double qq = fma(-alpha, r2, 1.0);
-  const double rq = qq > 0.0 ? rsqrt_d(qq) : (qq == 0.0 ? __longlong_as_double(0x7ff0000000000000ll)
-                                                       : __longlong_as_double(0x7ff8000000000000ll));
-  const double q = qq > 0.0 ? qq * rq : (qq == 0.0 ? 0.0 : rq);
-  const double id = rcp_d(1.0 + q);
-  double S = r2 * (c * id);
-  const float cf = m[15], idf = (float)id, r2f = (float)r2;
-  float d = cf * idf + 0.5f * (r2f * m[17]) * cf * idf * idf * (float)rq;
+// core/surfaces.py:25-39 _sag_raw and its r2-derivatives. With
+// q = sqrt(1 - alpha r2), alpha = (1+k) c^2:
+//   S = c r2 / (1 + q) + sum_i a_i r2^(2(i+1)),  S' = c / (2q) + ...,  S'' = c alpha / (4 q^3) + ...
+// float32 version: the first Newton phase of mirror_hit.
+__device__ __forceinline__ float sag_f(const float* m, float r2, float& dS) {
+  const float c = m[15];
+  const float qq = fmaf(-m[17], r2, 1.f);
+  const float rq = rsqrtf(qq);
+  float S = c * r2 * rcp_a(fmaf(qq, rq, 1.f));
+  float d = 0.5f * c * rq;
   const int na = (int)m[19];
   if (na > 0) {
-    const double r4 = r2 * r2;
-    const float r4f = r2f * r2f;
-    double p = r4, sa = 0.0;  // a_i r2^p, p = 2(i+1)
-    float pm1 = r2f, sd = 0.f;  // p a_i r2^(p-1)
+    const float r4 = r2 * r2;
+    float p = r4, pm1 = r2;
     for (int i = 0; i < na; ++i) {
       const float a = m[24 + i];
-      sa = fma((double)a, p, sa);
-      sd = fmaf(a * (float)(2 * (i + 1)), pm1, sd);
+      S = fmaf(a, p, S);
+      d = fmaf(a * (float)(2 * (i + 1)), pm1, d);
       p *= r4;
-      pm1 *= r4f;
+      pm1 *= r4;
     }
-    S += sa;
-    d += sd;
   }
   dS = d;
   return S;
 }
 
-// core/intersections.py:229-285 intersect_conic, on the raw-frame origin:
-// the roots in float32 by the cancellation-free form (q = -(B + sign(B)
-// sqrt(disc)) / 2, roots q / A and C / q), the smallest above 1e-8, then one
-// FP64 Newton step on the conic's implicit function
-// Q(t) = c (x^2 + y^2 + (1+k) z^2) - 2 z, which squares the float32 root's
-// error: the FP64 conic root. +inf (or NaN) when the ray misses the conic.
-__device__ __forceinline__ double conic_start(const float* m, float oxf, float oyf, float ozf, V3 d, double ox,
-                                              double oy, double oz) {
+// FP64 version: S in FP64 (one square root and one reciprocal, FP64 by one
+// Newton-Raphson step from the float32 approximations, as rsqrt_d / rcp_d),
+// S' and S'' in float32 from the same approximations (they scale the Newton
+// step, bound its remainder and set the float32 normal). Outside the
+// conic's domain (1 - alpha r2 < 0) S is NaN; at its edge q = 0.
+__device__ __forceinline__ double sag_s_d(const float* m, double r2, float r2f, float& dS, float& Srr,
+                                          float& qqf) {
+  const double c = mir_d(m, kMirC), alpha = mir_d(m, kMirAlpha);
+  const double qq = fma(-alpha, r2, 1.0);
+  qqf = (float)qq;
+  float yf;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(yf) : "f"(qqf));
+  const double y = yf;
+  const bool pos = qqf > 0.f, zero = qqf == 0.f;
+  const double q = pos ? qq * fma(0.5 * y, fma(-qq * y, y, 1.0), y)
+                       : (zero ? 0.0 : __longlong_as_double(0x7ff8000000000000ll));
+  const float rqf = pos ? yf : (zero ? __int_as_float(0x7f800000) : __int_as_float(0x7fc00000));
+  const double op = 1.0 + q;
+  const double z = rcp_a((float)op);
+  const double id = fma(z, fma(-op, z, 1.0), z);
+  double S = r2 * (c * id);
+  const float cf = m[15];
+  float d = 0.5f * cf * rqf;
+  float dd = 0.25f * cf * m[17] * rqf * rqf * rqf;
+  const int na = (int)m[19];
+  if (na > 0) {
+    const double r4 = r2 * r2;
+    const float r4f = r2f * r2f;
+    double p = r4, sa = 0.0;          // a_i r2^p, p = 2(i+1)
+    float pm1 = r2f, pm2 = 1.f;       // r2^(p-1), r2^(p-2)
+    for (int i = 0; i < na; ++i) {
+      const float a = m[24 + i], pf = (float)(2 * (i + 1));
+      sa = fma((double)a, p, sa);
+      d = fmaf(a * pf, pm1, d);
+      dd = fmaf(a * pf * (pf - 1.f), pm2, dd);
+      p *= r4;
+      pm1 *= r4f;
+      pm2 *= r4f;
+    }
+    S += sa;
+  }
+  dS = d;
+  Srr = dd;
+  return S;
+}
+
+// core/intersections.py:229-285 intersect_conic on the raw-frame origin, in
+// float32 by the cancellation-free form (q = -(B + sign(B) sqrt(disc)) / 2,
+// roots q / A and C / q): the smallest root above 1e-8, +inf (or NaN) when
+// the ray misses the conic.
+__device__ __forceinline__ float conic_start(const float* m, float ox, float oy, float oz, V3 d) {
   const float inf = __int_as_float(0x7f800000);
   const float c = m[15], kp = m[16];
-  float t;
-  if (fabsf(c) < 1e-12f) {  // plane
-    t = (fabsf(d.z) > 1e-10f) ? -ozf * rcp_a(d.z) : inf;
-  } else {
-    const float A = c * (d.x * d.x + d.y * d.y + kp * d.z * d.z);
-    const float B = 2.f * (c * (oxf * d.x + oyf * d.y + kp * ozf * d.z) - d.z);
-    const float C = c * (oxf * oxf + oyf * oyf + kp * ozf * ozf) - 2.f * ozf;
-    const float disc = B * B - 4.f * A * C;
-    const float qv = -0.5f * (B + copysignf(sqrtf(fmaxf(disc, 0.f)), B));
-    const float t1 = qv * rcp_a(A), t2 = C * rcp_a(qv);
-    const bool v1 = t1 > 1e-8f, v2 = t2 > 1e-8f;
-    t = (disc < 0.f) ? inf : ((v1 && v2) ? fminf(t1, t2) : (v1 ? t1 : (v2 ? t2 : inf)));
-  }
-  if (!(t < inf)) return (double)t;
-  const double td = t;
-  const double x = fma(td, (double)d.x, ox), y = fma(td, (double)d.y, oy), z = fma(td, (double)d.z, oz);
-  const double Q = mir_d(m, kMirC) * fma(x, x, fma(y, y, mir_d(m, kMirKp1) * z * z)) - 2.0 * z;
-  const float xf = fmaf(t, d.x, oxf), yf = fmaf(t, d.y, oyf), zf = fmaf(t, d.z, ozf);
-  const float Qp = 2.f * (c * (xf * d.x + yf * d.y + kp * zf * d.z) - d.z);
-  return (fabsf(Qp) > 1e-12f) ? td - Q * (double)rcp_a(Qp) : td;
+  if (fabsf(c) < 1e-12f) return (fabsf(d.z) > 1e-10f) ? -oz * rcp_a(d.z) : inf;  // plane
+  const float A = c * (d.x * d.x + d.y * d.y + kp * d.z * d.z);
+  const float B = 2.f * (c * (ox * d.x + oy * d.y + kp * oz * d.z) - d.z);
+  const float C = c * (ox * ox + oy * oy + kp * oz * oz) - 2.f * oz;
+  const float disc = B * B - 4.f * A * C;
+  const float qv = -0.5f * (B + copysignf(sqrtf(fmaxf(disc, 0.f)), B));
+  const float t1 = qv * rcp_a(A), t2 = C * rcp_a(qv);
+  const bool v1 = t1 > 1e-8f, v2 = t2 > 1e-8f;
+  return (disc < 0.f) ? inf : ((v1 && v2) ? fminf(t1, t2) : (v1 ? t1 : (v2 ? t2 : inf)));
 }
 
 // core/surfaces.py:67-108 AsphericSurface.intersect + core/intersections.py:290-367
-// newton_raphson_intersect (10 steps, tol 1e-8, valid if t > 1e-8 and
-// |g| < 1e-6). Local frame in, local point and unit normal out; returns t or
-// +inf when invalid or outside the aperture (core/render.py:100-101).
-// The root is FP64: the conic start (conic_start), the residual g and the
-// sag; g' is float32 (it only scales the step: the iteration still
-// converges to the FP64 root) and so is the unit normal. As in the
-// reference, the step taken at the first evaluation with |g| < 1e-8 is still
-// applied; when that step is below 1e-7 the residual at the returned t is
-// second order in it (far below 1e-6: valid) and the sag there is the last
-// evaluation's moved to first order, S + S'(r2 - r2_last); otherwise (no
-// convergence, or a large last step at a grazing ray) the surface is
-// evaluated again at t. A NaN start or residual stays NaN through every
+// newton_raphson_intersect (conic start, 10 steps, tol 1e-8, valid if
+// t > 1e-8 and |g| < 1e-6). Local frame in, local point and unit normal
+// out; returns t or +inf when invalid or outside the aperture
+// (core/render.py:100-101). g(t) = o_z + t d_z - sag(o_xy + t d_xy).
+//   1. conic start and Newton steps in float32 while the steps exceed the
+//      float32 resolution (1e-5): the conic root may lie on the quadric's
+//      other sheet, metres from the surface, and these steps carry t across.
+//   2. Newton steps in FP64 (g and the sag in FP64, g' in float32: it only
+//      scales the step, the iteration still converges to the FP64 root),
+//      with the reference's test |g| < 1e-8 (the step at the first
+//      evaluation that passes it is still applied, as in the reference).
+//      Where a step from a failing evaluation leaves a residual
+//      |g''| step^2 / 2 below 1e-9 |g'| (step below 1e-4, inside the domain),
+//      the evaluation the reference makes next passes the test and moves t
+//      by less than 1e-9: the iteration ends there.
+//   3. After a final step below 1e-4 the sag and its slope at t are the last
+//      evaluation's moved by Taylor steps in r2 (residual far below 1e-6:
+//      valid); otherwise the surface is evaluated again at t.
+// The float32 steps and the residual bound change t by far less than the
+// float32 resolution of the outputs. A NaN residual stays NaN through every
 // later step in the reference: the ray is invalid and the iteration stops.
 __device__ __forceinline__ float mirror_hit(const float* m, V3 o, V3 d, V3& pl, V3& nl) {
   const float inf = __int_as_float(0x7f800000);
-  const double x0 = m[12], y0 = m[13], z0 = mir_d(m, kMirZ0);
   // origin in the raw surface frame (core/surfaces.py:86-91)
+  const float oxf = o.x + m[12], oyf = o.y + m[13], ozf = o.z + m[14];
+  float tf = conic_start(m, oxf, oyf, ozf, d);
+  bool live = fabsf(tf) < inf;
+  int it = 0;
+  if (live) {
+    for (; it < 8; ++it) {
+      const float xs = fmaf(tf, d.x, oxf), ys = fmaf(tf, d.y, oyf);
+      float dSf;
+      const float Sf = sag_f(m, fmaf(xs, xs, ys * ys), dSf);
+      const float g = fmaf(tf, d.z, ozf) - Sf;
+      const float gp = d.z - 2.f * dSf * (xs * d.x + ys * d.y);
+      const float st = g * rcp_a((fabsf(gp) > 1e-12f) ? gp : 1e-12f);
+      if (!(fabsf(st) < inf)) break;  // keep the last finite t: the FP64 phase decides
+      tf -= st;
+      if (fabsf(st) < 1e-5f) {
+        ++it;
+        break;
+      }
+    }
+  }
+  const double x0 = m[12], y0 = m[13], z0 = mir_d(m, kMirZ0);
   const double ox = (double)o.x + x0, oy = (double)o.y + y0, oz = (double)o.z + z0;
   const double dx = d.x, dy = d.y, dz = d.z;
-  double t = conic_start(m, o.x + m[12], o.y + m[13], o.z + (float)z0, d, ox, oy, oz);
-  bool live = fabs(t) <= 1.79e308;  // finite
+  double t = tf, S = 0.0, r2e = 0.0;
+  float dS = 0.f, Srr = 0.f, stepf = 0.f;
   bool conv = false;
-  double S = 0.0, r2e = 0.0, step = 0.0;
-  float dS = 0.f;
-  for (int it = 0; it < 10 && live && !conv; ++it) {
+  for (; it < 10 && live && !conv; ++it) {
     const double xs = fma(t, dx, ox), ys = fma(t, dy, oy);
     r2e = fma(xs, xs, ys * ys);
-    S = sag_s_d(m, r2e, dS);
-    const double g = fma(t, dz, oz) - S;
-    const float gp = d.z - 2.f * dS * ((float)xs * d.x + (float)ys * d.y);
+    const float xsf = (float)xs, ysf = (float)ys;
+    float qqf;
+    S = sag_s_d(m, r2e, fmaf(xsf, xsf, ysf * ysf), dS, Srr, qqf);
+    const float g = (float)(fma(t, dz, oz) - S);
+    const float w = xsf * d.x + ysf * d.y;
+    const float gp = d.z - 2.f * dS * w;
     const float gs = (fabsf(gp) > 1e-12f) ? gp : 1e-12f;
-    conv = fabs(g) < 1e-8;
+    conv = fabsf(g) < 1e-8f;
     live = !isnan(g);
-    step = g * (double)rcp_a(gs);
-    t = t - step;
+    stepf = g * rcp_a(gs);
+    t -= (double)stepf;
+    if (!conv) {
+      const float gpp = fabsf(2.f * dS * (d.x * d.x + d.y * d.y) + 4.f * Srr * w * w);
+      conv = (fabsf(stepf) < 1e-4f) && (qqf > 1e-2f) && (0.5f * gpp * stepf * stepf < 1e-9f * fabsf(gs));
+    }
   }
   const double xs = fma(t, dx, ox), ys = fma(t, dy, oy);
   const double r2 = fma(xs, xs, ys * ys);
   bool valid;
   if (!live) {
     valid = false;
-  } else if (conv && fabs(step) < 1e-7) {
-    S = fma((double)dS, r2 - r2e, S);
+  } else if (conv && fabsf(stepf) < 1e-4f) {
+    const double dr2 = r2 - r2e;
+    const float dr2f = (float)dr2;
+    S = fma((double)fmaf(0.5f * Srr, dr2f, dS), dr2, S);
+    dS = fmaf(Srr, dr2f, dS);
     valid = t > 1e-8;
   } else {
-    S = sag_s_d(m, r2, dS);
+    float qqf;
+    S = sag_s_d(m, r2, (float)r2, dS, Srr, qqf);
     valid = (t > 1e-8) && (fabs(fma(t, dz, oz) - S) < 1e-6);
   }
   const float xsf = (float)xs, ysf = (float)ys;

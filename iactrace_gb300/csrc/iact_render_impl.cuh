@@ -81,7 +81,6 @@ __device__ __forceinline__ void prep_tables(const PrepK& p) {
     euler_to_matrix(m.rot[0], m.rot[1], m.rot[2], o);
     o[9] = m.pos[0]; o[10] = m.pos[1]; o[11] = m.pos[2];
     o[12] = m.offset[0]; o[13] = m.offset[1];
-    o[14] = 0.f;
     o[15] = m.curvature;
     o[16] = 1.f + m.conic;
     o[17] = (1.f + m.conic) * m.curvature * m.curvature;
@@ -103,6 +102,7 @@ __device__ __forceinline__ void prep_tables(const PrepK& p) {
     od[kMirC] = (double)m.curvature;
     od[kMirKp1] = 1.0 + (double)m.conic;
     od[kMirAlpha] = od[kMirKp1] * od[kMirC] * od[kMirC];
+    o[14] = (float)od[kMirZ0];
   }
 }
 
