@@ -174,6 +174,38 @@ __device__ __forceinline__ void soft_hex_bwd(const SensorK& s, const TT* table, 
 
 constexpr int kMaxAdjStages = 2;
 
+// Adds each lane's stage-mirror gradient terms g (mirror j; j < 0: none)
+// into the CTA's shared sums. Warp-collective (all 32 lanes). When every
+// contributing lane hit the same mirror, a butterfly reduce-scatter over the
+// 32 lanes (31 shuffles) leaves lane i with the warp's sum of term i and
+// lanes 0..kMirGrad-1 add one term each (distinct addresses); otherwise
+// each lane adds its own terms.
+__device__ __forceinline__ void warp_add_mirror_grads(float* mgrad, int j, const float (&g)[kMirGrad], int lane) {
+  const unsigned any = __ballot_sync(kFull, j >= 0);
+  if (any == 0u) return;
+  const int j0 = __shfl_sync(kFull, j, __ffs(any) - 1);
+  if (__all_sync(kFull, j < 0 || j == j0)) {
+    float v[32];
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = (i < kMirGrad && j >= 0) ? g[i] : 0.f;
+#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1) {
+      const bool hi = (lane & off) != 0;
+#pragma unroll
+      for (int i = 0; i < off; ++i) {
+        const float send = hi ? v[i] : v[i + off];
+        const float keep = hi ? v[i + off] : v[i];
+        v[i] = keep + __shfl_xor_sync(kFull, send, off);
+      }
+    }
+    if (lane < kMirGrad && v[0] != 0.f) atomicAdd(mgrad + j0 * kMirGrad + lane, v[0]);
+  } else if (j >= 0) {
+#pragma unroll
+    for (int i = 0; i < kMirGrad; ++i)
+      if (g[i] != 0.f) atomicAdd(mgrad + j * kMirGrad + i, g[i]);
+  }
+}
+
 // One stage >= 1 reflection as recorded by the forward re-trace.
 struct StageRec {
   V3 o, r;      // incoming ray (world)
@@ -322,8 +354,13 @@ __device__ __forceinline__ void adjoint_tile(const AdjK& p, const Obst& ob, cons
     const float v = __ldg(p.values + s);
     const V3 fpos = mk(__ldg(p.facet_pos + 3 * f), __ldg(p.facet_pos + 3 * f + 1), __ldg(p.facet_pos + 3 * f + 2));
     const int rowbase = (MODE == IACT_MODE_RESPONSE) ? s * p.P : 0;
-    if (m < p.M) {
-      const size_t si = (size_t)f * p.M + m;
+    // with stage mirrors, lanes past the chunk's last sample run the body on
+    // a clamped sample with no contribution, so the warp stays converged for
+    // the collective stage-mirror sums
+    const bool ok = m < p.M;
+    const int mc = ok ? m : p.M - 1;
+    if (STAGES || ok) {
+      const size_t si = (size_t)f * p.M + mc;
       const float4 P4 = __ldg(p.P4 + si), N4 = __ldg(p.N4 + si);
       const V3 tp = mk(P4.x, P4.y, P4.z), nn = mk(N4.x, N4.y, N4.z);
       const float iw = P4.w;
@@ -336,7 +373,7 @@ __device__ __forceinline__ void adjoint_tile(const AdjK& p, const Obst& ob, cons
         d = inv_len * w;
       } else if (SRC == IACT_SRC_EXTENDED) {  // jitter regenerated from its counter
         float z0, z1;
-        ray_normals(p.seed, s, f, m, z0, z1);
+        ray_normals(p.seed, s, f, mc, z0, z1);
         d = jitter_dir(rsqrtf(dot(src, src)) * src, __ldg(p.sources + SS * s + 3), z0, z1);
       } else {
         d = src;
@@ -348,7 +385,7 @@ __device__ __forceinline__ void adjoint_tile(const AdjK& p, const Obst& ob, cons
       // later stages, recorded for the reverse sweep (core/render.py:44-79)
       StageRec rec[kMaxAdjStages];
       int nst = 0;
-      bool alive = !shadowed;
+      bool alive = ok && !shadowed;
       V3 o = tp, r = r0;
       float val = val0;
       if (STAGES) {
@@ -405,23 +442,32 @@ __device__ __forceinline__ void adjoint_tile(const AdjK& p, const Obst& ob, cons
           gval = pix >= 0 ? __ldg(p.grad_out + rowbase + pix) : 0.f;
         }
       }
-      if ((gval != 0.f) | (gx != 0.f) | (gy != 0.f)) {
+      const bool act = (gval != 0.f) | (gx != 0.f) | (gy != 0.f);
+      V3 a = mk(0.f, 0.f, 0.f), gr = mk(0.f, 0.f, 0.f);
+      float gv0 = gval;
+      if (act) {
         // plane (intersections.py:23-35): p = o + t r, t = ns.(C - o) / ns.r
         V3 gpl = gx * u1 + gy * u2;  // dL/dp
         const float dLdt = dot(gpl, r);
-        V3 a = gpl - (dLdt * inv_nd) * ns;               // dL/do through the plane
-        V3 gr = tpl * gpl - (dLdt * tpl * inv_nd) * ns;  // dL/dr through the plane
-        float gv0 = gval;
-        if (STAGES) {
-          for (int k = nst - 1; k >= 0; --k) {
-            float gm[kMirGrad];
+        a = gpl - (dLdt * inv_nd) * ns;               // dL/do through the plane
+        gr = tpl * gpl - (dLdt * tpl * inv_nd) * ns;  // dL/dr through the plane
+      }
+      if (STAGES) {  // warp-converged: the mirror sums are warp-collective
+        const int kmax = __reduce_max_sync(kFull, act ? nst : 0);
+        for (int k = kmax - 1; k >= 0; --k) {
+          float gm[kMirGrad];
+          int j = -1;
+          if (act && k < nst) {
             stage_bwd(mir + rec[k].j * kMirF, rec[k], a, gr, gv0, gm);
-            float* dst = mgrad + rec[k].j * kMirGrad;
+            j = rec[k].j;
+          } else {
 #pragma unroll
-            for (int i = 0; i < kMirGrad; ++i)
-              if (gm[i] != 0.f) atomicAdd(dst + i, gm[i]);
+            for (int i = 0; i < kMirGrad; ++i) gm[i] = 0.f;
           }
+          warp_add_mirror_grads(mgrad, j, gm, lane);
         }
+      }
+      if (act) {
         // val = v (-c) iw ; r = d - 2 c n'
         const float dLdc = -gv0 * v * iw - 2.f * dot(gr, nn);
         const V3 b = (-2.f * c) * gr + dLdc * d;  // dL/dn'
