@@ -25,14 +25,14 @@ constexpr int kBoxF = 6;    // min(3) max(3)
 constexpr int kSphF = 4;    // center(3) r*r
 constexpr int kOboxF = 15;  // center(3) half(3) R(9) row-major local->world
 constexpr int kTriF = 9;    // v0(3) e1(3) e2(3)
-constexpr int kMirF = 56;   // see MirRec
+constexpr int kMirF = 52;   // see MirRec
 
 // One stage >= 1 mirror, as laid out in shared memory (floats).
 struct MirRec {
   float R[9];       // 0..8  local->world rotation
   float pos[3];     // 9..11
   float off[2];     // 12..13
-  float z0f;        // 14  z0 rounded to float32
+  float unused14;   // 14
   float c;          // 15  curvature
   float kp1;        // 16  1 + conic (float32)
   float alpha;      // 17  (1+k) c c (float32)
@@ -44,17 +44,53 @@ struct MirRec {
   float k;          // 23  conic constant
   float asph[8];    // 24..31
   float vert[16];   // 32..47
-  double z0;        // 48..49 sag at the offset (FP64)
-  double c_d;       // 50..51 curvature (FP64)
-  double alpha_d;   // 52..53 (1+k) c c (FP64)
-  double kp1_d;     // 54..55 1 + conic (FP64)
+  float z0_hi;      // 48  sag at the offset (FP64 value as a float pair hi + lo)
+  float z0_lo;      // 49
+  float alpha_hi;   // 50  (1+k) c c (FP64 value as a float pair)
+  float alpha_lo;   // 51
 };
 static_assert(sizeof(MirRec) == kMirF * sizeof(float), "MirRec layout");
-// FP64 fields of a mirror record (records start on 16-byte boundaries)
-enum MirD { kMirZ0 = 0, kMirC = 1, kMirAlpha = 2, kMirKp1 = 3 };
-__host__ __device__ __forceinline__ double mir_d(const float* m, MirD f) {
-  return reinterpret_cast<const double*>(m + 48)[f];
+
+// ------------------------------------------------- double-float arithmetic
+// A value hi + lo held as two float32 (|lo| <= ulp(hi) / 2): about 48
+// significant bits, computed on the FP32 pipe. Error-free transformations
+// (Knuth's two-sum, Dekker's fast two-sum, the FMA two-product) and the
+// double-float add / multiply built on them (Dekker 1971; Hida, Li and
+// Bailey, "Library for double-double and quad-double arithmetic", 2007:
+// the "sloppy" add, whose error is about 2^-47 (|a| + |b|)). Written with
+// round-to-nearest intrinsics so that no step is contracted or reordered.
+struct FF {
+  float hi, lo;
+};
+__device__ __forceinline__ FF ff_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
 }
+__device__ __forceinline__ FF ff_fast_two_sum(float a, float b) {  // |a| >= |b| or a = 0
+  const float s = __fadd_rn(a, b);
+  return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+  const FF s = ff_two_sum(a.hi, b.hi);
+  return ff_fast_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
+}
+__device__ __forceinline__ FF ff_add_f(FF a, float b) {
+  const FF s = ff_two_sum(a.hi, b);
+  return ff_fast_two_sum(s.hi, __fadd_rn(s.lo, a.lo));
+}
+__device__ __forceinline__ FF ff_neg(FF a) { return {-a.hi, -a.lo}; }
+__device__ __forceinline__ FF ff_mul(FF a, FF b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  const float e = __fmaf_rn(a.hi, b.hi, -p);
+  return ff_fast_two_sum(p, __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, e)));
+}
+__device__ __forceinline__ FF ff_mul_f(FF a, float b) {
+  const float p = __fmul_rn(a.hi, b);
+  const float e = __fmaf_rn(a.hi, b, -p);
+  return ff_fast_two_sum(p, __fmaf_rn(a.lo, b, e));
+}
+__device__ __forceinline__ float ff_f(FF a) { return __fadd_rn(a.hi, a.lo); }
 
 // Hardware approximations (PTX rcp.approx / sqrt.approx, <= 1 ulp-ish).
 // Used where the value only feeds a hit/miss comparison or a sensor-plane
@@ -520,30 +556,6 @@ __device__ __forceinline__ double sag_raw_d(const float* m, double r2) {
   }
   return z;
 }
-// FP64 reciprocal and reciprocal square root: the hardware float32
-// approximations (relative error below 2^-22.9, plus 2^-24 from rounding the
-// argument to float32) refined by one Newton-Raphson step each (y' = y + y e,
-// e = 1 - x y, and y' = y + y e / 2, e = 1 - x y^2; the classic iterations,
-// e.g. Muller et al., Handbook of Floating-Point Arithmetic, ch. 5). A step
-// maps a relative error eps to eps^2 (reciprocal) and 1.5 eps^2 (reciprocal
-// square root): about 4e-14 here, which sets the sag to 1e-14 m at metre
-// scale, six orders below the 1e-8 Newton tolerance and the float32 outputs.
-// Arguments must be normal float32 numbers (the callers guard the ranges).
-__device__ __forceinline__ double rcp_d(double x) {
-  const double y = (double)rcp_a((float)x);
-  return fma(y, fma(-x, y, 1.0), y);
-}
-__device__ __forceinline__ double rsqrt_d(double x) {
-  float xf = (float)x, yf;
-  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(yf) : "f"(xf));
-  const double y = yf;
-  return fma(0.5 * y, fma(-x * y, y, 1.0), y);
-}
-// sqrt(x) for x >= 0 (0 -> 0), NaN for x < 0 as the IEEE square root
-__device__ __forceinline__ double sqrt_d(double x) {
-  return x > 0.0 ? x * rsqrt_d(x) : (x == 0.0 ? 0.0 : __longlong_as_double(0x7ff8000000000000ll));
-}
-
 // core/surfaces.py:25-39 _sag_raw and its r2-derivatives. With
 // q = sqrt(1 - alpha r2), alpha = (1+k) c^2:
 //   S = c r2 / (1 + q) + sum_i a_i r2^(2(i+1)),  S' = c / (2q) + ...,  S'' = c alpha / (4 q^3) + ...
@@ -570,46 +582,50 @@ __device__ __forceinline__ float sag_f(const float* m, float r2, float& dS) {
   return S;
 }
 
-// FP64 version: S in FP64 (one square root and one reciprocal, FP64 by one
-// Newton-Raphson step from the float32 approximations, as rsqrt_d / rcp_d),
-// S' and S'' in float32 from the same approximations (they scale the Newton
-// step, bound its remainder and set the float32 normal). Outside the
-// conic's domain (1 - alpha r2 < 0) S is NaN; at its edge q = 0.
-__device__ __forceinline__ double sag_s_d(const float* m, double r2, float r2f, float& dS, float& Srr,
-                                          float& qqf) {
-  const double c = mir_d(m, kMirC), alpha = mir_d(m, kMirAlpha);
-  const double qq = fma(-alpha, r2, 1.0);
-  qqf = (float)qq;
-  float yf;
-  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(yf) : "f"(qqf));
-  const double y = yf;
-  const bool pos = qqf > 0.f, zero = qqf == 0.f;
-  const double q = pos ? qq * fma(0.5 * y, fma(-qq * y, y, 1.0), y)
-                       : (zero ? 0.0 : __longlong_as_double(0x7ff8000000000000ll));
-  const float rqf = pos ? yf : (zero ? __int_as_float(0x7f800000) : __int_as_float(0x7fc00000));
-  const double op = 1.0 + q;
-  const double z = rcp_a((float)op);
-  const double id = fma(z, fma(-op, z, 1.0), z);
-  double S = r2 * (c * id);
-  const float cf = m[15];
-  float d = 0.5f * cf * rqf;
-  float dd = 0.25f * cf * m[17] * rqf * rqf * rqf;
+// Double-float version: S to about 1e-13 relative (the square root and the
+// reciprocal from the float32 approximations plus one Newton-Raphson
+// correction each, y' = y + y (1 - x y) and q' = q + (x - q^2) / (2q): the
+// error 2^-22 squares to 2^-44), S' and S'' in float32 from the same
+// approximations (they scale the Newton step, bound its remainder and set
+// the float32 normal). Outside the conic's domain (1 - alpha r2 < 0) S is
+// NaN; at its edge q = 0.
+__device__ __forceinline__ FF sag_ff(const float* m, FF r2, float& dS, float& Srr, float& qqf) {
+  const float c = m[15];
+  const FF qq = ff_add_f(ff_neg(ff_mul(FF{m[50], m[51]}, r2)), 1.f);
+  qqf = ff_f(qq);
+  float y;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(qq.hi));
+  const bool pos = qq.hi > 0.f, zero = qq.hi == 0.f;
+  // q = sqrt(qq): q0 = qq y, corrected by (qq - q0^2) y / 2
+  const float q0 = __fmul_rn(qq.hi, y);
+  const FF rsd = ff_add(qq, ff_neg(FF{__fmul_rn(q0, q0), __fmaf_rn(q0, q0, -__fmul_rn(q0, q0))}));
+  FF q = ff_fast_two_sum(q0, __fmul_rn(ff_f(rsd), __fmul_rn(0.5f, y)));
+  if (!pos) q = FF{zero ? 0.f : __int_as_float(0x7fc00000), 0.f};
+  const float rq = pos ? y : (zero ? __int_as_float(0x7f800000) : __int_as_float(0x7fc00000));
+  // id = 1 / (1 + q): z0 = rcp(op), corrected by z0 (1 - op z0)
+  const FF op = ff_add_f(q, 1.f);
+  const float z0 = rcp_a(op.hi);
+  const float pz = __fmul_rn(op.hi, z0);
+  const float ez = __fsub_rn(__fsub_rn(__fsub_rn(1.f, pz), __fmaf_rn(op.hi, z0, -pz)), __fmul_rn(op.lo, z0));
+  const FF id = ff_fast_two_sum(z0, __fmul_rn(z0, ez));
+  FF S = ff_mul(r2, ff_mul_f(id, c));
+  float d = 0.5f * c * rq;
+  float dd = 0.25f * c * m[17] * rq * rq * rq;
   const int na = (int)m[19];
   if (na > 0) {
-    const double r4 = r2 * r2;
-    const float r4f = r2f * r2f;
-    double p = r4, sa = 0.0;          // a_i r2^p, p = 2(i+1)
-    float pm1 = r2f, pm2 = 1.f;       // r2^(p-1), r2^(p-2)
+    const FF r4 = ff_mul(r2, r2);
+    const float r2f = ff_f(r2), r4f = r2f * r2f;
+    FF p = r4;                    // r2^p, p = 2(i+1)
+    float pm1 = r2f, pm2 = 1.f;   // r2^(p-1), r2^(p-2)
     for (int i = 0; i < na; ++i) {
       const float a = m[24 + i], pf = (float)(2 * (i + 1));
-      sa = fma((double)a, p, sa);
+      S = ff_add(S, ff_mul_f(p, a));
       d = fmaf(a * pf, pm1, d);
       dd = fmaf(a * pf * (pf - 1.f), pm2, dd);
-      p *= r4;
+      p = ff_mul(p, r4);
       pm1 *= r4f;
       pm2 *= r4f;
     }
-    S += sa;
   }
   dS = d;
   Srr = dd;
@@ -659,7 +675,7 @@ __device__ __forceinline__ float conic_start(const float* m, float ox, float oy,
 __device__ __forceinline__ float mirror_hit(const float* m, V3 o, V3 d, V3& pl, V3& nl) {
   const float inf = __int_as_float(0x7f800000);
   // origin in the raw surface frame (core/surfaces.py:86-91)
-  const float oxf = o.x + m[12], oyf = o.y + m[13], ozf = o.z + m[14];
+  const float oxf = o.x + m[12], oyf = o.y + m[13], ozf = o.z + m[48];
   float tf = conic_start(m, oxf, oyf, ozf, d);
   bool live = fabsf(tf) < inf;
   int it = 0;
@@ -679,51 +695,58 @@ __device__ __forceinline__ float mirror_hit(const float* m, V3 o, V3 d, V3& pl, 
       }
     }
   }
-  const double x0 = m[12], y0 = m[13], z0 = mir_d(m, kMirZ0);
-  const double ox = (double)o.x + x0, oy = (double)o.y + y0, oz = (double)o.z + z0;
-  const double dx = d.x, dy = d.y, dz = d.z;
-  double t = tf, S = 0.0, r2e = 0.0;
-  float dS = 0.f, Srr = 0.f, stepf = 0.f;
+  // origin in the raw frame as exact float pairs
+  const FF ox = ff_two_sum(o.x, m[12]), oy = ff_two_sum(o.y, m[13]);
+  const FF oz = ff_add_f(FF{m[48], m[49]}, o.z);
+  FF t = {tf, 0.f}, S = {0.f, 0.f}, xs = {0.f, 0.f}, ys = {0.f, 0.f};
+  float dS = 0.f, Srr = 0.f, stepf = 0.f, w = 0.f;
   bool conv = false;
   for (; it < 10 && live && !conv; ++it) {
-    const double xs = fma(t, dx, ox), ys = fma(t, dy, oy);
-    r2e = fma(xs, xs, ys * ys);
-    const float xsf = (float)xs, ysf = (float)ys;
+    xs = ff_add(ox, ff_mul_f(t, d.x));
+    ys = ff_add(oy, ff_mul_f(t, d.y));
     float qqf;
-    S = sag_s_d(m, r2e, fmaf(xsf, xsf, ysf * ysf), dS, Srr, qqf);
-    const float g = (float)(fma(t, dz, oz) - S);
-    const float w = xsf * d.x + ysf * d.y;
+    S = sag_ff(m, ff_add(ff_mul(xs, xs), ff_mul(ys, ys)), dS, Srr, qqf);
+    const float g = ff_f(ff_add(ff_add(oz, ff_mul_f(t, d.z)), ff_neg(S)));
+    w = xs.hi * d.x + ys.hi * d.y;
     const float gp = d.z - 2.f * dS * w;
     const float gs = (fabsf(gp) > 1e-12f) ? gp : 1e-12f;
     conv = fabsf(g) < 1e-8f;
     live = !isnan(g);
     stepf = g * rcp_a(gs);
-    t -= (double)stepf;
+    t = ff_add_f(t, -stepf);
     if (!conv) {
       const float gpp = fabsf(2.f * dS * (d.x * d.x + d.y * d.y) + 4.f * Srr * w * w);
       conv = (fabsf(stepf) < 1e-4f) && (qqf > 1e-2f) && (0.5f * gpp * stepf * stepf < 1e-9f * fabsf(gs));
     }
   }
-  const double xs = fma(t, dx, ox), ys = fma(t, dy, oy);
-  const double r2 = fma(xs, xs, ys * ys);
   bool valid;
+  float px, py, pz;
   if (!live) {
     valid = false;
+    px = py = pz = 0.f;
   } else if (conv && fabsf(stepf) < 1e-4f) {
-    const double dr2 = r2 - r2e;
-    const float dr2f = (float)dr2;
-    S = fma((double)fmaf(0.5f * Srr, dr2f, dS), dr2, S);
-    dS = fmaf(Srr, dr2f, dS);
-    valid = t > 1e-8;
+    // r2(t) - r2(t + step) for the last step, then Taylor steps of S and S'
+    const float dr2 = stepf * (stepf * (d.x * d.x + d.y * d.y) - 2.f * w);
+    S = ff_add_f(S, fmaf(0.5f * Srr, dr2, dS) * dr2);
+    dS = fmaf(Srr, dr2, dS);
+    px = fmaf(-stepf, d.x, ff_f(ff_add_f(xs, -m[12])));
+    py = fmaf(-stepf, d.y, ff_f(ff_add_f(ys, -m[13])));
+    valid = t.hi > 1e-8f;
   } else {
+    xs = ff_add(ox, ff_mul_f(t, d.x));
+    ys = ff_add(oy, ff_mul_f(t, d.y));
     float qqf;
-    S = sag_s_d(m, r2, (float)r2, dS, Srr, qqf);
-    valid = (t > 1e-8) && (fabs(fma(t, dz, oz) - S) < 1e-6);
+    S = sag_ff(m, ff_add(ff_mul(xs, xs), ff_mul(ys, ys)), dS, Srr, qqf);
+    const float g = ff_f(ff_add(ff_add(oz, ff_mul_f(t, d.z)), ff_neg(S)));
+    px = ff_f(ff_add_f(xs, -m[12]));
+    py = ff_f(ff_add_f(ys, -m[13]));
+    valid = (t.hi > 1e-8f) && (fabsf(g) < 1e-6f);
   }
-  const float xsf = (float)xs, ysf = (float)ys;
+  pz = ff_f(ff_add(S, FF{-m[48], -m[49]}));
+  const float xsf = px + m[12], ysf = py + m[13];
   const float nx = -2.f * dS * xsf, ny = -2.f * dS * ysf;
   const float inn = rsqrtf(fmaf(nx, nx, fmaf(ny, ny, 1.f)));
-  pl = mk((float)(xs - x0), (float)(ys - y0), (float)(S - z0));
+  pl = mk(px, py, pz);
   nl = mk(nx * inn, ny * inn, inn);
   // telescope/mirrors.py:147-149 disk, :209-220 polygon check_aperture
   bool in_ap;
@@ -739,7 +762,7 @@ __device__ __forceinline__ float mirror_hit(const float* m, V3 o, V3 d, V3& pl, 
       in_ap = in_ap && (cr >= 0.f);
     }
   }
-  return (valid && in_ap) ? (float)t : inf;
+  return (valid && in_ap) ? ff_f(t) : inf;
 }
 
 // Offsets (floats) of the record groups inside the table region.

@@ -95,14 +95,15 @@ __device__ __forceinline__ void prep_tables(const PrepK& p) {
       o[32 + 2 * a] = a < m.n_vert ? m.vert[a][0] : 0.f;
       o[33 + 2 * a] = a < m.n_vert ? m.vert[a][1] : 0.f;
     }
-    // FP64 constants: the sag at the offset (core/surfaces.py:41-45 z0),
-    // the curvature, (1+k) c^2 and 1+k
-    double* od = reinterpret_cast<double*>(o + 48);
-    od[kMirZ0] = sag_raw_d(o, (double)m.offset[0] * m.offset[0] + (double)m.offset[1] * m.offset[1]);
-    od[kMirC] = (double)m.curvature;
-    od[kMirKp1] = 1.0 + (double)m.conic;
-    od[kMirAlpha] = od[kMirKp1] * od[kMirC] * od[kMirC];
-    o[14] = (float)od[kMirZ0];
+    // the sag at the offset (core/surfaces.py:41-45 z0) and (1+k) c^2, FP64,
+    // stored as float pairs hi + lo
+    o[14] = 0.f;
+    const double z0 = sag_raw_d(o, (double)m.offset[0] * m.offset[0] + (double)m.offset[1] * m.offset[1]);
+    const double al = (1.0 + (double)m.conic) * (double)m.curvature * (double)m.curvature;
+    o[48] = (float)z0;
+    o[49] = (float)(z0 - (double)o[48]);
+    o[50] = (float)al;
+    o[51] = (float)(al - (double)o[50]);
   }
 }
 
