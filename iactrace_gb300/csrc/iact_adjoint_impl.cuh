@@ -257,24 +257,17 @@ __device__ __forceinline__ void stage_bwd(const float* m, const StageRec& R, V3&
     sag_derivs(m, x0 * x0 + y0 * y0, D0);
   } else {  // no offset: z0 = 0 for every parameter value
     D0.S = D0.Sr = D0.Srr = D0.Sc = D0.Sk = D0.Src = D0.Srk = 0.f;
-#pragma unroll
-    for (int i = 0; i < 8; ++i) D0.Sa[i] = D0.Sra[i] = 0.f;
   }
   const float sX = 2.f * Xs * D.Sr, sY = 2.f * Ys * D.Sr;
   const float sXX = 2.f * D.Sr + 4.f * Xs * Xs * D.Srr, sXY = 4.f * Xs * Ys * D.Srr, sYY = 2.f * D.Sr + 4.f * Ys * Ys * D.Srr;
   float gX = -(gN.x * sXX + gN.y * sXY), gY = -(gN.x * sXY + gN.y * sYY);
   const float wN = -(2.f * Xs * gN.x + 2.f * Ys * gN.y);  // dL/dS_rho through the normal
   float gth_c = wN * D.Src, gth_k = wN * D.Srk;
-  float gth_a[8];
-#pragma unroll
-  for (int i = 0; i < 8; ++i) gth_a[i] = wN * D.Sra[i];
   // pl = (X, Y, S(rho) - S(rho0))
   gX += gpl.x + gpl.z * sX;
   gY += gpl.y + gpl.z * sY;
   gth_c += gpl.z * (D.Sc - D0.Sc);
   gth_k += gpl.z * (D.Sk - D0.Sk);
-#pragma unroll
-  for (int i = 0; i < 8; ++i) gth_a[i] += gpl.z * (D.Sa[i] - D0.Sa[i]);
   // X = ol_x + t dl_x, Y = ol_y + t dl_y ; t implicit
   const V3 ol = rtmul(Rj, R.o - Pj), dl = rtmul(Rj, R.r);
   V3 gol = mk(gX, gY, 0.f);
@@ -287,8 +280,23 @@ __device__ __forceinline__ void stage_bwd(const float* m, const StageRec& R, V3&
   gdl = gdl - (lam * R.t) * Nv;
   gth_c += lam * (D.Sc - D0.Sc);
   gth_k += lam * (D.Sk - D0.Sk);
+  // aspheric terms: dS/da_i = rho^p - rho0^p, dS_rho/da_i = p rho^(p-1), p = 2(i+1)
+  float gth_a[8];
+  {
+    const int na = (int)m[19];
+    const float rho = Xs * Xs + Ys * Ys, rho0 = x0 * x0 + y0 * y0, kz = gpl.z + lam;
+    float rp = rho * rho, rpm1 = rho, rp0 = rho0 * rho0;
 #pragma unroll
-  for (int i = 0; i < 8; ++i) gth_a[i] += lam * (D.Sa[i] - D0.Sa[i]);
+    for (int i = 0; i < 8; ++i) {
+      gth_a[i] = 0.f;
+      if (i < na) {
+        gth_a[i] = wN * (2.f * (i + 1)) * rpm1 + kz * (rp - rp0);
+        rp *= rho * rho;
+        rpm1 *= rho * rho;
+        rp0 *= rho0 * rho0;
+      }
+    }
+  }
   (void)ol;
   // ol = Rj^T (o - Pj), dl = Rj^T r
   const V3 Rg_ol = rmul(Rj, gol), Rg_dl = rmul(Rj, gdl);

@@ -807,13 +807,12 @@ namespace iact {
 //   S_rho = c / (2q) + sum_i p_i a_i rho^(p_i - 1),  S_rhorho = c (1+k) c^2 / (4 q^3) + ...
 //   S_c = rho/(1+q) + (1+k) c^2 rho^2 / (q (1+q)^2),  S_k = c^3 rho^2 / (2 q (1+q)^2)
 //   S_rho,c = 1/(2q) + (1+k) c^2 rho / (2 q^3),       S_rho,k = c^3 rho / (4 q^3)
-//   S_a_i = rho^p_i,  S_rho,a_i = p_i rho^(p_i - 1)
+//   S_a_i = rho^p_i,  S_rho,a_i = p_i rho^(p_i - 1)  (formed by the caller)
 // float32: these are derivatives at a known hit, sums of positive-scale
 // terms without the cancellation of the root's residual (the root itself is
-// FP64, mirror_hit).
+// found to about 1e-13, mirror_hit).
 struct SagD {
   float S, Sr, Srr, Sc, Sk, Src, Srk;
-  float Sa[8], Sra[8];
 };
 
 __device__ __forceinline__ void sag_derivs(const float* m, float rho, SagD& o) {
@@ -830,11 +829,6 @@ __device__ __forceinline__ void sag_derivs(const float* m, float rho, SagD& o) {
   o.Src = 0.5f * iq + 0.5f * al * rho * iq3;
   o.Srk = 0.25f * c * c * c * rho * iq3;
   const int na = (int)m[19];
-#pragma unroll
-  for (int i = 0; i < 8; ++i) {
-    o.Sa[i] = 0.f;
-    o.Sra[i] = 0.f;
-  }
   float rp = rho * rho;  // rho^p, p = 2
   float rpm1 = rho;      // rho^(p-1)
   float rpm2 = 1.f;      // rho^(p-2)
@@ -843,8 +837,6 @@ __device__ __forceinline__ void sag_derivs(const float* m, float rho, SagD& o) {
     o.S += a * rp;
     o.Sr += a * p * rpm1;
     o.Srr += a * p * (p - 1.f) * rpm2;
-    o.Sa[i] = rp;
-    o.Sra[i] = p * rpm1;
     rp *= rho * rho;
     rpm1 *= rho * rho;
     rpm2 *= rho * rho;
