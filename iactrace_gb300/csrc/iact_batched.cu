@@ -50,7 +50,7 @@ int launch_batch_prep(const BatchJob* jobs, int n_jobs, int gx, int backward, cu
 }
 
 template <int SRC, bool SOFT, int MODE, bool STAGES>
-__global__ void __launch_bounds__(256, STAGES ? 2 : IACT_RENDER_MIN_CTAS) k_batch_render(const BatchK b) {
+__global__ void __launch_bounds__(256, STAGES ? 3 : IACT_RENDER_MIN_CTAS) k_batch_render(const BatchK b) {
   extern __shared__ __align__(16) float smem[];
   __shared__ __align__(16) RenderK s_p;
   __shared__ int s_tile, s_job, s_begin;

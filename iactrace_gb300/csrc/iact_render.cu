@@ -38,7 +38,7 @@ __global__ void __launch_bounds__(256) k_prep(const PrepK p) {
 }
 
 template <int SRC, bool SOFT, int MODE, bool STAGES>
-__global__ void __launch_bounds__(256, STAGES ? 2 : IACT_RENDER_MIN_CTAS) k_render(const RenderK p) {
+__global__ void __launch_bounds__(256, STAGES ? 3 : IACT_RENDER_MIN_CTAS) k_render(const RenderK p) {
   extern __shared__ __align__(16) float smem[];
   __shared__ int s_tile;
   const int tab_n = (p.n_table_floats + 3) & ~3;
