@@ -125,10 +125,12 @@ def workload_config(name, tel, S, mode, flush):
     return cfg, F * M * S
 
 
-def adjoint_kernel_seconds(tel, src, val, stype, mode, gout, flush_buf, steps):
+def adjoint_kernel_seconds(tel, src, val, stype, mode, gout, flush_buf, steps, samples=False):
     """Event time of the adjoint kernel alone (iact_render_backward through
     the C ABI, gradients w.r.t. facet rotations and positions, sources and
-    values), averaged over `steps` launches with the L2 flushed before each."""
+    values, and with `samples` the per-sample sums that carry the primary
+    surface's gradients), averaged over `steps` launches with the L2 flushed
+    before each."""
     import ctypes
     from iactrace_gb300 import _native as N
     from iactrace_gb300.core.render import source_code
@@ -141,6 +143,7 @@ def adjoint_kernel_seconds(tel, src, val, stype, mode, gout, flush_buf, steps):
     ws = torch.empty(ps.workspace_bytes(sdesc, S, N.MODE_BACKWARD), dtype=torch.uint8, device=dev)
     g = [torch.empty((ps.F, 3), device=dev), torch.empty((ps.F, 3), device=dev),
          torch.empty((S, 3), device=dev), torch.empty(S, device=dev)]
+    gsamp = torch.empty((ps.F * ps.M, 7), device=dev) if samples else None
     nm = N.MODE_RESPONSE if mode == "response" else N.MODE_IMAGE
     gout = gout.contiguous()
     ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
@@ -156,7 +159,8 @@ def adjoint_kernel_seconds(tel, src, val, stype, mode, gout, flush_buf, steps):
         N.check(lib.iact_render_backward(ctypes.byref(ps.desc), ctypes.byref(sdesc), code, src.data_ptr(),
                                          val.data_ptr(), S, nm, gout.data_ptr(), g[0].data_ptr(), g[1].data_ptr(),
                                          None, None if no_src else g[2].data_ptr(), g[3].data_ptr(), None, None,
-                                         None, None, ws.data_ptr(), ws.numel(), ctypes.byref(o), stream.cuda_stream))
+                                         None, gsamp.data_ptr() if samples else None, ws.data_ptr(),
+                                         ws.numel(), ctypes.byref(o), stream.cuda_stream))
 
     call()
     tot = 0.0
@@ -624,30 +628,46 @@ def main():
     grp = tel.mirror_groups[0]
     rot = grp.rotations.clone().to(dev).requires_grad_(True)
     pos = grp.positions.clone().to(dev).requires_grad_(True)
-    tel_g = tel.set_mirror_rotations(0, rot).set_mirror_positions(0, pos)
     src_g = src.clone().requires_grad_(True)
     val_g = val.clone().requires_grad_(True)
+    grads = "facet rotations and positions, sources, values"
+    resample = args.workload == "cassegrain"
+    if resample:
+        # the two-mirror config's backward includes the primary's aspheric
+        # coefficients: each step resamples the primary on the device with
+        # the coefficients as autograd leaves (per-sample adjoint sums, mapped
+        # to the surface by the sampler's differentiable restatement)
+        asph = torch.as_tensor(grp.aspheric, dtype=torch.float32).clone().requires_grad_(True)
+        integ = it.DeviceIntegrator(grp.n_samples, device=dev)
+        grads += ", primary aspheric coefficients (resampling)"
+
+    def tel_for_step():
+        if not resample:
+            return tel.set_mirror_rotations(0, rot).set_mirror_positions(0, pos)
+        gs = integ.sample_group(grp.replace(aspheric=asph), 0).replace(rotations=rot, positions=pos)
+        return it.Telescope([gs] + tel.mirror_groups[1:], tel.obstruction_groups, tel.sensors, tel.name)
+
     gout = torch.randn(out.shape, device=dev, generator=torch.Generator(device=dev).manual_seed(0))
     fwdadj = None
     try:
         for _ in range(2):
-            fn(tel_g, src_g, val_g, stype).backward(gout)
+            fn(tel_for_step(), src_g, val_g, stype).backward(gout)
         torch.cuda.synchronize(dev)
         fa_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
                  for _ in range(args.steps)]
         for k in range(args.steps):
             flush_buf.fill_(float(k))
             fa_ev[k][0].record(stream)
-            fn(tel_g, src_g, val_g, stype).backward(gout)
+            fn(tel_for_step(), src_g, val_g, stype).backward(gout)
             fa_ev[k][1].record(stream)
         torch.cuda.synchronize(dev)
         fa_s = sum(a.elapsed_time(b) for a, b in fa_ev) / 1e3 / args.steps
-        adj_s = adjoint_kernel_seconds(tel, src, val, stype, mode, gout, flush_buf, args.steps)
+        adj_s = adjoint_kernel_seconds(tel, src, val, stype, mode, gout, flush_buf, args.steps, samples=resample)
         fwdadj = {"value": rays / fa_s, "unit": "rays/s", "ms_per_step": fa_s * 1e3,
                   "time_ratio_vs_fwd": fa_s / step_s,
                   "adjoint_kernel_ms": adj_s * 1e3,
                   "kernel_time_ratio_vs_fwd": (kern_s + adj_s) / kern_s,
-                  "grads": "facet rotations and positions, sources, values"}
+                  "grads": grads}
     except NotImplementedError as e:
         fwdadj = {"unavailable": str(e)}
 

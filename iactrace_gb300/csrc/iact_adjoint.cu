@@ -190,6 +190,7 @@ int launch_backward(const iact_scene_t* sc, const iact_sensor_t* sn, int src_typ
     if (rc) return rc;
     AdjK p = adjoint_params(sc, sn, L, w, sources, values, grad_out, S, g_scale != nullptr, opts);
     p.gsamp = g_samples;
+    p.want_mgrad = (g_mrot || g_mpos || g_msurf) ? 1 : 0;
     const int block = (opts && opts->block_threads > 0) ? opts->block_threads : 256;
     size_t smem = 0;
     rc = plan_adjoint(p, sn, block, smem, 8LL * std::max(device_info().sm_count, 1));

@@ -34,6 +34,7 @@ struct AdjK {
   const float4* B4;  // per (facet, chunk) bundle bounds (culling on)
   int n_words;       // 32-bit candidate-mask words per task; 0 = no culling
   float* gsamp;      // optional [F*M, 7]: per sample dL/d(world point, perturbed normal, 1/weight)
+  int want_mgrad;    // stage-mirror parameter gradients requested (gmir)
 };
 
 // Per-lane running sums of one (facet, source) stream of rays.
@@ -223,6 +224,9 @@ struct StageRec {
 // differentiated implicitly (dt = -(dG) / G_t with G_t = N . d_local,
 // N = (-sag_x, -sag_y, 1)); the reference unrolls its 10 Newton steps, which
 // agrees to the root's residual.
+// PARAMS: also form the mirror's parameter gradients g (else g is untouched
+// and only the chain through the stage is reversed).
+template <bool PARAMS>
 __device__ __forceinline__ void stage_bwd(const float* m, const StageRec& R, V3& go, V3& gr, float& gv,
                                           float* g) {
   const float* Rj = m;
@@ -308,13 +312,15 @@ __device__ __forceinline__ void stage_bwd(const float* m, const StageRec& R, V3&
   gR[6] += op.z * gol.x + R.r.z * gdl.x; gR[7] += op.z * gol.y + R.r.z * gdl.y; gR[8] += op.z * gol.z + R.r.z * gdl.z;
   gr = gr_in + Rg_dl;
   gv = gval_in;
+  if (PARAMS) {
 #pragma unroll
-  for (int i = 0; i < 9; ++i) g[i] = gR[i];
-  g[9] = gP.x; g[10] = gP.y; g[11] = gP.z;
-  g[12] = gth_c;
-  g[13] = gth_k;
+    for (int i = 0; i < 9; ++i) g[i] = gR[i];
+    g[9] = gP.x; g[10] = gP.y; g[11] = gP.z;
+    g[12] = gth_c;
+    g[13] = gth_k;
 #pragma unroll
-  for (int i = 0; i < 8; ++i) g[14 + i] = gth_a[i];
+    for (int i = 0; i < 8; ++i) g[14 + i] = gth_a[i];
+  }
 }
 
 // One work tile (source block, facet chunk, 32-sample chunk) of the
@@ -460,13 +466,19 @@ __device__ __forceinline__ void adjoint_tile(const AdjK& p, const Obst& ob, cons
         a = gpl - (dLdt * inv_nd) * ns;               // dL/do through the plane
         gr = tpl * gpl - (dLdt * tpl * inv_nd) * ns;  // dL/dr through the plane
       }
-      if (STAGES) {  // warp-converged: the mirror sums are warp-collective
+      if (STAGES && !p.want_mgrad && act) {  // the chain through the stages only
+        for (int k = nst - 1; k >= 0; --k) {
+          float gm[kMirGrad];
+          stage_bwd<false>(mir + rec[k].j * kMirF, rec[k], a, gr, gv0, gm);
+        }
+      }
+      if (STAGES && p.want_mgrad) {  // warp-converged: the mirror sums are warp-collective
         const int kmax = __reduce_max_sync(kFull, act ? nst : 0);
         for (int k = kmax - 1; k >= 0; --k) {
           float gm[kMirGrad];
           int j = -1;
           if (act && k < nst) {
-            stage_bwd(mir + rec[k].j * kMirF, rec[k], a, gr, gv0, gm);
+            stage_bwd<true>(mir + rec[k].j * kMirF, rec[k], a, gr, gv0, gm);
             j = rec[k].j;
           } else {
 #pragma unroll

@@ -393,6 +393,7 @@ int iact_batch_prepare(iact_batch* b, void* workspace, size_t workspace_bytes, v
         a.gfacet = reinterpret_cast<double*>(base + b->lay[i].acc);
         a.gsrc = a.gfacet + (size_t)a.F * kFacetGrad;
         a.gmir = a.gsrc + (size_t)a.S * 4;
+        a.want_mgrad = (U.g_mirror_rot || U.g_mirror_pos || U.g_mirror_surface) ? 1 : 0;
         J.pkb = prep_params(&b->scenes[i], b->lay[i], base, U.g_facet_scale != nullptr);
         J.gr.g_rot = U.g_facet_rot; J.gr.g_pos = U.g_facet_pos; J.gr.g_scale = U.g_facet_scale;
         J.gr.g_src = U.g_sources; J.gr.g_val = U.g_values;

@@ -177,8 +177,10 @@ SensorK make_sensor(const iact_sensor_t* s) {
     k.hr_y = (float)(2.0 / (3.0 * sz));
   }
   k.inv_inr = s->inradius > 0.f ? (float)(1.0 / (double)s->inradius) : 0.f;
-  const double lim = (double)s->inradius * s->edge_threshold - 1e-5;
-  k.hex_lim2 = lim > 0.0 ? (float)(lim * lim) : -1.f;  // -1: the cache never hits
+  // cached-cell radius: inside the cell's inscribed circle and the edge
+  // threshold, less a rounding margin (-1: the cache never hits)
+  const double lim = (double)s->inradius * std::min((double)s->edge_threshold, 1.0) - 1e-5;
+  k.hex_lim2 = lim > 0.0 ? (float)(lim * lim) : -1.f;
   return k;
 }
 
