@@ -637,7 +637,15 @@ def main():
         # coefficients: each step resamples the primary on the device with
         # the coefficients as autograd leaves (per-sample adjoint sums, mapped
         # to the surface by the sampler's differentiable restatement)
-        asph = torch.as_tensor(grp.aspheric, dtype=torch.float32).clone().requires_grad_(True)
+        asph = torch.as_tensor(grp.aspheric, dtype=torch.float32).clone().to(dev).requires_grad_(True)
+        grp = grp.replace(offsets=grp.offsets.to(dev), vertices=grp.vertices.to(dev),
+                          perturbation_scale=grp.perturbation_scale.to(dev))
+        # fixed stage >= 1 mirrors with device-resident parameters (nothing is
+        # copied from the host inside a captured step)
+        dev_t = lambda x: (x if isinstance(x, torch.Tensor) else torch.tensor(float(x))).to(dev)
+        later = [g.replace(**{n: dev_t(getattr(g, n)) for n in ("positions", "rotations", "offsets", "aspheric",
+                                                                  "radii", "vertices", "curvature", "conic")
+                              if getattr(g, n, None) is not None}) for g in tel.mirror_groups[1:]]
         integ = it.DeviceIntegrator(grp.n_samples, device=dev)
         grads += ", primary aspheric coefficients (resampling)"
 
@@ -645,7 +653,7 @@ def main():
         if not resample:
             return tel.set_mirror_rotations(0, rot).set_mirror_positions(0, pos)
         gs = integ.sample_group(grp.replace(aspheric=asph), 0).replace(rotations=rot, positions=pos)
-        return it.Telescope([gs] + tel.mirror_groups[1:], tel.obstruction_groups, tel.sensors, tel.name)
+        return it.Telescope([gs] + later, tel.obstruction_groups, tel.sensors, tel.name)
 
     gout = torch.randn(out.shape, device=dev, generator=torch.Generator(device=dev).manual_seed(0))
     fwdadj = None
@@ -668,6 +676,33 @@ def main():
                   "adjoint_kernel_ms": adj_s * 1e3,
                   "kernel_time_ratio_vs_fwd": (kern_s + adj_s) / kern_s,
                   "grads": grads}
+        if resample:
+            # the same step (resample, render, adjoint, sampler reverse)
+            # captured once in a CUDA graph and replayed
+            side = torch.cuda.Stream(dev)
+            side.wait_stream(stream)
+            with torch.cuda.stream(side):
+                for _ in range(2):
+                    fn(tel_for_step(), src_g, val_g, stype).backward(gout)
+            stream.wait_stream(side)
+            for t in (rot, pos, src_g, val_g, asph):
+                t.grad = None
+            graph = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(graph):
+                fn(tel_for_step(), src_g, val_g, stype).backward(gout)
+            graph.replay()
+            torch.cuda.synchronize(dev)
+            gr_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                     for _ in range(args.steps)]
+            for k in range(args.steps):
+                flush_buf.fill_(float(k))
+                gr_ev[k][0].record(stream)
+                graph.replay()
+                gr_ev[k][1].record(stream)
+            torch.cuda.synchronize(dev)
+            gr_s = sum(a.elapsed_time(b) for a, b in gr_ev) / 1e3 / args.steps
+            fwdadj["graph"] = {"value": rays / gr_s, "unit": "rays/s", "ms_per_step": gr_s * 1e3,
+                               "time_ratio_vs_fwd": gr_s / step_s}
     except NotImplementedError as e:
         fwdadj = {"unavailable": str(e)}
 

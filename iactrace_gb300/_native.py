@@ -105,7 +105,7 @@ class IactSampler(ctypes.Structure):
     _fields_ = [("n_facets", _i), ("n_samples", _i), ("aperture", _i), ("n_vert", _i),
                 ("curvature", _f), ("conic", _f), ("n_asph", _i), ("asph", _f * IACT_MAX_ASPH),
                 ("offsets", ctypes.c_void_p), ("radii", ctypes.c_void_p), ("vertices", ctypes.c_void_p),
-                ("seed", ctypes.c_uint32)]
+                ("seed", ctypes.c_uint32), ("surface", ctypes.c_void_p)]
 
 
 class IactError(RuntimeError):
@@ -145,6 +145,8 @@ _SIGS = {
     "iact_batch_destroy": ([ctypes.c_void_p], None),
     "iact_sample_facets": ([ctypes.POINTER(IactSampler), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                             ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
+    "iact_sample_facets_backward": ([ctypes.POINTER(IactSampler), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                     ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p], ctypes.c_int),
 }
 
 # symbols declared by include/iactrace_gb300.h that bindings resolve
@@ -180,12 +182,12 @@ def load(build_if_missing: bool = False):
 
 
 def check_layout(lib) -> None:
-    out = (ctypes.c_size_t * 5)()
-    rc = lib.iact_abi_layout(out, 5)
+    out = (ctypes.c_size_t * 6)()
+    rc = lib.iact_abi_layout(out, 6)
     if rc != IACT_OK:
         raise IactError(rc, "iact_abi_layout failed")
     mine = [ctypes.sizeof(IactScene), ctypes.sizeof(IactSensor), ctypes.sizeof(IactMirror), ctypes.sizeof(IactOpts),
-            ctypes.sizeof(IactJob)]
+            ctypes.sizeof(IactJob), ctypes.sizeof(IactSampler)]
     if list(out) != mine:
         raise ImportError(f"ABI struct layout mismatch: library {list(out)} vs binding {mine}")
 

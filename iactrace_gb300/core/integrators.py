@@ -18,7 +18,7 @@ import torch
 from .. import _native as N
 from ..utils import keys as _keys
 from ..utils.sampling import sample_disk, sample_polygon
-from .reflection import compute_perturbation_delta, perturbation_delta_from_normals
+from .reflection import compute_perturbation_delta
 
 
 class Integrator(ABC):
@@ -75,23 +75,31 @@ class MCIntegrator(Integrator):
         return self._finish(group, params["surface"], xy, params["offsets"].double(), area, gen)
 
 
-def sampler_desc(group, key, n_samples: int, device):
+def sampler_desc(group, key, n_samples: int, device, surface=None):
     """The iact_sampler_t of a stage-0 group and its arrays on `device`
-    (returns the descriptor and the tensors it points at)."""
+    (returns the descriptor and the tensors it points at). surface: an
+    optional device float32 tensor [2 + n_asph] (curvature, conic,
+    aspheric) read by the kernels instead of the group's values; the host
+    then reads no parameter value (a captured launch follows updates)."""
     params = group.get_sampling_params()
     surf = params["surface"]
     d = N.IactSampler()
     d.n_facets, d.n_samples = len(group), int(n_samples)
-    value = lambda x: float(x.detach()) if isinstance(x, torch.Tensor) else float(x)
-    d.curvature, d.conic = value(surf.curvature), value(surf.conic)
-    a = surf.aspheric.detach().reshape(-1).tolist()
-    if len(a) > N.IACT_MAX_ASPH:
+    n_asph = int(torch.as_tensor(surf.aspheric).numel()) if surface is None else int(surface.numel()) - 2
+    if n_asph > N.IACT_MAX_ASPH:
         raise ValueError(f"at most {N.IACT_MAX_ASPH} aspheric coefficients")
-    d.n_asph = len(a)
-    for i, v in enumerate(a):
-        d.asph[i] = float(v)
-    keep = [params["offsets"].reshape(-1, 2).to(device=device, dtype=torch.float32).contiguous()]
-    d.offsets = keep[0].data_ptr()
+    d.n_asph = n_asph
+    if surface is None:
+        value = lambda x: float(x.detach()) if isinstance(x, torch.Tensor) else float(x)
+        d.curvature, d.conic = value(surf.curvature), value(surf.conic)
+        for i, v in enumerate(torch.as_tensor(surf.aspheric).detach().reshape(-1).tolist()):
+            d.asph[i] = float(v)
+        keep = []
+    else:
+        keep = [surface]
+        d.surface = surface.data_ptr()
+    keep.append(params["offsets"].reshape(-1, 2).to(device=device, dtype=torch.float32).contiguous())
+    d.offsets = keep[-1].data_ptr()
     if params["type"] == "disk":
         d.aperture = N.APERTURE_DISK
         keep.append(params["radii"].reshape(-1).to(device=device, dtype=torch.float32).contiguous())
@@ -108,6 +116,38 @@ def sampler_desc(group, key, n_samples: int, device):
     return d, keep
 
 
+def _launch_sample(d, F, M, dev):
+    pts, nrm, dlt = (torch.empty((F, M, 3), device=dev) for _ in range(3))
+    w = torch.empty((F, M, 1), device=dev)
+    N.check(N.load().iact_sample_facets(ctypes.byref(d), pts.data_ptr(), nrm.data_ptr(), dlt.data_ptr(),
+                                        w.data_ptr(), torch.cuda.current_stream(dev).cuda_stream))
+    return pts, nrm, dlt, w
+
+
+class _SampleFunction(torch.autograd.Function):
+    """Sample arrays as a function of the surface vector theta = (curvature,
+    conic, aspheric...): iact_sample_facets forward, its reverse
+    iact_sample_facets_backward (dL/d theta from dL/d(points, normals,
+    deltas, weights)) backward."""
+
+    @staticmethod
+    def forward(ctx, theta, desc, keep, F, M):
+        ctx.desc, ctx.keep = desc, keep
+        ctx.save_for_backward(theta)
+        return _launch_sample(desc, F, M, theta.device)
+
+    @staticmethod
+    def backward(ctx, gp, gn, gd, gw):
+        (theta,) = ctx.saved_tensors
+        dev = theta.device
+        g = torch.empty(theta.numel(), dtype=torch.float64, device=dev)
+        ptr = lambda t: t.contiguous().data_ptr() if t is not None else None
+        gs = [t.contiguous() if t is not None else None for t in (gp, gn, gd, gw)]
+        N.check(N.load().iact_sample_facets_backward(ctypes.byref(ctx.desc), *(ptr(t) for t in gs), g.data_ptr(),
+                                                     torch.cuda.current_stream(dev).cuda_stream))
+        return g.to(theta.dtype), None, None, None, None
+
+
 class DeviceIntegrator(Integrator):
     """MCIntegrator on the GPU: same aperture, surface, roughness-delta and
     weight construction (core/integrators.py:97-187), variates from the
@@ -118,45 +158,32 @@ class DeviceIntegrator(Integrator):
         self.device = device
 
     def sample_group(self, group, key):
+        """Sample `group` on the device. When the surface parameters
+        (curvature, conic, aspheric) are autograd tensors, the arrays are a
+        differentiable function of them (resampling gradients through
+        iact_sample_facets_backward); the kernels then read the parameters
+        from device memory (keep them on the device to capture a step in a
+        CUDA graph)."""
         dev = torch.device(self.device) if self.device is not None else torch.device("cuda", torch.cuda.current_device())
-        d, keep = sampler_desc(group, key, self.n_samples, dev)
         F, M = len(group), self.n_samples
-        pts, nrm, dlt = (torch.empty((F, M, 3), device=dev) for _ in range(3))
-        w = torch.empty((F, M, 1), device=dev)
-        lib = N.load()
-        N.check(lib.iact_sample_facets(ctypes.byref(d), pts.data_ptr(), nrm.data_ptr(), dlt.data_ptr(), w.data_ptr(),
-                                       torch.cuda.current_stream(dev).cuda_stream))
-        del keep
         surf = group.get_surface()
         params = [surf.curvature, surf.conic, surf.aspheric]
-        if any(isinstance(t, torch.Tensor) and t.requires_grad for t in params):
-            pts, nrm, dlt, w = self._differentiable(group, surf, pts, nrm, dlt, w)
+        grad = any(isinstance(t, torch.Tensor) and t.requires_grad for t in params)
+        on_dev = any(isinstance(t, torch.Tensor) and t.is_cuda for t in params)
+        if not (grad or on_dev):
+            d, keep = sampler_desc(group, key, M, dev)
+            pts, nrm, dlt, w = _launch_sample(d, F, M, dev)
+            del keep
+            return group.with_samples(pts, nrm, dlt, w)
+        # the surface as a device vector read by the kernels (python numbers
+        # become device fills: no host-to-device copy, no device read)
+        as_t = lambda x: x.to(device=dev, dtype=torch.float32) if isinstance(x, torch.Tensor) else \
+            torch.full((1,), float(x), device=dev)
+        theta = torch.cat([as_t(surf.curvature).reshape(1), as_t(surf.conic).reshape(1),
+                           as_t(surf.aspheric).reshape(-1)])
+        d, keep = sampler_desc(group, key, M, dev, surface=theta.detach())
+        if grad:
+            pts, nrm, dlt, w = _SampleFunction.apply(theta, d, keep, F, M)
+        else:
+            pts, nrm, dlt, w = _launch_sample(d, F, M, dev)
         return group.with_samples(pts, nrm, dlt, w)
-
-    def _differentiable(self, group, surf, pts, nrm, dlt, w):
-        """The sample arrays as functions of the surface parameters (FP64
-        torch restatement of the kernel's mapping, core/surfaces.py:41-65 and
-        core/reflection.py:22-49): the aperture positions and the roughness
-        coefficients do not depend on the surface; points, normals, deltas
-        and weights do (resampling gradients)."""
-        dev = pts.device
-        xy = pts[..., :2].double()
-        n0 = nrm.double()
-        # the roughness coefficients of the drawn deltas in their tangent basis
-        ref_z = torch.tensor([0.0, 0.0, 1.0], dtype=torch.float64, device=dev)
-        ref_x = torch.tensor([1.0, 0.0, 0.0], dtype=torch.float64, device=dev)
-        ref = torch.where(n0[..., 2:3].abs() > 0.9, ref_x, ref_z)
-        t1 = torch.linalg.cross(n0, ref.expand_as(n0))
-        t1 = t1 / torch.linalg.norm(t1, dim=-1, keepdim=True)
-        t2 = torch.linalg.cross(n0, t1)
-        d0 = dlt.double()
-        th1, th2 = (d0 * t1).sum(-1), (d0 * t2).sum(-1)
-        s64 = type(surf)(surf.curvature if not isinstance(surf.curvature, torch.Tensor) else surf.curvature.double(),
-                         surf.conic if not isinstance(surf.conic, torch.Tensor) else surf.conic.double(),
-                         surf.aspheric.double())
-        off = group.offsets.reshape(-1, 1, 2).to(device=dev, dtype=torch.float64)
-        p, n = s64.point_and_normal(xy, off)
-        dl = perturbation_delta_from_normals(n, th1, th2)
-        area = (n0[..., 2] / w[..., 0].double() * self.n_samples).detach()  # per facet: pi R^2 or polygon area
-        ww = n[..., 2:3] / area[..., None] * self.n_samples
-        return p.float(), n.float(), dl.float(), ww.float()

@@ -13,7 +13,7 @@ import math
 import torch
 
 from .. import _native as N
-from .scene import pack_scene, primary_params, stages_of
+from .scene import _join, pack_scene, primary_params, stages_of
 
 
 def _device():
@@ -76,8 +76,11 @@ def _sample_grads(gs, rot, scale, nrm, dlt, wts):
     g = gs.double()
     R = euler_to_matrix(rot.double())  # (F, 3, 3)
     a, b, giw = g[..., 0:3], g[..., 3:6], g[..., 6]
-    gp = torch.einsum("fji,fmj->fmi", R, a)  # R^T a
-    bl = torch.einsum("fji,fmj->fmi", R, b)
+    # R^T a, R^T b as broadcast products (no batched GEMM: nothing to set up
+    # per stream inside a captured backward)
+    Rt = R[:, None, :, :]  # (F, 1, 3(j), 3(i))
+    gp = (Rt * a[..., :, None]).sum(-2)
+    bl = (Rt * b[..., :, None]).sum(-2)
     m = nrm.double() + scale.double()[:, None, None] * dlt.double()
     mn = torch.linalg.norm(m, dim=-1, keepdim=True)
     u = m / mn
@@ -149,8 +152,9 @@ class RenderFunction(torch.autograd.Function):
 
 
 def _as_t(x, device):
+    # python numbers become device fills (no host-to-device copy)
     return x.to(device=device, dtype=torch.float32) if isinstance(x, torch.Tensor) else \
-        torch.tensor(float(x), device=device)
+        torch.full((), float(x), device=device)
 
 
 def _stage_params(tel, device):
@@ -177,7 +181,7 @@ def primary_samples(tel, device):
     """Concatenated stage-0 sample arrays: points, normals, deltas (F,M,3)
     and weights (F,M), float32 on `device`, differentiable."""
     prim = stages_of(tel).get(0, [])
-    cat = lambda name: torch.cat([getattr(g, name) for g in prim]).to(device=device, dtype=torch.float32)
+    cat = lambda name: _join([getattr(g, name) for g in prim]).to(device=device, dtype=torch.float32)
     pts, nrm, dlt, w = cat("points"), cat("normals"), cat("perturbation_delta"), cat("weights")
     return pts, nrm, dlt, w.reshape(w.shape[0], w.shape[1])
 

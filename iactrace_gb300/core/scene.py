@@ -64,11 +64,85 @@ def _mirror_records(stage_groups) -> np.ndarray:
     return np.frombuffer(b"".join(recs), dtype=np.uint8) if recs else np.zeros(0, np.uint8)
 
 
-def _require_finite(what: str, t: torch.Tensor) -> None:
-    """Host-side input validation at pack time (once per scene): the kernels
-    do not check their tables, so NaN / Inf never reach them."""
-    if t.numel() and not bool(torch.isfinite(t).all()):
-        raise ValueError(f"{what} contains NaN or Inf")
+def _join(ts):
+    """torch.cat, without the copy for a single tensor."""
+    return ts[0] if len(ts) == 1 else torch.cat(ts)
+
+
+def _tkey(x):
+    """Cache key of a tensor by its storage (address, version, shape, stride,
+    dtype): unique while the cache keeps a detached alias of it alive (the
+    alias holds the storage and shares the version counter, but not the
+    autograd graph); numbers by value."""
+    if isinstance(x, torch.Tensor):
+        return (x.data_ptr(), x._version, tuple(x.shape), tuple(x.stride()), x.dtype, str(x.device))
+    return None if x is None else float(x)
+
+
+def _alias(x):
+    return x.detach() if isinstance(x, torch.Tensor) else x
+
+
+def _require_finite(items) -> None:
+    """Input validation at pack time (once per packed scene): the kernels do
+    not check their tables, so NaN / Inf never reach them. items: (what,
+    tensor) pairs; one device-to-host read for all of them. Skipped while
+    the stream is being captured into a CUDA graph (a read is not allowed
+    there): validate inputs before capturing."""
+    items = [(w, t) for w, t in items if t.numel()]
+    if not items or (torch.cuda.is_available() and torch.cuda.is_current_stream_capturing()):
+        return
+    ok = torch.stack([torch.isfinite(t).all() for _, t in items]).cpu()
+    for (what, _), good in zip(items, ok.tolist()):
+        if not good:
+            raise ValueError(f"{what} contains NaN or Inf")
+
+
+# Stage-mirror records and obstruction tables on the device, shared by every
+# packed scene with the same stage >= 1 groups and obstruction groups (a
+# per-step resampled primary does not rebuild or re-upload them; no host to
+# device copy then happens inside a captured step). Entries keep their
+# source objects alive so the ids in the key stay unique.
+_STATIC = OrderedDict()
+_STATIC_MAX = 16
+
+
+def _static_key(tel, later, device):
+    sv = _tkey
+    fp = [str(torch.device(device))]
+    for stage, groups in later:
+        for g in groups:
+            fp.append((stage, len(g), sv(g.curvature), sv(g.conic)))
+            fp += [sv(getattr(g, n)) for n in ("positions", "rotations", "offsets", "aspheric", "radii", "vertices")
+                   if getattr(g, n, None) is not None]
+    fp += [id(g) for g in (tel.obstruction_groups or [])]
+    return tuple(fp)
+
+
+def _static_tables(tel, later, device):
+    key = _static_key(tel, later, device)
+    hit = _STATIC.get(key)
+    if hit is not None:
+        _STATIC.move_to_end(key)
+        return hit[1], hit[2]
+    recs = _mirror_records(later)
+    if len(recs) and not np.isfinite(recs.view(np.float32)).all():
+        # the records are float32 fields and int32 counts; counts are finite as floats too
+        raise ValueError("stage-mirror parameters contain NaN or Inf")
+    mirrors = torch.from_numpy(recs.copy()).to(device) if len(recs) else None
+    kinds = defaultdict(list)
+    for g in (tel.obstruction_groups or []):
+        kinds[g.kind].append(g.table().float())
+    _require_finite([(f"{kind} obstruction table", t) for kind, ts in kinds.items() for t in ts])
+    obst = {kind: _f32(torch.cat(kinds[kind]), device) for kind in ("cyl", "box", "sph", "obox", "tri")
+            if kinds[kind]}
+    keep = [tuple(_alias(getattr(g, n, None)) for n in ("curvature", "conic", "positions", "rotations", "offsets",
+                                                        "aspheric", "radii", "vertices"))
+            for _, gs in later for g in gs] + list(tel.obstruction_groups or [])
+    _STATIC[key] = (keep, mirrors, obst)
+    while len(_STATIC) > _STATIC_MAX:
+        _STATIC.popitem(last=False)
+    return mirrors, obst
 
 
 class PackedScene:
@@ -92,38 +166,25 @@ class PackedScene:
         d = N.IactScene()
         d.n_facets, d.n_samples = self.F, self.M
         if self.F and self.M:
-            cat = lambda name: torch.cat([getattr(g, name).detach().float() for g in prim])
-            for name in ("points", "normals", "perturbation_delta", "weights"):
-                _require_finite(f"primary {name}", cat(name))
-            self.points = _f32(cat("points"), device)
-            self.normals = _f32(cat("normals"), device)
-            self.delta = _f32(cat("perturbation_delta"), device)
-            self.weights = _f32(cat("weights").reshape(self.F, self.M), device)
+            cat = lambda name: _f32(_join([getattr(g, name).detach() for g in prim]), device)
+            self.points = cat("points")
+            self.normals = cat("normals")
+            self.delta = cat("perturbation_delta")
+            self.weights = cat("weights").reshape(self.F, self.M)
+            _require_finite([(f"primary {name}", getattr(self, name))
+                             for name in ("points", "normals", "delta", "weights")])
             for name in ("points", "normals", "delta", "weights"):
                 setattr(d, name, getattr(self, name).data_ptr())
         later = [(s, gs) for s, gs in st.items() if s != 0]
-        recs = _mirror_records(later)
-        if len(recs) and not np.isfinite(recs.view(np.float32)).all():
-            # the records are float32 fields and int32 counts; counts are finite as floats too
-            raise ValueError("stage-mirror parameters contain NaN or Inf")
-        self.n_mirrors = len(recs) // ctypes.sizeof(N.IactMirror)
-        self.mirrors = torch.from_numpy(recs.copy()).to(device) if self.n_mirrors else None
+        self.mirrors, self.obst = _static_tables(tel, later, device)
+        self.n_mirrors = int(self.mirrors.numel()) // ctypes.sizeof(N.IactMirror) if self.mirrors is not None else 0
         d.n_mirrors = self.n_mirrors
         d.n_stages = len(later)
         self.n_stages = len(later)
         d.mirrors = self.mirrors.data_ptr() if self.n_mirrors else None
-        kinds = defaultdict(list)
-        for g in (tel.obstruction_groups or []):
-            t = g.table().float()
-            _require_finite(f"{g.kind} obstruction table", t)
-            kinds[g.kind].append(t)
-        self.obst = {}
-        for kind in ("cyl", "box", "sph", "obox", "tri"):
-            if kinds[kind]:
-                t = _f32(torch.cat(kinds[kind]), device)
-                self.obst[kind] = t
-                setattr(d, "n_" + kind, int(t.shape[0]))
-                setattr(d, kind, t.data_ptr())
+        for kind, t in self.obst.items():
+            setattr(d, "n_" + kind, int(t.shape[0]))
+            setattr(d, kind, t.data_ptr())
         self.desc = d
         self.device = device
 
@@ -148,6 +209,9 @@ def primary_params(tel, device):
     if not prim:
         z = torch.zeros((0, 3), device=device)
         return z, z, torch.zeros(0, device=device)
+    # a fresh tensor even for one group: autograd then accumulates a leaf's
+    # gradient behind an op of the calling stream (a leaf handed to the render
+    # directly would tie its creation stream into a captured backward)
     cat = lambda name, w: torch.cat([getattr(g, name).reshape(len(g), w) if w else getattr(g, name).reshape(-1)
                                      for g in prim]).to(device=device, dtype=torch.float32)
     return cat("rotations", 3), cat("positions", 3), cat("perturbation_scale", 0)
@@ -162,12 +226,13 @@ def _fingerprint(tel):
     fp = []
     for g in tel.mirror_groups:
         names = ("points", "normals", "perturbation_delta", "weights") if g.optical_stage == 0 else \
-            ("positions", "rotations", "offsets", "aspheric")
+            ("positions", "rotations", "offsets", "aspheric", "radii", "vertices")
         for name in names:
             t = getattr(g, name, None)
             if t is not None:
-                fp.append((id(t), t._version))
-        fp.append((g.optical_stage, _value(g.curvature), _value(g.conic), len(g)))
+                fp.append(_tkey(t))
+        # surface constants: values, or tensor identities (no device read)
+        fp.append((g.optical_stage, _tkey(g.curvature), _tkey(g.conic), len(g)))
     for g in (tel.obstruction_groups or []):
         fp.append(id(g))
     return tuple(fp)
@@ -175,8 +240,11 @@ def _fingerprint(tel):
 
 # Packed scenes shared by telescopes built from the same sample arrays, stage
 # mirrors and obstructions (an optimiser's functional updates of the facet
-# transforms create a new Telescope per step). The entries keep their source
-# tensors alive, so the ids in the fingerprint cannot be reused while cached.
+# transforms create a new Telescope per step). The entries keep detached
+# aliases of their source tensors: the storages stay alive, so the addresses
+# in the fingerprint cannot be reused while cached, and no autograd graph is
+# kept (a cached graph would pin its gradient accumulators to the streams
+# they were first built on).
 _SHARED = OrderedDict()
 _SHARED_MAX = 16
 
@@ -185,8 +253,8 @@ def _sources(tel):
     out = []
     for g in tel.mirror_groups:
         names = ("points", "normals", "perturbation_delta", "weights") if g.optical_stage == 0 else \
-            ("positions", "rotations", "offsets", "aspheric")
-        out += [getattr(g, n, None) for n in names]
+            ("positions", "rotations", "offsets", "aspheric", "radii", "vertices")
+        out += [_alias(getattr(g, n, None)) for n in names] + [_alias(g.curvature), _alias(g.conic)]
     return out + list(tel.obstruction_groups or [])
 
 
@@ -216,12 +284,12 @@ def pack_scene(tel, device, facets=None) -> PackedScene:
         # tensors are the same objects at the same version (kept alive here so
         # their ids stay unique)
         src = [t for g in stages_of(tel).get(0, []) for t in (g.rotations, g.positions, g.perturbation_scale)]
-        fkey = tuple((id(t), getattr(t, "_version", 0)) for t in src)
+        fkey = tuple(_tkey(t) for t in src)
         cached = ps.__dict__.get("_facet_cache")
         if cached is not None and cached[0] == fkey:
             facets = cached[2]
         else:
             facets = tuple(t.detach().contiguous() for t in primary_params(tel, ps.device))
-            ps._facet_cache = (fkey, src, facets)
+            ps._facet_cache = (fkey, [_alias(t) for t in src], facets)
     ps.set_facets(*facets)
     return ps

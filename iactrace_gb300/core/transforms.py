@@ -21,11 +21,10 @@ def euler_to_matrix(tip_tilt_rotation) -> torch.Tensor:
     r = torch.deg2rad(a)
     cx, cy, cz = torch.cos(r[..., 0]), torch.cos(r[..., 1]), torch.cos(r[..., 2])
     sx, sy, sz = torch.sin(r[..., 0]), torch.sin(r[..., 1]), torch.sin(r[..., 2])
-    one, zero = torch.ones_like(cx), torch.zeros_like(cx)
-    Rx = torch.stack([one, zero, zero, zero, cx, -sx, zero, sx, cx], -1).reshape(*cx.shape, 3, 3)
-    Ry = torch.stack([cy, zero, sy, zero, one, zero, -sy, zero, cy], -1).reshape(*cx.shape, 3, 3)
-    Rz = torch.stack([cz, -sz, zero, sz, cz, zero, zero, zero, one], -1).reshape(*cx.shape, 3, 3)
-    return Rz @ Ry @ Rx
+    # Rz @ Ry @ Rx written out (elementwise: no batched GEMM)
+    return torch.stack([cz * cy, cz * sy * sx - sz * cx, cz * sy * cx + sz * sx,
+                        sz * cy, sz * sy * sx + cz * cx, sz * sy * cx - cz * sx,
+                        -sy, cy * sx, cy * cx], -1).reshape(*cx.shape, 3, 3)
 
 
 def look_at_rotation(mirror_pos, target_pos=(0.0, 0.0, 0.0), up=(0.0, 1.0, 0.0)) -> torch.Tensor:

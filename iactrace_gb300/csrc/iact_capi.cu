@@ -108,7 +108,7 @@ int iact_abi_version(void) { return IACT_ABI_VERSION; }
 const char* iact_last_error(void) { return g_last_error.c_str(); }
 
 // sizes of the ABI structs as this library sees them (bindings check theirs);
-// a fifth slot receives sizeof(iact_job_t)
+// a fifth slot receives sizeof(iact_job_t), a sixth sizeof(iact_sampler_t)
 int iact_abi_layout(size_t* out, int n) {
   if (!out || n < 4) return set_error(IACT_E_INVALID, "iact_abi_layout needs room for 4 sizes");
   out[0] = sizeof(iact_scene_t);
@@ -116,6 +116,7 @@ int iact_abi_layout(size_t* out, int n) {
   out[2] = sizeof(iact_mirror_t);
   out[3] = sizeof(iact_opts_t);
   if (n >= 5) out[4] = sizeof(iact_job_t);
+  if (n >= 6) out[5] = sizeof(iact_sampler_t);
   return IACT_OK;
 }
 

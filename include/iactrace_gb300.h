@@ -42,7 +42,7 @@
 extern "C" {
 #endif
 
-#define IACT_ABI_VERSION 2
+#define IACT_ABI_VERSION 3
 
 /* status codes */
 #define IACT_OK 0
@@ -159,8 +159,8 @@ typedef struct {
 int iact_abi_version(void);
 const char* iact_last_error(void);
 /* sizeof(iact_scene_t), sizeof(iact_sensor_t), sizeof(iact_mirror_t),
- * sizeof(iact_opts_t) and, if n >= 5, sizeof(iact_job_t) as compiled into
- * the library (binding self-check). */
+ * sizeof(iact_opts_t) and, if n >= 5, sizeof(iact_job_t), if n >= 6,
+ * sizeof(iact_sampler_t) as compiled into the library (binding self-check). */
 int iact_abi_layout(size_t* out, int n);
 
 /* Diagnostics: runs `iters` dependent FP32 FMAs per thread over
@@ -325,11 +325,28 @@ typedef struct {
   const float* radii;         /* device [F] (disk)                           */
   const float* vertices;      /* device [F, n_vert, 2] (polygon, convex)     */
   uint32_t seed;
+  const float* surface;       /* optional device [2 + n_asph]: curvature,
+                                 conic, aspheric coefficients, read on the
+                                 device instead of the values above (a
+                                 captured launch then follows updates)      */
 } iact_sampler_t;
 
 /* points, normals, delta: device [F, M, 3]; weights: device [F, M] */
 int iact_sample_facets(const iact_sampler_t* sampler, float* points, float* normals,
                        float* delta, float* weights, void* stream);
+
+/* Reverse of iact_sample_facets with respect to the shared surface: given
+ * dL/d(points, normals, delta, weights) of the sampled arrays (device, same
+ * shapes; any may be NULL = zero), writes dL/d(curvature, conic, aspheric
+ * coefficients) to g_surface (device, 2 + n_asph doubles). The aperture
+ * positions and roughness coefficients are the forward's (same seed); the
+ * surface enters through the points' sag, the normals, the tangent-plane
+ * deltas and the weights (core/surfaces.py:25-65, core/reflection.py:22-49,
+ * core/integrators.py:124-127). Replaces the reference's autodiff of
+ * MCIntegrator.sample_group (core/integrators.py:97-187). */
+int iact_sample_facets_backward(const iact_sampler_t* sampler, const float* g_points,
+                                const float* g_normals, const float* g_delta,
+                                const float* g_weights, double* g_surface, void* stream);
 
 #ifdef __cplusplus
 }

@@ -61,8 +61,9 @@ def test_resampling_gradients_match_the_twin(cuda):
     a2 = torch.tensor(a0, dtype=torch.float64, requires_grad=True)
     g2 = g.replace(curvature=c2, conic=k2, aspheric=a2)
     surf2 = g2.get_surface()
-    p, n, dl, w = integ._differentiable(g2, surf2, raw.points.cpu(), raw.normals.cpu(),
-                                        raw.perturbation_delta.cpu(), raw.weights.cpu())
+    p, n, dl, w = twin.resample_mapping(g2, surf2, raw.points.cpu(), raw.normals.cpu(),
+                                        raw.perturbation_delta.cpu(), raw.weights.cpu(), 96)
+    p, n, dl, w = p.float(), n.float(), dl.float(), w.float()
     tel2 = Telescope([g.replace(points=p, normals=n, perturbation_delta=dl, weights=w)], [], [cam])
     pts, vals, pix, _ = it.render_debug(Telescope([raw], [], [cam]), d, val, "parallel", extras=True)
     sc, sn = twin.scene_of(tel2, 0, "parallel")
@@ -78,3 +79,42 @@ def test_resampling_gradients_match_the_twin(cuda):
         print(name, gx, gy, err)
         assert np.linalg.norm(gy) > 0
         assert err <= GRAD_TOL, f"d/d{name}: relative error {err:.3g}"
+
+
+def test_resampled_step_replays_in_a_cuda_graph(cuda):
+    """The resample (iact_sample_facets with the surface read on the device),
+    render, adjoint and sampler reverse of one step, captured once in a CUDA
+    graph: a replay gives the eager step's surface and tilt gradients (up to
+    the summation order of the float atomics)."""
+    from iactrace_gb300 import DifferentiableSquareSensor
+    g = _dish(1.0 / 30.0, -0.4, [2e-3, -4e-4])
+    g = g.replace(**{n: getattr(g, n).to(cuda) for n in ("positions", "offsets", "vertices", "perturbation_scale")})
+    rot = g.rotations.clone().to(cuda).requires_grad_(True)
+    a1 = torch.tensor([2e-3, -4e-4], device=cuda, requires_grad=True)
+    cam = DifferentiableSquareSensor([0, 0, 15.0], [0, 0, 0], 24, 24, (-0.504, 0.504, -0.504, 0.504), sigma=0.5)
+    d = torch.tensor([[0.01, -0.02, -1.0], [-0.015, 0.01, -1.0]], device=cuda)
+    d = d / d.norm(dim=1, keepdim=True)
+    val = torch.tensor([1.0, 0.7], device=cuda)
+    gw = torch.randn((24, 24), generator=torch.Generator(device=cuda).manual_seed(2), device=cuda)
+    integ = it.DeviceIntegrator(64)
+
+    def step():
+        gs = integ.sample_group(g.replace(aspheric=a1, rotations=rot), 17)
+        it.render(Telescope([gs], [], [cam]), d, val, "parallel").backward(gw)
+
+    step()
+    ref_a, ref_r = a1.grad.clone(), rot.grad.clone()
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        step()
+    torch.cuda.current_stream().wait_stream(side)
+    a1.grad, rot.grad = None, None
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        step()
+    graph.replay()
+    torch.cuda.synchronize()
+    for name, x, y in (("aspheric", a1.grad, ref_a), ("rotations", rot.grad, ref_r)):
+        err = (x - y).norm() / y.norm()
+        assert y.norm() > 0 and err < 1e-5, f"{name}: graph replay differs by {err:.3g}"

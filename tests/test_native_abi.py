@@ -29,7 +29,7 @@ def test_exports_every_declared_symbol(built):
 
 def test_layout_and_version(built):
     N.check_layout(built)
-    assert built.iact_abi_version() == 2
+    assert built.iact_abi_version() == 3
 
 
 def _square(n=4):

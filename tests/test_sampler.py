@@ -125,3 +125,42 @@ def test_oracle_sampler_distribution_on_cpu(built, which):
     if which == 0:
         r2 = (pts[0, :, :2] ** 2).sum(-1) / 0.6 ** 2
         assert abs(r2.mean() - 0.5) < 0.01 and r2.max() <= 1.0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("which", [0, 1])
+def test_sampler_reverse_matches_the_fp64_mapping(cuda, which):
+    """iact_sample_facets_backward against torch FP64 autograd of the same
+    mapping (tests/twin.py resample_mapping) on the same drawn samples, for
+    random dL/d(points, normals, deltas, weights); and the forward with the
+    surface read from device memory equals the by-value forward."""
+    import twin
+    g = _groups()[which]
+    M = 512
+    integ = it.DeviceIntegrator(M)
+    raw = integ.sample_group(g, 5)
+    c = torch.tensor(0.05, device=cuda, requires_grad=True)
+    k = torch.tensor(-1.05, device=cuda, requires_grad=True)
+    a = torch.tensor([1e-4, -2e-6], device=cuda, requires_grad=True)
+    gs = integ.sample_group(g.replace(curvature=c, conic=k, aspheric=a), 5)
+    for x, y in ((gs.points, raw.points), (gs.normals, raw.normals), (gs.perturbation_delta, raw.perturbation_delta),
+                 (gs.weights, raw.weights)):
+        assert torch.equal(x.detach(), y)
+    gen = torch.Generator(device="cpu").manual_seed(3 + which)
+    G = [torch.randn(t.shape, generator=gen, dtype=torch.float64) for t in (gs.points, gs.normals,
+                                                                           gs.perturbation_delta, gs.weights)]
+    loss = sum((t.double() * u.to(cuda)).sum() for t, u in zip((gs.points, gs.normals, gs.perturbation_delta,
+                                                               gs.weights), G))
+    loss.backward()
+    c2 = torch.tensor(0.05, dtype=torch.float64, requires_grad=True)
+    k2 = torch.tensor(-1.05, dtype=torch.float64, requires_grad=True)
+    a2 = torch.tensor([1e-4, -2e-6], dtype=torch.float64, requires_grad=True)
+    g2 = g.replace(curvature=c2, conic=k2, aspheric=a2)
+    p, n, dl, w = twin.resample_mapping(g2, g2.get_surface(), raw.points.cpu(), raw.normals.cpu(),
+                                        raw.perturbation_delta.cpu(), raw.weights.cpu(), M)
+    sum((t * u).sum() for t, u in zip((p, n, dl, w), G)).backward()
+    for name, x, y in (("curvature", c, c2), ("conic", k, k2), ("aspheric", a, a2)):
+        gx = x.grad.double().cpu().numpy().reshape(-1)
+        gy = y.grad.numpy().reshape(-1)
+        err = np.abs(gx - gy).max() / np.abs(gy).max()
+        assert err < 1e-5, f"d/d{name}: {gx} vs {gy} ({err:.3g})"

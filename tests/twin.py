@@ -323,3 +323,33 @@ def soft_hex_kink_pixels(sensor, pts, band=1e-6, wmin=1e-6):
             if 0 <= qi < table.shape[0] and 0 <= ri < table.shape[1] and table[qi, ri] >= 0:
                 bad.append(int(table[qi, ri]))
     return np.unique(np.array(bad, dtype=np.int64))
+
+
+def resample_mapping(group, surf, pts, nrm, dlt, w, n_samples):
+    """The sampled arrays as functions of the surface parameters, FP64 torch
+    autograd (core/surfaces.py:41-65, core/reflection.py:22-49,
+    core/integrators.py:124-127): the aperture positions and the roughness
+    coefficients of drawn samples do not depend on the surface; points,
+    normals, deltas and weights do. Reference for the device sampler's
+    reverse (iact_sample_facets_backward)."""
+    from iactrace_gb300.core.reflection import perturbation_delta_from_normals
+    dev = pts.device
+    xy = pts[..., :2].double()
+    n0 = nrm.double()
+    ref_z = torch.tensor([0.0, 0.0, 1.0], dtype=torch.float64, device=dev)
+    ref_x = torch.tensor([1.0, 0.0, 0.0], dtype=torch.float64, device=dev)
+    ref = torch.where(n0[..., 2:3].abs() > 0.9, ref_x, ref_z)
+    t1 = torch.linalg.cross(n0, ref.expand_as(n0))
+    t1 = t1 / torch.linalg.norm(t1, dim=-1, keepdim=True)
+    t2 = torch.linalg.cross(n0, t1)
+    d0 = dlt.double()
+    th1, th2 = (d0 * t1).sum(-1), (d0 * t2).sum(-1)
+    s64 = type(surf)(surf.curvature if not isinstance(surf.curvature, torch.Tensor) else surf.curvature.double(),
+                     surf.conic if not isinstance(surf.conic, torch.Tensor) else surf.conic.double(),
+                     surf.aspheric.double())
+    off = group.offsets.reshape(-1, 1, 2).to(device=dev, dtype=torch.float64)
+    p, n = s64.point_and_normal(xy, off)
+    dl = perturbation_delta_from_normals(n, th1, th2)
+    area = (n0[..., 2] / w[..., 0].double() * n_samples).detach()
+    ww = n[..., 2:3] / area[..., None] * n_samples
+    return p, n, dl, ww
