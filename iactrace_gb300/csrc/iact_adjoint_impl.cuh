@@ -105,7 +105,7 @@ __device__ __forceinline__ void soft_square_bwd(const SensorK& s, const float* g
   for (int i = 0; i < n; ++i)
     for (int j = 0; j < n; ++j) {
       float ddx = xf - (float)(j - K), ddy = yf - (float)(i - K);
-      float w = expf(-0.5f * is2 * (ddx * ddx + ddy * ddy));
+      float w = __expf(-0.5f * is2 * (ddx * ddx + ddy * ddy));
       float wx = -w * ddx * is2 * s.inv_dx, wy = -w * ddy * is2 * s.inv_dy;  // dw/dx, dw/dy
       int xi = xi0 + j - K, yi = yi0 + i - K;
       float gk = (xi >= 0 && xi < s.width && yi >= 0 && yi < s.height) ? g[rowbase + yi * s.width + xi] : 0.f;
@@ -149,7 +149,7 @@ __device__ __forceinline__ void soft_hex_bwd(const SensorK& s, const TT* table, 
       bool first = ax >= m2;  // hex norm = max(|ux|, |ux|/2 + sqrt(3)/2 |uy|) / inradius
       float hd = (first ? ax : m2) * s.inv_inr;
       float a = hd * isg;
-      float w = expf(-0.5f * a * a);
+      float w = __expf(-0.5f * a * a);
       float dhx = (first ? 1.f : 0.5f) * (ux >= 0.f ? 1.f : -1.f) * s.inv_inr;
       float dhy = (first ? 0.f : 0.8660254037844386f) * (uy >= 0.f ? 1.f : -1.f) * s.inv_inr;
       float dwda = -w * a * isg;  // dw/dhd
@@ -352,6 +352,8 @@ __device__ __forceinline__ void adjoint_tile(const AdjK& p, const Obst& ob, cons
   int fl = (tb - sl * FCc * CCc) / CCc;
   int cl = tb - sl * FCc * CCc - fl * CCc;
   int cur_f = -1, cur_s = -1;
+  JBasis jb;  // tangent basis of the current source (extended sources)
+  int jb_s = -1;
   for (int t = tb; t < te; ++t) {
     const int s = s0 + sl, f = f0 + fl;
     if (f != cur_f) {
@@ -388,7 +390,11 @@ __device__ __forceinline__ void adjoint_tile(const AdjK& p, const Obst& ob, cons
       } else if (SRC == IACT_SRC_EXTENDED) {  // jitter regenerated from its counter
         float z0, z1;
         ray_normals(p.seed, s, f, mc, z0, z1);
-        d = jitter_dir(rsqrtf(dot(src, src)) * src, __ldg(p.sources + SS * s + 3), z0, z1);
+        if (s != jb_s) {  // warp-uniform
+          jb = jitter_basis(src);
+          jb_s = s;
+        }
+        d = jitter_dir(jb, __ldg(p.sources + SS * s + 3), z0, z1);
       } else {
         d = src;
       }

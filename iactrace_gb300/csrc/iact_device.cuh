@@ -870,9 +870,11 @@ __device__ __forceinline__ void ray_normals(uint32_t seed, int s, int f, int m, 
   philox4x32_10(c, seed, 0x5EEDu);
   const float u1 = (float)((c[0] >> 8) + 1u) * (1.0f / 16777216.0f);
   const float u2 = (float)(c[1] >> 8) * (1.0f / 16777216.0f);
-  const float rad = sqrtf(-2.f * logf(u1));
+  // hardware approximations (absolute error ~1e-6 in z0, z1: a jitter of
+  // sigma * 1e-6 rad, far below the binning and parity tolerances)
+  const float rad = sqrtf(-2.f * __logf(u1));
   float sn, cs;
-  sincospif(2.f * u2, &sn, &cs);
+  __sincosf(6.28318530717958647f * u2, &sn, &cs);
   z0 = rad * cs;
   z1 = rad * sn;
 }
@@ -880,12 +882,23 @@ __device__ __forceinline__ void ray_normals(uint32_t seed, int s, int f, int m, 
 // Extended source: unit direction dh (normalised source direction) tilted by
 // sigma * (z0 t1 + z1 t2) in its tangent plane, t1 = normalize(dh x ref),
 // ref = x if |dh_z| > 0.9 else z (the basis of core/reflection.py:40-47), t2 = dh x t1.
-__device__ __forceinline__ V3 jitter_dir(V3 dh, float sigma, float z0, float z1) {
+// The basis depends on the source only (computed once per source run).
+struct JBasis {
+  V3 dh, t1, t2;
+};
+__device__ __forceinline__ JBasis jitter_basis(V3 src) {
+  JBasis b;
+  b.dh = rsqrtf(dot(src, src)) * src;
+  const V3 dh = b.dh;
   const V3 ref = fabsf(dh.z) > 0.9f ? mk(1.f, 0.f, 0.f) : mk(0.f, 0.f, 1.f);
   V3 t1 = mk(dh.y * ref.z - dh.z * ref.y, dh.z * ref.x - dh.x * ref.z, dh.x * ref.y - dh.y * ref.x);
   t1 = rsqrtf(dot(t1, t1)) * t1;
-  const V3 t2 = mk(dh.y * t1.z - dh.z * t1.y, dh.z * t1.x - dh.x * t1.z, dh.x * t1.y - dh.y * t1.x);
-  V3 d = dh + sigma * (z0 * t1 + z1 * t2);
+  b.t1 = t1;
+  b.t2 = mk(dh.y * t1.z - dh.z * t1.y, dh.z * t1.x - dh.x * t1.z, dh.x * t1.y - dh.y * t1.x);
+  return b;
+}
+__device__ __forceinline__ V3 jitter_dir(const JBasis& b, float sigma, float z0, float z1) {
+  const V3 d = b.dh + sigma * (z0 * b.t1 + z1 * b.t2);
   return rsqrtf(dot(d, d)) * d;
 }
 

@@ -103,8 +103,9 @@ __global__ void __launch_bounds__(256) k_debug(const RenderK p, float* pts, floa
     constexpr int SS = (SRC == IACT_SRC_EXTENDED) ? 4 : 3;
     float z0 = 0.f, z1 = 0.f;
     if (SRC == IACT_SRC_EXTENDED) ray_normals(p.seed, s, f, m, z0, z1);
-    trace_ray<SRC, STAGES>(p, ob, mir, p.P4[si], p.N4[si],
-                           mk(p.sources[SS * s], p.sources[SS * s + 1], p.sources[SS * s + 2]),
+    const V3 src = mk(p.sources[SS * s], p.sources[SS * s + 1], p.sources[SS * s + 2]);
+    const JBasis jb = jitter_basis(src);
+    trace_ray<SRC, STAGES>(p, ob, mir, p.P4[si], p.N4[si], src, jb,
                            SRC == IACT_SRC_EXTENDED ? p.sources[SS * s + 3] : 0.f, z0, z1, p.values[s], x, y, val, hm,
                            nullptr, 0);
     pts[2 * i] = x;

@@ -218,14 +218,14 @@ __device__ __forceinline__ void splat_square(const SensorK& s, const Sink& sink,
   for (int i = 0; i < n; ++i)
     for (int j = 0; j < n; ++j) {
       float ddx = xf - (float)(j - K), ddy = yf - (float)(i - K);
-      tot += expf(inv2s * (ddx * ddx + ddy * ddy));
+      tot += __expf(inv2s * (ddx * ddx + ddy * ddy));
     }
   const float scale = ok ? v / tot : 0.f;
   const int xi0 = ok ? (int)xb : 0, yi0 = ok ? (int)yb : 0;
   for (int i = 0; i < n; ++i)
     for (int j = 0; j < n; ++j) {
       float ddx = xf - (float)(j - K), ddy = yf - (float)(i - K);
-      float w = expf(inv2s * (ddx * ddx + ddy * ddy)) * scale;
+      float w = __expf(inv2s * (ddx * ddx + ddy * ddy)) * scale;
       int xi = xi0 + j - K, yi = yi0 + i - K;
       bool in = ok && xi >= 0 && xi < s.width && yi >= 0 && yi < s.height;
       warp_add(sink, in ? rowbase + yi * s.width + xi : -1, w);
@@ -252,7 +252,7 @@ __device__ __forceinline__ void splat_hex(const SensorK& s, const TT* table, con
     for (int j = 0; j < 7; ++j) {
       const float a = hex_norm(ddx - s.hex_sx * ((float)dq[j] + 0.5f * (float)dr[j]),
                                ddy - s.hex_sy * (float)dr[j], s.inv_inr) * inv_sig;
-      w[j] = expf(-0.5f * (a * a));
+      w[j] = __expf(-0.5f * (a * a));
       tot += w[j];
     }
     const float scale = ok ? v / tot : 0.f;
@@ -279,7 +279,7 @@ __device__ __forceinline__ void splat_hex(const SensorK& s, const TT* table, con
       if (max(max(abs(q), abs(r)), abs(q + r)) > K) continue;
       float a = hex_norm(ddx - s.hex_sx * ((float)q + 0.5f * (float)r), ddy - s.hex_sy * (float)r, s.inv_inr) *
                 inv_sig;
-      tot += expf(-0.5f * (a * a));
+      tot += __expf(-0.5f * (a * a));
     }
   const float scale = ok ? v / tot : 0.f;
   for (int q = -K; q <= K; ++q)
@@ -287,7 +287,7 @@ __device__ __forceinline__ void splat_hex(const SensorK& s, const TT* table, con
       if (max(max(abs(q), abs(r)), abs(q + r)) > K) continue;
       float a = hex_norm(ddx - s.hex_sx * ((float)q + 0.5f * (float)r), ddy - s.hex_sy * (float)r, s.inv_inr) *
                 inv_sig;
-      float w = expf(-0.5f * (a * a)) * scale;
+      float w = __expf(-0.5f * (a * a)) * scale;
       int p = ok ? hex_lookup(s, table, qi + (float)q, ri + (float)r) : -1;
       warp_add(sink, p >= 0 ? rowbase + p : -1, w);
     }
@@ -299,7 +299,8 @@ __device__ __forceinline__ void splat_hex(const SensorK& s, const TT* table, con
 // candidate mask (n_words == 0: every primitive).
 template <int SRC, bool STAGES>
 __device__ __forceinline__ void trace_ray(const RenderK& p, const Obst& ob, const float* mir, float4 P,
-                                          float4 N, V3 src, float sigma, float z0, float z1, float v, float& x,
+                                          float4 N, V3 src, const JBasis& jb, float sigma, float z0, float z1,
+                                          float v, float& x,
                                           float& y, float& val, int& hit_mirror, const uint32_t* cmask,
                                           int n_words) {
   V3 tp = mk(P.x, P.y, P.z), tn = mk(N.x, N.y, N.z);
@@ -308,7 +309,7 @@ __device__ __forceinline__ void trace_ray(const RenderK& p, const Obst& ob, cons
     V3 dd = tp - src;  // dirs = normalize(tp - src)
     d = rsqrtf(dot(dd, dd)) * dd;
   } else if (SRC == IACT_SRC_EXTENDED) {
-    d = jitter_dir(rsqrtf(dot(src, src)) * src, sigma, z0, z1);
+    d = jitter_dir(jb, sigma, z0, z1);
   } else {
     d = src;  // parallel: the source entry is the direction, as given
   }
@@ -422,6 +423,8 @@ __device__ __forceinline__ void render_tile(const RenderK& p, const Obst& ob, co
   int rl_key = -1;  // run-length merged hit of this lane (hard sensors)
   float rl_val = 0.f;
   HexCache hc = {3.0e38f, 3.0e38f, -1};  // last hexagon of this lane (hard hex sensors)
+  JBasis jb;                             // tangent basis of the current source (extended sources)
+  int jb_s = -1;
   const int T = SBc * FCc * CCc;
   const int tb = (warp * T) / nw, te = ((warp + 1) * T) / nw;
   if (p.n_words) warp_masks<SRC>(p.B4, p.sources, p.M, p.n_words, ob, s0, f0, c0, FCc, CCc, tb, te, tmask);
@@ -437,14 +440,18 @@ __device__ __forceinline__ void render_tile(const RenderK& p, const Obst& ob, co
     const V3 src = mk(__ldg(p.sources + SS * s), __ldg(p.sources + SS * s + 1), __ldg(p.sources + SS * s + 2));
     const float sig = (SRC == IACT_SRC_EXTENDED) ? __ldg(p.sources + SS * s + 3) : 0.f;
     const float v = __ldg(p.values + s);
+    if (SRC == IACT_SRC_EXTENDED && s != jb_s) {  // warp-uniform
+      jb = jitter_basis(src);
+      jb_s = s;
+    }
     float x = 0.f, y = 0.f, val = 0.f;
     int hm;
     if (act) {
       const size_t si = (size_t)f * p.M + m;
       float z0 = 0.f, z1 = 0.f;
       if (SRC == IACT_SRC_EXTENDED) ray_normals(p.seed, s, f, m, z0, z1);
-      trace_ray<SRC, STAGES>(p, ob, mir, __ldg(p.P4 + si), __ldg(p.N4 + si), src, sig, z0, z1, v, x, y, val, hm,
-                             tmask + t * p.n_words, p.n_words);
+      trace_ray<SRC, STAGES>(p, ob, mir, __ldg(p.P4 + si), __ldg(p.N4 + si), src, jb, sig, z0, z1, v, x, y, val,
+                             hm, tmask + t * p.n_words, p.n_words);
     }
     int rowbase;
     if (MODE == IACT_MODE_RESPONSE) rowbase = (p.rows_in_smem ? sl : s) * p.P;
