@@ -5,8 +5,8 @@ differentiable function of the surface (FP64 torch restatement); the
 adjoint kernel returns per-sample sums dL/d(point, normal, 1/weight)
 (iact_render_backward g_samples) which RenderFunction maps to the arrays.
 Checked against the FP64 autograd twin on the same samples and the GPU's
-decisions (primary asphere coefficients "only through
-resampling"), tolerance GRAD_TOL."""
+decisions (the reference differentiates the primary's asphere coefficients
+only through resampling), tolerance GRAD_TOL."""
 from __future__ import annotations
 
 import numpy as np
