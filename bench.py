@@ -42,7 +42,10 @@ sys.path.insert(0, ROOT)
 METRIC = "traced rays/s: fwd and fwd+adjoint vs plain fwd kernel, img err<=1e-5 vs FP64"
 # algorithmic FP32 flops per ray (FMA = 2), reference evaluation without early-out:
 # point primary 26 + 4 cylinders x 98 + box 29 + sensor plane 34 + hex bin 56
-F_RAY = {"response": 537, "plain": 503, "cassegrain": 894, "batched": 537}
+F_RAY = {"response": 537, "plain": 503, "cassegrain": 894, "batched": 537,
+         # primary point source 26 + 271 cylinders x 98 + 2 spheres x 35 + box 29 + oriented box 47
+         # (rotation 18 + slab 29) + triangle 40 (Moller-Trumbore) + plane 34 + hex bin 56
+         "obstructed": 26 + 271 * 98 + 2 * 35 + 29 + 47 + 40 + 34 + 56}
 
 
 def _env_rank():
@@ -110,6 +113,8 @@ def build_workload(name: str):
         return W.plain_forward(), "image"
     if name == "cassegrain":
         return W.cassegrain(), "image"
+    if name == "obstructed":
+        return W.obstructed(), "image"
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -117,7 +122,8 @@ def workload_config(name, tel, S, mode, flush):
     F = sum(len(g) for g in tel.mirror_groups if g.optical_stage == 0)
     M = tel.mirror_groups[0].n_samples
     cfg = {"workload": {"response": "response_matrix_dc380_hex2048", "plain": "plain_forward_dc380_square960",
-                        "cassegrain": "cassegrain_61seg_square1024"}[name],
+                        "cassegrain": "cassegrain_61seg_square1024",
+                        "obstructed": "obstructed_dc380_struts271_hex960"}[name],
            "facets": F, "samples_per_facet": M, "sources": S,
            "pixels": int(math.prod(tel.sensors[0].get_accumulator_shape())),
            "output": "response matrix (S, P) fp32" if mode == "response" else "image fp32",
@@ -550,7 +556,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="response",
-                    choices=["response", "plain", "cassegrain", "alignment", "batched"])
+                    choices=["response", "plain", "cassegrain", "obstructed", "alignment", "batched"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--instances", type=int, default=64, help="batched workload: telescope variants")
     ap.add_argument("--max-sources", type=int, default=4096, help="batched workload: largest source count")
@@ -623,6 +629,25 @@ def main():
         tdist.barrier()
     step_s = sum(a.elapsed_time(b) for a, b in ev) / 1e3 / args.steps
     kern_s = sum(a.elapsed_time(b) for a, b in kev) / 1e3 / args.steps
+    culling = None
+    if args.workload == "obstructed":
+        # the same launches with every primitive tested on every ray
+        nc = N.IactOpts()
+        nc.flags = N.FLAG_NO_CULL
+        nev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        for a, b in nev:
+            a.record(stream)
+            b.record(stream)
+        fn(tel, src, val, stype, opts=nc)
+        for k in range(args.steps):
+            flush_buf.fill_(float(k))
+            nc.kernel_events[0] = nev[k][0].cuda_event
+            nc.kernel_events[1] = nev[k][1].cuda_event
+            fn(tel, src, val, stype, opts=nc)
+        torch.cuda.synchronize(dev)
+        nc_s = sum(a.elapsed_time(b) for a, b in nev) / 1e3 / args.steps
+        culling = {"kernel_ms": kern_s * 1e3, "no_cull_kernel_ms": nc_s * 1e3, "speedup": nc_s / kern_s,
+                   "primitives": 276, "note": "exact warp-bundle culling vs every primitive on every ray"}
 
     # forward + adjoint through torch.autograd (recompute-based adjoint kernel)
     grp = tel.mirror_groups[0]
@@ -746,6 +771,7 @@ def main():
                      "peak_source": "measured live: FP32 FMA-chain probe kernel (iact_probe_fma)"},
         "fwd_adjoint": fwdadj,
         "gpu_launches": 3 * args.steps,  # k_prep, k_render, k_finish per step
+        **({"culling": culling} if culling else {}),
         "clocks": clk,
     }
     if rank == 0 and not args.no_cpu_baseline:

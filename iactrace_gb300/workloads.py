@@ -176,6 +176,39 @@ def cassegrain(n_samples: int = 500, n_sources: int = 64, seed: int = 0, with_as
     return tel, src, torch.ones(n_sources), "point"
 
 
+def strut_lattice(n_struts: int = 270, seed: int = 0):
+    """Obstructions with a CT5-like primitive count: n_struts thin cylinders
+    (radius 1-6 cm) at random between the dish and the camera, an axial
+    strut, two spheres, an oriented box, a triangle and the camera box."""
+    from .core import Box, Cylinder, OrientedBox, Sphere, Triangle
+    from .core.transforms import euler_to_matrix
+    rng = np.random.default_rng(seed + 5)
+    prims = []
+    for _ in range(n_struts):
+        a0, a1 = rng.uniform(0, 2 * math.pi, 2)
+        r0, r1 = rng.uniform(0.5, 7.5), rng.uniform(0.2, 2.0)
+        z0, z1 = rng.uniform(0.5, 6.0), rng.uniform(9.0, 15.5)
+        prims.append(Cylinder([r0 * math.cos(a0), r0 * math.sin(a0), z0], [r1 * math.cos(a1), r1 * math.sin(a1), z1],
+                              float(rng.uniform(0.01, 0.06))))
+    prims.append(Cylinder([0.0, 0.0, 2.0], [0.0, 0.0, 14.0], 0.08))  # a vertical strut on the axis
+    prims += [Sphere([1.0, 0.5, 8.0], 0.4), Sphere([-2.0, 1.0, 5.0], 0.3),
+              OrientedBox([0.0, -2.0, 7.0], [0.8, 0.3, 0.4], euler_to_matrix(torch.tensor([10.0, 20.0, 30.0]))),
+              Triangle([-1.0, -1.0, 9.0], [1.5, -0.5, 9.5], [0.0, 1.5, 8.5]),
+              Box([-0.75, -0.75, 15.0], [0.75, 0.75, 16.6])]
+    return prims
+
+
+def obstructed(n_samples: int = 256, n_sources: int = 16, n_struts: int = 270, seed: int = 0, pixels: int = 960):
+    """Davies-Cotton dish under a lattice of struts (strut_lattice), hex
+    camera, point sources: the large-obstruction-set case of the shadow
+    test. Returns (telescope, sources, values, source_type)."""
+    from .core import group_obstructions
+    groups, _ = davies_cotton(n_samples=n_samples, seed=seed, obstructions=False)
+    tel = Telescope(groups, group_obstructions(strut_lattice(n_struts, seed)), [hex_camera(pixels)],
+                    name="dc380_struts")
+    return tel, point_sources_disk(n_sources, 2.5, seed + 21), torch.ones(n_sources), "point"
+
+
 def _first_facets(g, n: int, rot):
     """The first n facets of a sampled polygon-aperture group, with rotations `rot`."""
     return g.replace(positions=g.positions[:n], rotations=rot, offsets=g.offsets[:n], vertices=g.vertices[:n],

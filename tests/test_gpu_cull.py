@@ -59,23 +59,9 @@ def _same(tel, src, val, st, mode="image", seed=0):
 def lattice_scene(n_cyl=270, n_samples=32, seed=0):
     """A dish under a lattice of thin struts (CT5-like primitive count):
     n_cyl random cylinders between the rim and the camera, plus the camera
-    box, spheres, an oriented box and triangles."""
+    box, spheres, an oriented box and triangles (workloads.strut_lattice)."""
     groups, _ = W.davies_cotton(n_samples=n_samples, seed=seed, obstructions=False)
-    rng = np.random.default_rng(seed + 5)
-    prims = []
-    for _ in range(n_cyl):
-        a0, a1 = rng.uniform(0, 2 * math.pi, 2)
-        r0, r1 = rng.uniform(0.5, 7.5), rng.uniform(0.2, 2.0)
-        z0, z1 = rng.uniform(0.5, 6.0), rng.uniform(9.0, 15.5)
-        prims.append(Cylinder([r0 * math.cos(a0), r0 * math.sin(a0), z0], [r1 * math.cos(a1), r1 * math.sin(a1), z1],
-                              float(rng.uniform(0.01, 0.06))))
-    prims.append(Cylinder([0.0, 0.0, 2.0], [0.0, 0.0, 14.0], 0.08))  # a vertical strut on the axis
-    prims += [Sphere([1.0, 0.5, 8.0], 0.4), Sphere([-2.0, 1.0, 5.0], 0.3),
-              OrientedBox([0.0, -2.0, 7.0], [0.8, 0.3, 0.4], euler_to_matrix(torch.tensor([10.0, 20.0, 30.0]))),
-              Triangle([-1.0, -1.0, 9.0], [1.5, -0.5, 9.5], [0.0, 1.5, 8.5])]
-    from iactrace_gb300.core import Box
-    prims.append(Box([-0.75, -0.75, 15.0], [0.75, 0.75, 16.6]))
-    return Telescope(groups, group_obstructions(prims), [W.hex_camera(960)])
+    return Telescope(groups, group_obstructions(W.strut_lattice(n_cyl, seed)), [W.hex_camera(960)])
 
 
 def test_cull_exact_plain_and_response(cuda):
