@@ -2,8 +2,8 @@
 
 Same public names as the reference package (GerritRo/iactrace v0.4.0,
 iactrace/__init__.py): Telescope, Mirror, Integrator, MCIntegrator,
-SquareSensor, HexagonalSensor, load_telescope; plotting is not part of this
-package. Rendering runs in hand-written CUDA kernels behind a C ABI
+SquareSensor, HexagonalSensor, load_telescope; plotting data (no drawing) is in
+iactrace_gb300.viz. Rendering runs in hand-written CUDA kernels behind a C ABI
 (include/iactrace_gb300.h).
 """
 from .core import BatchRenderer, DeviceIntegrator, Integrator, MCIntegrator, render, render_debug, render_response_matrix
