@@ -48,6 +48,12 @@ F_RAY = {"response": 537, "plain": 503, "cassegrain": 894, "batched": 537,
          "obstructed": 26 + 271 * 98 + 2 * 35 + 29 + 47 + 40 + 34 + 56}
 
 
+# DRAM bytes (read + write) per launch of the workload's render kernel from
+# one ncu capture of the same kernel and workload (summaries under profiles/)
+TRAFFIC = {"response": (7.35e6, "profiles/k_render_response_matrix_dc380_hex2048.md"),
+           "cassegrain": (1.05e6, "profiles/k_render_cassegrain_61seg_square1024.md")}
+
+
 def _env_rank():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
 
@@ -766,7 +772,10 @@ def main():
         "e2e": {"value": rays * world / e2e_s, "unit": "rays/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-                     "traffic": None, "kernel": "k_render", "kernel_ms": kern_s * 1e3,
+                     "traffic": TRAFFIC[args.workload][0] if args.workload in TRAFFIC else None,
+                     "traffic_unit": "bytes per launch (ncu dram__bytes_read + write)",
+                     "traffic_source": TRAFFIC[args.workload][1] if args.workload in TRAFFIC else None,
+                     "kernel": "k_render", "kernel_ms": kern_s * 1e3,
                      "flops_per_ray": F_RAY[args.workload],
                      "peak_source": "measured live: FP32 FMA-chain probe kernel (iact_probe_fma)"},
         "fwd_adjoint": fwdadj,
