@@ -159,7 +159,7 @@ int plan_adjoint(AdjK& p, const iact_sensor_t* sn, int block, size_t& smem, long
   const size_t htab_bytes = sizeof(short) * ((htab + 7) & ~(size_t)7);
   p.hex_in_smem = (hex && sn->n_pixels < 32768 && tab_bytes + htab_bytes <= 96 * 1024) ? 1 : 0;
   smem = tab_bytes + (p.hex_in_smem ? htab_bytes : 0) + sizeof(float) * (size_t)p.n_mir * kMirGrad +
-         sizeof(uint32_t) * (size_t)p.n_words * p.SB * p.FC * p.CC;
+         sizeof(uint32_t) * (size_t)p.n_words * p.SB * p.FC;
   return IACT_OK;
 }
 

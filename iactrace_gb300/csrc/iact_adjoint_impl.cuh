@@ -31,7 +31,7 @@ struct AdjK {
   int SB, FC, CC, n_fchunk, n_cchunk, n_tiles;
   int* counter;
   uint32_t seed;  // jitter stream of extended sources
-  const float4* B4;  // per (facet, chunk) bundle bounds (culling on)
+  const float4* B4;  // per facet bundle bounds (culling on)
   int n_words;       // 32-bit candidate-mask words per task; 0 = no culling
   float* gsamp;      // optional [F*M, 7]: per sample dL/d(world point, perturbed normal, 1/weight)
   int want_mgrad;    // stage-mirror parameter gradients requested (gmir)
@@ -347,7 +347,7 @@ __device__ __forceinline__ void adjoint_tile(const AdjK& p, const Obst& ob, cons
   const int SBc = min(p.SB, p.S - s0), FCc = min(p.FC, p.F - f0), CCc = min(p.CC, nch - c0);
   const int T = SBc * FCc * CCc;
   const int tb = (warp * T) / nw, te = ((warp + 1) * T) / nw;
-  if (p.n_words) warp_masks<SRC>(p.B4, p.sources, p.M, p.n_words, ob, s0, f0, c0, FCc, CCc, tb, te, tmask);
+  if (p.n_words) warp_masks<SRC>(p.B4, p.sources, p.n_words, ob, s0, f0, FCc, CCc, tb, te, tmask);
   int sl = tb / (FCc * CCc);
   int fl = (tb - sl * FCc * CCc) / CCc;
   int cl = tb - sl * FCc * CCc - fl * CCc;
@@ -398,7 +398,8 @@ __device__ __forceinline__ void adjoint_tile(const AdjK& p, const Obst& ob, cons
       } else {
         d = src;
       }
-      const bool shadowed = occluded_mask(ob, tmask + t * p.n_words, p.n_words, tp, mk(-d.x, -d.y, -d.z));
+      const bool shadowed = occluded_mask(ob, tmask + (sl * FCc + fl) * p.n_words, p.n_words, tp,
+                                          mk(-d.x, -d.y, -d.z));
       const float c = dot(d, nn);
       const V3 r0 = d - (2.f * c) * nn;
       const float val0 = v * -c * iw;

@@ -37,7 +37,7 @@ __global__ void __launch_bounds__(256) k_batch_prep(const BatchJob* __restrict__
   const PrepK& p = backward ? J.pkb : J.pk;
   if (blockIdx.x == 0) prep_tables(p);
   const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  prep_chunks(p, w, ((long long)gridDim.x * blockDim.x) >> 5);
+  prep_units(p, w, ((long long)gridDim.x * blockDim.x) >> 5);
   if (backward)
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < J.gr.n_bucket;
          i += (long long)gridDim.x * blockDim.x)
@@ -255,7 +255,7 @@ int iact_batch_create(const iact_job_t* jobs, int32_t n_jobs, int32_t source_typ
         htab_floor = std::max(htab_floor, sp.htab_bytes);
     }
     size_t masks = 0;  // candidate masks of one tile, largest over the class
-    for (int i : mem) masks = std::max(masks, sizeof(uint32_t) * (size_t)rk[i].n_words * rk[i].SB * rk[i].FC * rk[i].CC);
+    for (int i : mem) masks = std::max(masks, sizeof(uint32_t) * (size_t)rk[i].n_words * rk[i].SB * rk[i].FC);
     size_t hist = 0;
     long long tile = 0;
     for (int i : mem) {
@@ -290,7 +290,7 @@ int iact_batch_create(const iact_job_t* jobs, int32_t n_jobs, int32_t source_typ
         if (a.hex_in_smem)
           ahtab = std::max(ahtab, sizeof(short) * (((size_t)a.sn.table_q * a.sn.table_r + 7) & ~(size_t)7));
         amir = std::max(amir, sizeof(float) * (size_t)a.n_mir * kMirGrad);
-        amask = std::max(amask, sizeof(uint32_t) * (size_t)a.n_words * a.SB * a.FC * a.CC);
+        amask = std::max(amask, sizeof(uint32_t) * (size_t)a.n_words * a.SB * a.FC);
         at += a.n_tiles;
       }
       if (at > 0x7fffffffLL || atab + ahtab + amir + amask > budget) {

@@ -28,7 +28,7 @@ struct WsLayout {
   size_t p4;       // float4 [F*M] world point, 1/weight
   size_t n4;       // float4 [F*M] perturbed world normal
   size_t d4;       // float4 [F*M] world delta / |n + scale delta| (backward only)
-  size_t b4;       // float4 [F*ceil(M/32)] bundle centre, radius (scenes with obstructions)
+  size_t b4;       // float4 [F] facet bundle centre, radius (scenes with obstructions)
   size_t n_b4;     // entries of b4 (0: no obstructions, no culling)
   size_t acc;      // double: [rows * P] render accumulator, or the gradient buckets
   size_t total;

@@ -34,7 +34,7 @@ namespace iact {
 __global__ void __launch_bounds__(256) k_prep(const PrepK p) {
   if (blockIdx.x == 0) prep_tables(p);
   const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  prep_chunks(p, w, ((long long)gridDim.x * blockDim.x) >> 5);
+  prep_units(p, w, ((long long)gridDim.x * blockDim.x) >> 5);
 }
 
 template <int SRC, bool SOFT, int MODE, bool STAGES>
@@ -206,7 +206,8 @@ PrepK prep_params(const iact_scene_t* sc, const WsLayout& L, char* ws, bool with
 
 int launch_prep(const iact_scene_t* sc, const WsLayout& L, char* ws, cudaStream_t st, bool with_delta) {
   const PrepK p = prep_params(sc, L, ws, with_delta);
-  const long long units = (long long)p.F * ((p.M + 31) / 32);  // one warp per (facet, 32-sample chunk)
+  // one warp per (facet, 32-sample chunk), plus one per facet bound with culling
+  const long long units = (long long)p.F * ((p.M + 31) / 32) + (p.B4 ? p.F : 0);
   const int blocks = (int)std::min<long long>(std::max<long long>(1, (units + 7) / 8), 65535);
   k_prep<<<blocks, 256, 0, st>>>(p);
   return check_cuda(cudaGetLastError(), "k_prep launch");
@@ -308,7 +309,7 @@ WsLayout workspace_layout(const iact_scene_t* sc, size_t acc_elems, bool with_de
   L.d4 = off;
   if (with_delta) off = align256(off + sizeof(float4) * n);
   L.b4 = off;  // bundle bounds, only for scenes with obstructions
-  L.n_b4 = n_primitives(sc) > 0 ? (size_t)std::max(sc->n_facets, 0) * ((std::max(sc->n_samples, 0) + 31) / 32) : 0;
+  L.n_b4 = n_primitives(sc) > 0 ? (size_t)std::max(sc->n_facets, 0) : 0;
   off = align256(off + sizeof(float4) * L.n_b4);
   L.acc = off;
   off = align256(off + sizeof(double) * acc_elems);
@@ -406,7 +407,7 @@ int launch_render(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type,
   DevInfo di = device_info();
   rc = plan_tiles(p, mode, block, opts, 8LL * std::max(di.sm_count, 1));
   if (rc) return rc;
-  const size_t mask_bytes = sizeof(uint32_t) * (size_t)p.n_words * p.SB * p.FC * p.CC;
+  const size_t mask_bytes = sizeof(uint32_t) * (size_t)p.n_words * p.SB * p.FC;
   const size_t budget = (size_t)std::min(di.smem_optin > 0 ? di.smem_optin : 49152, 200 * 1024) - mask_bytes;
   SmemPlan sp;
   rc = plan_smem(sn, L.n_table_floats, p.SB, mode, opts ? opts->hist_mode : 0, budget, 0, 0, sp);

@@ -25,7 +25,7 @@ struct PrepK {
   float4* P4;
   float4* N4;
   float4* D4;  // optional: world delta / |n + scale delta| (roughness-scale gradients)
-  float4* B4;  // optional: per (facet, 32-sample chunk) bundle centre and radius
+  float4* B4;  // optional (culling): per facet bundle centre and radius
   float* tables;
   const float* cyl;
   const float* box;
@@ -127,34 +127,45 @@ __device__ __forceinline__ V3 prep_sample(const PrepK& p, long long i) {
   return pw;
 }
 
-// World samples of (facet, 32-sample chunk) units, one warp per unit (warp
-// `w0` of `nw` warps striding over the units), and each unit's bundle
-// bound B4 = (centre of its world points, largest distance from it).
-__device__ __forceinline__ void prep_chunks(const PrepK& p, long long w0, long long nw) {
+// Bundle bound of facet f for the candidate masks, one warp: B4[f] =
+// (facet position, largest |p| of its local sample points). Every world
+// point R p + pos lies within |p| of pos (rotations keep lengths), so the
+// sphere bounds the facet's samples exactly, and no rotation is needed
+// (this runs beside the sample warps of the same launch). The local origin
+// is the facet's centre, so the sphere is nearly as tight as one about the
+// points' centroid; Monte-Carlo samples cover a facet at random, so one
+// mask per (source, facet) serves all of its 32-sample chunks.
+__device__ __forceinline__ void facet_bound(const PrepK& p, int f) {
+  const int lane = threadIdx.x & 31;
+  const float* pts = p.points + (size_t)f * p.M * 3;
+  float r2 = 0.f;
+#pragma unroll 4
+  for (int m = lane; m < p.M; m += 32) {
+    const float x = __ldg(pts + 3 * m), y = __ldg(pts + 3 * m + 1), z = __ldg(pts + 3 * m + 2);
+    r2 = fmaxf(r2, x * x + y * y + z * z);
+  }
+#pragma unroll
+  for (int k = 16; k > 0; k >>= 1) r2 = fmaxf(r2, __shfl_xor_sync(kFull, r2, k));
+  if (lane == 0)
+    p.B4[f] = make_float4(p.facet_pos[3 * f], p.facet_pos[3 * f + 1], p.facet_pos[3 * f + 2],
+                          sqrtf(r2) * 1.0001f + 1e-6f);
+}
+
+// World samples of (facet, 32-sample chunk) units, one warp per unit, then
+// (with culling) one warp per facet bound: warp `w0` of `nw` warps strides
+// over both.
+__device__ __forceinline__ void prep_units(const PrepK& p, long long w0, long long nw) {
   const int lane = threadIdx.x & 31;
   const int nch = (p.M + 31) >> 5;
   const long long units = (long long)p.F * nch;
-  for (long long u = w0; u < units; u += nw) {
-    const int f = (int)(u / nch), m = (int)(u - (long long)f * nch) * 32 + lane;
-    const bool act = m < p.M;
-    V3 pw = mk(0.f, 0.f, 0.f);
-    if (act) pw = prep_sample(p, (long long)f * p.M + m);
-    if (p.B4) {
-      float n = act ? 1.f : 0.f, sx = pw.x, sy = pw.y, sz = pw.z;
-#pragma unroll
-      for (int k = 16; k > 0; k >>= 1) {
-        n += __shfl_xor_sync(kFull, n, k);
-        sx += __shfl_xor_sync(kFull, sx, k);
-        sy += __shfl_xor_sync(kFull, sy, k);
-        sz += __shfl_xor_sync(kFull, sz, k);
-      }
-      const V3 c = (1.f / n) * mk(sx, sy, sz);
-      V3 w = pw - c;
-      float r2 = act ? dot(w, w) : 0.f;
-#pragma unroll
-      for (int k = 16; k > 0; k >>= 1) r2 = fmaxf(r2, __shfl_xor_sync(kFull, r2, k));
-      if (lane == 0) p.B4[u] = make_float4(c.x, c.y, c.z, sqrtf(r2) * 1.0001f + 1e-6f);
+  const long long total = units + (p.B4 ? p.F : 0);
+  for (long long u = w0; u < total; u += nw) {
+    if (u >= units) {
+      facet_bound(p, (int)(u - units));
+      continue;
     }
+    const int f = (int)(u / nch), m = (int)(u - (long long)f * nch) * 32 + lane;
+    if (m < p.M) prep_sample(p, (long long)f * p.M + m);
   }
 }
 
@@ -176,7 +187,7 @@ struct RenderK {
   int n_fchunk, n_cchunk, n_tiles;
   int* counter;
   uint32_t seed;  // jitter stream of extended sources
-  const float4* B4;  // per (facet, chunk) bundle bounds (culling on)
+  const float4* B4;  // per facet bundle bounds (culling on)
   int n_words;       // 32-bit candidate-mask words per task; 0 = no culling
 };
 
@@ -382,18 +393,22 @@ __device__ __forceinline__ void bundle_axis(V3 src, float sigma, V3 c, float R0,
 // bundle is decoded once and its word assembled in a register; no
 // CTA-wide barrier (each warp reads only its own tasks' masks).
 template <int SRC>
-__device__ __forceinline__ void warp_masks(const float4* B4, const float* sources, int M, int nw, const Obst& ob,
-                                           int s0, int f0, int c0, int FCc, int CCc, int tb, int te,
-                                           uint32_t* mask) {
+// Candidate masks of the (source, facet) pairs of this warp's tasks
+// [tb, te) (tasks are ordered (source, facet, chunk): a pair's CCc chunk
+// tasks share its mask): lane = (pair, 32-primitive word); mask index =
+// pair * nw + word, pair = source_local * FCc + facet_local. Pairs at the
+// ends of the range may also be computed by the neighbouring warp, which
+// writes the same words.
+__device__ __forceinline__ void warp_masks(const float4* B4, const float* sources, int nw, const Obst& ob,
+                                           int s0, int f0, int FCc, int CCc, int tb, int te, uint32_t* mask) {
   const int np = ob.n_cyl + ob.n_box + ob.n_sph + ob.n_obox + ob.n_tri;
-  const int nch = (M + 31) >> 5;
   constexpr int SS = (SRC == IACT_SRC_EXTENDED) ? 4 : 3;
-  for (int i = tb * nw + (threadIdx.x & 31); i < te * nw; i += 32) {
-    const int t = i / nw, w = i - t * nw;
-    const int sl = t / (FCc * CCc), rem = t - sl * FCc * CCc;
-    const int fl = rem / CCc, cl = rem - fl * CCc;
+  const int pb = tb / CCc, pe = (te + CCc - 1) / CCc;
+  for (int i = pb * nw + (threadIdx.x & 31); i < pe * nw; i += 32) {
+    const int q = i / nw, w = i - q * nw;
+    const int sl = q / FCc, fl = q - sl * FCc;
     const int s = s0 + sl;
-    const float4 B = __ldg(B4 + (size_t)(f0 + fl) * nch + c0 + cl);
+    const float4 B = __ldg(B4 + f0 + fl);
     Bundle bd;
     bd.c = mk(B.x, B.y, B.z);
     bd.R0 = B.w;
@@ -427,7 +442,7 @@ __device__ __forceinline__ void render_tile(const RenderK& p, const Obst& ob, co
   int jb_s = -1;
   const int T = SBc * FCc * CCc;
   const int tb = (warp * T) / nw, te = ((warp + 1) * T) / nw;
-  if (p.n_words) warp_masks<SRC>(p.B4, p.sources, p.M, p.n_words, ob, s0, f0, c0, FCc, CCc, tb, te, tmask);
+  if (p.n_words) warp_masks<SRC>(p.B4, p.sources, p.n_words, ob, s0, f0, FCc, CCc, tb, te, tmask);
   // task t = (source sl, facet fl, chunk cl), chunk fastest; decoded once
   int sl = tb / (FCc * CCc);
   int fl = (tb - sl * FCc * CCc) / CCc;
@@ -451,7 +466,7 @@ __device__ __forceinline__ void render_tile(const RenderK& p, const Obst& ob, co
       float z0 = 0.f, z1 = 0.f;
       if (SRC == IACT_SRC_EXTENDED) ray_normals(p.seed, s, f, m, z0, z1);
       trace_ray<SRC, STAGES>(p, ob, mir, __ldg(p.P4 + si), __ldg(p.N4 + si), src, jb, sig, z0, z1, v, x, y, val,
-                             hm, tmask + t * p.n_words, p.n_words);
+                             hm, tmask + (sl * FCc + fl) * p.n_words, p.n_words);
     }
     int rowbase;
     if (MODE == IACT_MODE_RESPONSE) rowbase = (p.rows_in_smem ? sl : s) * p.P;
