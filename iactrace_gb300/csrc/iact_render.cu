@@ -405,7 +405,13 @@ int launch_render(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type,
   int block = (opts && opts->block_threads > 0) ? opts->block_threads : 256;
   if (block % 32 || block > 256) return set_error(IACT_E_INVALID, "opts.block_threads must be a multiple of 32, <= 256");
   DevInfo di = device_info();
-  rc = plan_tiles(p, mode, block, opts, 8LL * std::max(di.sm_count, 1));
+  // tiles per SM below which small launches shrink their tiles: each tile
+  // ends with a flush of its histogram rows, so cheap rays (single-stage
+  // scenes) want fewer, larger tiles and costly rays (stage mirrors) a finer
+  // balance (measured: 1000-sample plain forward 7 % faster at 4 than at 8
+  // per SM, the Cassegrain forward 13 % slower)
+  const long long tiles_per_sm = sc->n_mirrors > 0 ? 8 : 4;
+  rc = plan_tiles(p, mode, block, opts, tiles_per_sm * std::max(di.sm_count, 1));
   if (rc) return rc;
   const size_t mask_bytes = sizeof(uint32_t) * (size_t)p.n_words * p.SB * p.FC;
   const size_t budget = (size_t)std::min(di.smem_optin > 0 ? di.smem_optin : 49152, 200 * 1024) - mask_bytes;
