@@ -19,11 +19,17 @@ from .. import _native as N
 
 
 def stages_of(tel):
-    """core/render.py:12-18 _get_stages."""
+    """core/render.py:12-18 _get_stages (cached per telescope and group list)."""
+    key = tuple(map(id, tel.mirror_groups))
+    hit = tel.__dict__.get("_stages")
+    if hit is not None and hit[0] == key:
+        return hit[1]
     by = defaultdict(list)
     for g in tel.mirror_groups:
         by[g.optical_stage].append(g)
-    return dict(sorted(by.items()))
+    out = dict(sorted(by.items()))
+    tel.__dict__["_stages"] = (key, out)
+    return out
 
 
 def _f32(t, device):
@@ -196,9 +202,14 @@ class PackedScene:
             self.desc.facet_scale = scale.data_ptr()
 
     def workspace_bytes(self, sensor_desc, n_sources: int, mode: int) -> int:
+        key = (ctypes.addressof(sensor_desc), bytes(sensor_desc), int(n_sources), int(mode))
+        cache = self.__dict__.setdefault("_ws_bytes", {})
+        if key in cache:
+            return cache[key]
         size = ctypes.c_size_t(0)
         N.check(N.load().iact_workspace_size(ctypes.byref(self.desc), ctypes.byref(sensor_desc), int(n_sources),
                                              int(mode), ctypes.byref(size)))
+        cache[key] = int(size.value)
         return int(size.value)
 
 

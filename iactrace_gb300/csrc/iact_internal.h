@@ -48,7 +48,9 @@ DevInfo device_info();
 // CTAs of `kern` an SM holds at (block, smem), cached per device and launch
 // shape; raises the kernel's dynamic shared-memory limit when smem > 48 KiB.
 int resident_ctas(const void* kern, int block, size_t smem, int* per_sm);
-int launch_prep(const iact_scene_t* sc, const WsLayout& L, char* ws, cudaStream_t st, bool with_delta);
+// zero / zero_bytes: a region the prep launch clears; counter: 16 ints it clears
+int launch_prep(const iact_scene_t* sc, const WsLayout& L, char* ws, cudaStream_t st, bool with_delta,
+                void* zero = nullptr, size_t zero_bytes = 0, int* counter = nullptr);
 void host_euler(const float* deg, float* R);
 SensorK make_sensor(const iact_sensor_t* s);
 

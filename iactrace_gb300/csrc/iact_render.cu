@@ -33,6 +33,10 @@ namespace iact {
 
 __global__ void __launch_bounds__(256) k_prep(const PrepK p) {
   if (blockIdx.x == 0) prep_tables(p);
+  if (p.counter && blockIdx.x == 0 && threadIdx.x < 16) p.counter[threadIdx.x] = 0;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < p.n_zero;
+       i += (long long)gridDim.x * blockDim.x)
+    p.zero[i] = make_uint4(0u, 0u, 0u, 0u);
   const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   prep_units(p, w, ((long long)gridDim.x * blockDim.x) >> 5);
 }
@@ -189,6 +193,7 @@ int n_primitives(const iact_scene_t* sc) { return sc->n_cyl + sc->n_box + sc->n_
 
 PrepK prep_params(const iact_scene_t* sc, const WsLayout& L, char* ws, bool with_delta) {
   PrepK p;
+  memset(&p, 0, sizeof(p));
   p.F = sc->n_facets; p.M = sc->n_samples;
   p.facet_pos = sc->facet_pos; p.facet_rot = sc->facet_rot; p.facet_scale = sc->facet_scale;
   p.points = sc->points; p.normals = sc->normals; p.delta = sc->delta; p.weights = sc->weights;
@@ -204,11 +209,16 @@ PrepK prep_params(const iact_scene_t* sc, const WsLayout& L, char* ws, bool with
   return p;
 }
 
-int launch_prep(const iact_scene_t* sc, const WsLayout& L, char* ws, cudaStream_t st, bool with_delta) {
-  const PrepK p = prep_params(sc, L, ws, with_delta);
+int launch_prep(const iact_scene_t* sc, const WsLayout& L, char* ws, cudaStream_t st, bool with_delta, void* zero,
+                size_t zero_bytes, int* counter) {
+  PrepK p = prep_params(sc, L, ws, with_delta);
+  p.zero = static_cast<uint4*>(zero);
+  p.n_zero = zero ? (long long)((zero_bytes + 15) / 16) : 0;
+  p.counter = counter;
   // one warp per (facet, 32-sample chunk), plus one per facet bound with culling
   const long long units = (long long)p.F * ((p.M + 31) / 32) + (p.B4 ? p.F : 0);
-  const int blocks = (int)std::min<long long>(std::max<long long>(1, (units + 7) / 8), 65535);
+  const long long zb = (p.n_zero + 256LL * 8 - 1) / (256LL * 8);  // about 8 words per thread
+  const int blocks = (int)std::min<long long>(std::max<long long>({1LL, (units + 7) / 8, zb}), 65535);
   k_prep<<<blocks, 256, 0, st>>>(p);
   return check_cuda(cudaGetLastError(), "k_prep launch");
 }
@@ -392,11 +402,8 @@ int launch_render(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type,
     if (n_acc) return check_cuda(cudaMemsetAsync(out, 0, n_acc * sizeof(float), st), "zero output");
     return IACT_OK;
   }
-  rc = check_cuda(cudaMemsetAsync(w + L.counter, 0, 64, st), "reset tile counter");
-  if (rc) return rc;
-  rc = check_cuda(cudaMemsetAsync(w + L.acc, 0, n_acc * sizeof(double), st), "zero accumulator");
-  if (rc) return rc;
-  rc = launch_prep(sc, L, w, st, false);
+  // the prep launch also clears the tile counter and the accumulator
+  rc = launch_prep(sc, L, w, st, false, w + L.acc, n_acc * sizeof(double), reinterpret_cast<int*>(w + L.counter));
   if (rc) return rc;
 
   RenderK p = base_params(sc, sn, L, w, sources, values, S);

@@ -34,6 +34,9 @@ struct PrepK {
   const float* tri;
   const iact_mirror_t* mirrors;
   int n_cyl, n_box, n_sph, n_obox, n_tri, n_mir;
+  uint4* zero;         // optional: region cleared by the prep launch (the accumulator)
+  long long n_zero;    // its size in 16-byte words
+  int* counter;        // optional: 16 ints cleared (tile counter, error word)
 };
 
 // Per-launch constant tables: telescope/mirrors.py and core/obstructions.py

@@ -9,6 +9,7 @@ from __future__ import annotations
 import numpy as np
 import torch
 
+from ._pack import pack_cached
 from .. import _native as N
 
 SQRT3 = 1.7320508075688772
@@ -105,6 +106,11 @@ class HexagonalSensor:
         return (self.n_pixels,)
 
     def pack(self, device) -> tuple[N.IactSensor, list]:
+        """The iact_sensor_t of this sensor on `device` (cached while its pose
+        tensors and scalar settings are unchanged)."""
+        return pack_cached(self, device, self._pack)
+
+    def _pack(self, device) -> tuple[N.IactSensor, list]:
         key = str(device)
         if key not in self._dev_table:
             self._dev_table[key] = self.lookup_table.to(device=device, dtype=torch.int32).contiguous()

@@ -8,6 +8,7 @@ from __future__ import annotations
 import numpy as np
 import torch
 
+from ._pack import pack_cached
 from .. import _native as N
 
 
@@ -38,6 +39,11 @@ class SquareSensor:
         return self.width * self.height
 
     def pack(self, device) -> tuple[N.IactSensor, list]:
+        """The iact_sensor_t of this sensor on `device` (cached while its pose
+        tensors and scalar settings are unchanged)."""
+        return pack_cached(self, device, self._pack)
+
+    def _pack(self, device) -> tuple[N.IactSensor, list]:
         s = N.IactSensor()
         s.type = self.kind
         s.n_pixels = self.n_pixels

@@ -26,6 +26,7 @@ class Telescope:
     def __getstate__(self):
         st = dict(self.__dict__)
         st.pop("_packed", None)
+        st.pop("_stages", None)
         return st
 
     @classmethod
