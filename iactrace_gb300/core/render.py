@@ -35,10 +35,23 @@ def source_code(source_type) -> int:
     return N.SRC_PARALLEL
 
 
+def _ready(t, device, shape_ok):
+    """t as it is when it is already a contiguous float32 tensor on `device`."""
+    return isinstance(t, torch.Tensor) and t.dtype == torch.float32 and t.device == device and \
+        t.is_contiguous() and shape_ok(t)
+
+
 def _inputs(sources, values, device, source_type="point"):
     width = 4 if source_type == "extended" else 3
-    src = torch.as_tensor(sources).to(device=device, dtype=torch.float32).reshape(-1, width).contiguous()
-    val = torch.as_tensor(values).to(device=device, dtype=torch.float32).reshape(-1).contiguous()
+    device = torch.device(device)
+    if _ready(sources, device, lambda t: t.dim() == 2 and t.shape[1] == width):
+        src = sources
+    else:
+        src = torch.as_tensor(sources).to(device=device, dtype=torch.float32).reshape(-1, width).contiguous()
+    if _ready(values, device, lambda t: t.dim() == 1):
+        val = values
+    else:
+        val = torch.as_tensor(values).to(device=device, dtype=torch.float32).reshape(-1).contiguous()
     if src.shape[0] != val.shape[0]:
         raise ValueError(f"sources ({src.shape[0]}) and values ({val.shape[0]}) disagree in length")
     return src, val
