@@ -176,17 +176,21 @@ int launch_backward(const iact_scene_t* sc, const iact_sensor_t* sn, int src_typ
   double* gmir = gsrc + (size_t)S * 4;
   const int n_mir = sc->n_mirrors;
   const size_t nacc = (size_t)F * kFacetGrad + (size_t)S * 4 + (size_t)n_mir * kMirGrad;
-  int rc = check_cuda(cudaMemsetAsync(gfacet, 0, nacc * sizeof(double), st), "zero gradient buckets");
-  if (rc) return rc;
+  const bool work = S > 0 && F > 0 && sc->n_samples > 0;
+  int rc = IACT_OK;
+  if (!work) {  // the finish kernels still read the (empty) buckets
+    rc = check_cuda(cudaMemsetAsync(gfacet, 0, nacc * sizeof(double), st), "zero gradient buckets");
+    if (rc) return rc;
+  }
   const size_t nsamp = (size_t)F * std::max(sc->n_samples, 0) * 7;
   if (g_samples && nsamp) {
     rc = check_cuda(cudaMemsetAsync(g_samples, 0, nsamp * sizeof(float), st), "zero sample gradients");
     if (rc) return rc;
   }
-  if (S > 0 && F > 0 && sc->n_samples > 0) {
-    rc = check_cuda(cudaMemsetAsync(w + L.counter, 0, 64, st), "reset tile counter");
-    if (rc) return rc;
-    rc = launch_prep(sc, L, w, st, g_scale != nullptr);
+  if (work) {
+    // the prep launch also clears the gradient buckets and the tile counter
+    rc = launch_prep(sc, L, w, st, g_scale != nullptr, gfacet, nacc * sizeof(double),
+                     reinterpret_cast<int*>(w + L.counter));
     if (rc) return rc;
     AdjK p = adjoint_params(sc, sn, L, w, sources, values, grad_out, S, g_scale != nullptr, opts);
     p.gsamp = g_samples;
