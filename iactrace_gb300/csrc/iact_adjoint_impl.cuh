@@ -354,6 +354,7 @@ __device__ __forceinline__ void adjoint_tile(const AdjK& p, const Obst& ob, cons
   int cur_f = -1, cur_s = -1;
   JBasis jb;  // tangent basis of the current source (extended sources)
   int jb_s = -1;
+  HexCache hc = {3.0e38f, 3.0e38f, -1};  // last hexagon of this lane (hard hex sensors)
   for (int t = tb; t < te; ++t) {
     const int s = s0 + sl, f = f0 + fl;
     if (f != cur_f) {
@@ -459,7 +460,8 @@ __device__ __forceinline__ void adjoint_tile(const AdjK& p, const Obst& ob, cons
           else soft_hex_bwd(sn, p.hex_table, p.grad_out, rowbase, x, y, val, gval, gx, gy);
         } else {
           const int pix = (sn.type == IACT_SENSOR_SQUARE) ? bin_square(sn, x, y)
-                          : (p.hex_in_smem ? bin_hex(sn, htab, x, y) : bin_hex(sn, p.hex_table, x, y));
+                          : (p.hex_in_smem ? bin_hex_cached(sn, htab, x, y, hc)
+                                           : bin_hex_cached(sn, p.hex_table, x, y, hc));
           gval = pix >= 0 ? __ldg(p.grad_out + rowbase + pix) : 0.f;
         }
       }

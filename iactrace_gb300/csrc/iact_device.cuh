@@ -505,7 +505,8 @@ __device__ __forceinline__ int bin_hex(const SensorK& s, const TT* table, float 
   return (hd > s.edge_threshold) ? -1 : p;
 }
 
-// The last hexagon a lane binned into: its centre (grid frame) and pixel id.
+// The last hexagon a lane binned into: its centre (sensor-plane frame) and
+// pixel id.
 struct HexCache {
   float cx, cy;
   int pid;
@@ -515,14 +516,14 @@ struct HexCache {
 // - 1e-5 m of the cached cell's centre lies inside that cell (the hexagonal
 // norm never exceeds the Euclidean one over the inradius) and outside the
 // edge band, so the reference's rounding, lookup and edge test give the
-// cached id; the 1e-5 m margin covers their float32 rounding. Otherwise the
-// full path runs and refills the cache.
+// cached id; the 1e-5 m margin covers their float32 rounding. The test runs
+// in the sensor-plane frame (the grid frame is a rotation and a shift of
+// it, which keep distances), with the centre mapped back from the grid
+// frame on a miss (rounding ~1e-7 m, inside the margin). Otherwise the full
+// path runs and refills the cache.
 template <typename TT>
 __device__ __forceinline__ int bin_hex_cached(const SensorK& s, const TT* table, float x, float y, HexCache& hc) {
-  const float xs = __fsub_rn(x, s.off_x), ys = __fsub_rn(y, s.off_y);
-  const float xg = __fsub_rn(__fmul_rn(s.gc, xs), __fmul_rn(s.gs, ys));
-  const float yg = __fadd_rn(__fmul_rn(s.gs, xs), __fmul_rn(s.gc, ys));
-  const float ex = xg - hc.cx, ey = yg - hc.cy;
+  const float ex = x - hc.cx, ey = y - hc.cy;
   if (ex * ex + ey * ey < s.hex_lim2) return hc.pid;
   float xg2, yg2, qi, ri;
   hex_axial(s, x, y, xg2, yg2, qi, ri);
@@ -530,8 +531,9 @@ __device__ __forceinline__ int bin_hex_cached(const SensorK& s, const TT* table,
   float hcx, hcy;
   hex_centre(s, qi, ri, hcx, hcy);
   const float hd = hex_norm(__fsub_rn(xg2, hcx), __fsub_rn(yg2, hcy), s.inv_inr);
-  hc.cx = hcx;
-  hc.cy = hcy;
+  // grid -> sensor frame: x - off_x = gc xg + gs yg, y - off_y = -gs xg + gc yg
+  hc.cx = s.off_x + (s.gc * hcx + s.gs * hcy);
+  hc.cy = s.off_y + (s.gc * hcy - s.gs * hcx);
   hc.pid = p;
   return (hd > s.edge_threshold) ? -1 : p;
 }
