@@ -164,3 +164,51 @@ def test_sampler_reverse_matches_the_fp64_mapping(cuda, which):
         gy = y.grad.numpy().reshape(-1)
         err = np.abs(gx - gy).max() / np.abs(gy).max()
         assert err < 1e-5, f"d/d{name}: {gx} vs {gy} ({err:.3g})"
+
+
+@pytest.mark.parametrize("which", [0, 1])
+def test_fp64_mapping_matches_oracle_finite_differences(built, which):
+    """The torch FP64 mapping that checks the device sampler's reverse
+    (tests/twin.py resample_mapping) against central finite differences of
+    the oracle's own sampler (same variates, perturbed surface constants):
+    d/d(curvature, conic, aspheric) of sum(G * (points, normals, deltas,
+    weights)) for random G."""
+    import oracle.oracle as O
+    import twin
+    g = _groups()[which]
+    M = 64
+    theta0 = [np.float32(0.05), np.float32(-1.05), np.float32(1e-4), np.float32(-2e-6)]
+    rng = np.random.default_rng(11 + which)
+    G = [rng.standard_normal((len(g), M, 3)) for _ in range(3)] + [rng.standard_normal((len(g), M))]
+
+    def arrays(theta):
+        d, keep = sampler_desc(g, 9, M, "cpu")
+        d.curvature, d.conic = float(theta[0]), float(theta[1])
+        d.n_asph = 2
+        d.asph[0], d.asph[1] = float(theta[2]), float(theta[3])
+        out = O.sample_facets(d, len(g), M)
+        del keep
+        return out
+
+    def loss(theta):
+        return sum(float((a * b).sum()) for a, b in zip(arrays(theta), G))
+
+    fd = []
+    for j in range(4):
+        h = abs(float(theta0[j])) * 1e-3
+        tp, tm = list(theta0), list(theta0)
+        tp[j] = np.float32(float(theta0[j]) + h)
+        tm[j] = np.float32(float(theta0[j]) - h)
+        fd.append((loss(tp) - loss(tm)) / (float(tp[j]) - float(tm[j])))
+    pts, nrm, dlt, wts = arrays(theta0)
+    c = torch.tensor(float(theta0[0]), dtype=torch.float64, requires_grad=True)
+    k = torch.tensor(float(theta0[1]), dtype=torch.float64, requires_grad=True)
+    a = torch.tensor([float(theta0[2]), float(theta0[3])], dtype=torch.float64, requires_grad=True)
+    g2 = g.replace(curvature=c, conic=k, aspheric=a)
+    p, n, dl, w = twin.resample_mapping(g2, g2.get_surface(), torch.from_numpy(pts), torch.from_numpy(nrm),
+                                        torch.from_numpy(dlt), torch.from_numpy(wts)[..., None], M)
+    L = sum((t * torch.from_numpy(u).reshape(t.shape)).sum() for t, u in zip((p, n, dl, w), G))
+    L.backward()
+    ad = [float(c.grad), float(k.grad), float(a.grad[0]), float(a.grad[1])]
+    for j, name in enumerate(("curvature", "conic", "a0", "a1")):  # measured: below 1.1e-7 relative
+        assert abs(ad[j] - fd[j]) <= 1e-6 * abs(fd[j]), f"d/d{name}: autograd {ad[j]} vs FD {fd[j]}"
