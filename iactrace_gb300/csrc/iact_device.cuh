@@ -660,9 +660,11 @@ __device__ __forceinline__ float conic_start(const float* m, float ox, float oy,
 //   1. conic start and Newton steps in float32 while the steps exceed the
 //      float32 resolution (1e-5): the conic root may lie on the quadric's
 //      other sheet, metres from the surface, and these steps carry t across.
-//   2. Newton steps in FP64 (g and the sag in FP64, g' in float32: it only
-//      scales the step, the iteration still converges to the FP64 root),
-//      with the reference's test |g| < 1e-8 (the step at the first
+//   2. Newton steps in double-float arithmetic (the ray point, the sag and
+//      the residual g as float pairs, about 2^-44 relative; g' in float32:
+//      it only scales the step, the iteration still converges to the root
+//      an FP64 evaluation gives), with the reference's test |g| < 1e-8
+//      (the step at the first
 //      evaluation that passes it is still applied, as in the reference).
 //      Where a step from a failing evaluation leaves a residual
 //      |g''| step^2 / 2 below 1e-9 |g'| (step below 1e-4, inside the domain),
@@ -689,7 +691,7 @@ __device__ __forceinline__ float mirror_hit(const float* m, V3 o, V3 d, V3& pl, 
       const float g = fmaf(tf, d.z, ozf) - Sf;
       const float gp = d.z - 2.f * dSf * (xs * d.x + ys * d.y);
       const float st = g * rcp_a((fabsf(gp) > 1e-12f) ? gp : 1e-12f);
-      if (!(fabsf(st) < inf)) break;  // keep the last finite t: the FP64 phase decides
+      if (!(fabsf(st) < inf)) break;  // keep the last finite t: the double-float phase decides
       tf -= st;
       if (fabsf(st) < 1e-5f) {
         ++it;
