@@ -664,8 +664,8 @@ __device__ __forceinline__ float conic_start(const float* m, float ox, float oy,
 //      the residual g as float pairs, about 2^-44 relative; g' in float32:
 //      it only scales the step, the iteration still converges to the root
 //      an FP64 evaluation gives), with the reference's test |g| < 1e-8
-//      (the step at the first
-//      evaluation that passes it is still applied, as in the reference).
+//      (the step at the first evaluation that passes it is still applied,
+//      as in the reference).
 //      Where a step from a failing evaluation leaves a residual
 //      |g''| step^2 / 2 below 1e-9 |g'| (step below 1e-4, inside the domain),
 //      the evaluation the reference makes next passes the test and moves t
