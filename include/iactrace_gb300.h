@@ -47,7 +47,7 @@ extern "C" {
 /* status codes */
 #define IACT_OK 0
 #define IACT_E_INVALID (-1)     /* bad argument (null pointer, size, enum)  */
-#define IACT_E_UNSUPPORTED (-2) /* valid request this build cannot serve    */
+#define IACT_E_UNSUPPORTED (-2) /* valid request the library cannot serve   */
 #define IACT_E_CUDA (-3)        /* CUDA runtime error (launch/config)       */
 #define IACT_E_WORKSPACE (-4)   /* workspace missing, too small, misaligned */
 #define IACT_E_DEVICE (-5)      /* a kernel-side check failed (see message) */

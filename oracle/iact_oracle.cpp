@@ -4,7 +4,7 @@
 //
 // All descriptor pointers are HOST pointers here; the descriptor layout is
 // the product's C ABI (include/iactrace_gb300.h) so the same packed tables
-// feed the CUDA path and this checker.
+// feed the CUDA path and this oracle.
 #include <omp.h>
 
 #include <cstdio>

@@ -1,7 +1,7 @@
 // ORACLE — test infrastructure only. Nothing in the iactrace_gb300 product
 // path includes, links or calls this file; only tests/, the smoke check of
 // __graft_entry__ and the cpu_baseline / reference arm of bench.py use it,
-// as the checker and as the timed CPU restatement.
+// as the oracle of the parity tests and as the timed CPU restatement.
 //
 // A CPU restatement of the render path of GerritRo/iactrace v0.4.0
 // (JAX/Equinox), templated on the arithmetic type T:

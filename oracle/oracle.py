@@ -3,7 +3,8 @@
 path, fed the same packed tables as the CUDA library (host copies).
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline / reference
-arm use this module, as the checker and as the timed CPU restatement.
+arm use this module, as the oracle of the parity tests and as the timed CPU
+restatement.
 """
 from __future__ import annotations
 

@@ -106,7 +106,7 @@ def test_render_with_device_sampled_facets(cuda):
 
 @pytest.mark.parametrize("which", [0, 1])
 def test_oracle_sampler_distribution_on_cpu(built, which):
-    """The checker itself (CPU replay) follows the integrator's distribution."""
+    """The oracle itself (CPU replay) follows the integrator's distribution."""
     import oracle.oracle as O
     g = _groups()[which]
     M = 20000
