@@ -426,19 +426,26 @@ struct SensorK {
   float sigma;
   int kernel_size;
   float hex_lim2;  // (inradius * edge_threshold - 1e-5)^2: points this close to a cell centre bin to that cell
+  int axes;        // 1: the sensor's rotation is exactly the identity (local axes = world axes)
 };
 
-// core/intersections.py:6-41 intersect_plane -> local (x, y) or (1e10, 1e10)
+// core/intersections.py:6-41 intersect_plane -> local (x, y) or (1e10, 1e10).
+// AX = true is the same computation for a sensor whose rotation is exactly
+// the identity (s.axes): the dot products with the unit axes reduce to
+// components. fmaf with exact zeros and ones returns the other operand, so
+// both forms give the same floats (up to the sign of a zero result, which
+// no binning distinguishes).
+template <bool AX = false>
 __device__ __forceinline__ void plane_hit(const SensorK& s, V3 o, V3 d, float& x, float& y) {
   V3 u1 = mk(s.R[0], s.R[3], s.R[6]), u2 = mk(s.R[1], s.R[4], s.R[7]), n = mk(s.R[2], s.R[5], s.R[8]);
   V3 c = mk(s.pos[0], s.pos[1], s.pos[2]);
-  float ndotd = dot(d, n), ndoto = dot(o, n), ndotp = dot(n, c);
+  float ndotd = AX ? d.z : dot(d, n), ndoto = AX ? o.z : dot(o, n), ndotp = AX ? c.z : dot(n, c);
   bool parallel = fabsf(ndotd) < 1e-10f;
   float t = (ndotp - ndoto) * rcp_a(parallel ? 1.f : ndotd);
   V3 op = (o + t * d) - c;
   bool invalid = parallel || (t <= 0.f);
-  x = invalid ? kBig : dot(op, u1);
-  y = invalid ? kBig : dot(op, u2);
+  x = invalid ? kBig : (AX ? op.x : dot(op, u1));
+  y = invalid ? kBig : (AX ? op.y : dot(op, u2));
 }
 
 // sensors/square.py:66-91 SquareSensor.accumulate: pixel id or -1

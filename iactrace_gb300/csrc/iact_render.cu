@@ -71,7 +71,11 @@ __global__ void __launch_bounds__(256, STAGES ? 3 : IACT_RENDER_MIN_CTAS) k_rend
     __syncthreads();
     const int tile = s_tile;
     if (tile >= p.n_tiles) break;
-    render_tile<SRC, SOFT, MODE, STAGES>(p, ob, mir, htab, sh_hist, sink, tile, tmask);
+    // single-stage scenes with an axis-aligned sensor (the common case) take
+    // the plane hit without the frame's dot products; p.sn.axes is uniform.
+    // Not for extended sources, whose kernels would spill with two tile bodies.
+    if (!STAGES && SRC != IACT_SRC_EXTENDED && p.sn.axes) render_tile<SRC, SOFT, MODE, STAGES, true>(p, ob, mir, htab, sh_hist, sink, tile, tmask);
+    else render_tile<SRC, SOFT, MODE, STAGES>(p, ob, mir, htab, sh_hist, sink, tile, tmask);
   }
 }
 
@@ -186,6 +190,8 @@ SensorK make_sensor(const iact_sensor_t* s) {
   // threshold, less a rounding margin (-1: the cache never hits)
   const double lim = (double)s->inradius * std::min((double)s->edge_threshold, 1.0) - 1e-5;
   k.hex_lim2 = lim > 0.0 ? (float)(lim * lim) : -1.f;
+  k.axes = (k.R[0] == 1.f && k.R[4] == 1.f && k.R[8] == 1.f && k.R[1] == 0.f && k.R[2] == 0.f && k.R[3] == 0.f &&
+            k.R[5] == 0.f && k.R[6] == 0.f && k.R[7] == 0.f) ? 1 : 0;
   return k;
 }
 

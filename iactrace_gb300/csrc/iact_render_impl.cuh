@@ -311,7 +311,7 @@ __device__ __forceinline__ void splat_hex(const SensorK& s, const TT* table, con
 // the index of the last stage mirror hit (-1 if none).
 // The primary shadow test covers the set bits of the warp bundle's
 // candidate mask (n_words == 0: every primitive).
-template <int SRC, bool STAGES>
+template <int SRC, bool STAGES, bool AX = false>
 __device__ __forceinline__ void trace_ray(const RenderK& p, const Obst& ob, const float* mir, float4 P,
                                           float4 N, V3 src, const JBasis& jb, float sigma, float z0, float z1,
                                           float v, float& x,
@@ -364,7 +364,7 @@ __device__ __forceinline__ void trace_ray(const RenderK& p, const Obst& ob, cons
       mi = mj;
     }
   }
-  plane_hit(p.sn, o, r, x, y);
+  plane_hit<AX>(p.sn, o, r, x, y);
 }
 
 // One work tile (source block, facet chunk, 32-sample chunk) of the forward
@@ -426,7 +426,7 @@ __device__ __forceinline__ void warp_masks(const float4* B4, const float* source
   __syncwarp();
 }
 
-template <int SRC, bool SOFT, int MODE, bool STAGES>
+template <int SRC, bool SOFT, int MODE, bool STAGES, bool AX = false>
 __device__ __forceinline__ void render_tile(const RenderK& p, const Obst& ob, const float* mir, const short* htab,
                                             float* sh_hist, const Sink& sink, int tile, uint32_t* tmask) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5, nthr = blockDim.x;
@@ -468,7 +468,7 @@ __device__ __forceinline__ void render_tile(const RenderK& p, const Obst& ob, co
       const size_t si = (size_t)f * p.M + m;
       float z0 = 0.f, z1 = 0.f;
       if (SRC == IACT_SRC_EXTENDED) ray_normals(p.seed, s, f, m, z0, z1);
-      trace_ray<SRC, STAGES>(p, ob, mir, __ldg(p.P4 + si), __ldg(p.N4 + si), src, jb, sig, z0, z1, v, x, y, val,
+      trace_ray<SRC, STAGES, AX>(p, ob, mir, __ldg(p.P4 + si), __ldg(p.N4 + si), src, jb, sig, z0, z1, v, x, y, val,
                              hm, tmask + (sl * FCc + fl) * p.n_words, p.n_words);
     }
     int rowbase;
