@@ -35,7 +35,7 @@
 
 namespace iact {
 
-template <int SRC, bool SOFT, int MODE, bool STAGES>
+template <int SRC, bool SOFT, int MODE, bool STAGES, bool AX = false>
 __global__ void __launch_bounds__(256, STAGES ? 2 : (SOFT ? 3 : 4)) k_adjoint(const AdjK p) {
   extern __shared__ __align__(16) float smem[];
   __shared__ int s_tile;
@@ -59,7 +59,7 @@ __global__ void __launch_bounds__(256, STAGES ? 2 : (SOFT ? 3 : 4)) k_adjoint(co
     const int tile = s_tile;
     __syncthreads();
     if (tile >= p.n_tiles) break;
-    adjoint_tile<SRC, SOFT, MODE, STAGES>(p, ob, mir, htab, mgrad, tmask, tile);
+    adjoint_tile<SRC, SOFT, MODE, STAGES, AX>(p, ob, mir, htab, mgrad, tmask, tile);
   }
   if (STAGES) {
     __syncthreads();
@@ -85,6 +85,10 @@ namespace {
 template <int SRC, bool SOFT, int MODE, bool STAGES>
 int run_adjoint(const AdjK& p, int block, size_t smem, cudaStream_t st) {
   auto kern = k_adjoint<SRC, SOFT, MODE, STAGES>;
+  // hard pixels, single stage, axis-aligned sensor: a kernel whose plane hit
+  // takes components instead of dot products with the sensor axes
+  if constexpr (!SOFT && !STAGES && SRC != IACT_SRC_EXTENDED)
+    if (p.sn.axes) kern = k_adjoint<SRC, SOFT, MODE, STAGES, true>;
   int per_sm = 0;
   const int rc = resident_ctas(reinterpret_cast<const void*>(kern), block, smem, &per_sm);
   if (rc) return rc;

@@ -327,7 +327,10 @@ __device__ __forceinline__ void stage_bwd(const float* m, const StageRec& R, V3&
 // adjoint: candidate masks, then every warp re-traces and reverses its share
 // of the tasks; per-lane (facet, source) sums are flushed by the end of the
 // tile. CTA-collective (contains __syncthreads).
-template <int SRC, bool SOFT, int MODE, bool STAGES>
+// AX: the sensor's rotation is exactly the identity (p.sn.axes): the plane
+// hit takes components instead of dot products with the unit axes (the same
+// floats, as plane_hit<true>).
+template <int SRC, bool SOFT, int MODE, bool STAGES, bool AX = false>
 __device__ __forceinline__ void adjoint_tile(const AdjK& p, const Obst& ob, const float* mir, const short* htab,
                                              float* mgrad, uint32_t* tmask, int tile) {
   const SensorK& sn = p.sn;
@@ -444,13 +447,14 @@ __device__ __forceinline__ void adjoint_tile(const AdjK& p, const Obst& ob, cons
           mi = mj;
         }
       }
-      const float ndotd = dot(r, ns);
+      const float ndotd = AX ? r.z : dot(r, ns);
       const bool parallel = fabsf(ndotd) < 1e-10f;
       const float inv_nd = rcp_a(parallel ? 1.f : ndotd);
-      const float tpl = (dot(ns, C) - dot(o, ns)) * inv_nd;
+      const float tpl = ((AX ? C.z : dot(ns, C)) - (AX ? o.z : dot(o, ns))) * inv_nd;
       const V3 op = (o + tpl * r) - C;
       const bool hit_plane = !parallel && (tpl > 0.f);
-      const float x = hit_plane ? dot(op, u1) : kBig, y = hit_plane ? dot(op, u2) : kBig;
+      const float x = hit_plane ? (AX ? op.x : dot(op, u1)) : kBig;
+      const float y = hit_plane ? (AX ? op.y : dot(op, u2)) : kBig;
       // ---- reverse of the deposit
       float gval = 0.f, gx = 0.f, gy = 0.f;
       if (alive) {
@@ -468,7 +472,7 @@ __device__ __forceinline__ void adjoint_tile(const AdjK& p, const Obst& ob, cons
       const bool act = (gval != 0.f) | (gx != 0.f) | (gy != 0.f);
       V3 a = mk(0.f, 0.f, 0.f), gr = mk(0.f, 0.f, 0.f);
       float gv0 = gval;
-      if (act) {
+      if (SOFT && act) {  // hard pixels are constants: nothing flows back through the hit point
         // plane (intersections.py:23-35): p = o + t r, t = ns.(C - o) / ns.r
         V3 gpl = gx * u1 + gy * u2;  // dL/dp
         const float dLdt = dot(gpl, r);
