@@ -501,14 +501,16 @@ __device__ __forceinline__ void adjoint_tile(const AdjK& p, const Obst& ob, cons
         }
       }
       if (act) {
-        // val = v (-c) iw ; r = d - 2 c n'
-        const float dLdc = -gv0 * v * iw - 2.f * dot(gr, nn);
-        const V3 b = (-2.f * c) * gr + dLdc * d;  // dL/dn'
-        const V3 gd = gr + dLdc * nn;             // dL/dd
+        // val = v (-c) iw ; r = d - 2 c n'. With hard pixels and no later
+        // stage, a = dL/do and gr = dL/dr are exactly zero here (kHit false).
+        constexpr bool kHit = SOFT || STAGES;
+        const float dLdc = kHit ? -gv0 * v * iw - 2.f * dot(gr, nn) : -gv0 * v * iw;
+        const V3 b = kHit ? (-2.f * c) * gr + dLdc * d : dLdc * d;  // dL/dn'
+        const V3 gd = kHit ? gr + dLdc * nn : dLdc * nn;            // dL/dd
         V3 gsrc;
         if (SRC == IACT_SRC_POINT) {
           const V3 gw = inv_len * (gd - dot(d, gd) * d);  // d = w/|w|
-          a = a + gw;
+          a = kHit ? a + gw : gw;
           gsrc = mk(-gw.x, -gw.y, -gw.z);
         } else {
           gsrc = gd;
