@@ -139,11 +139,14 @@ AdjK adjoint_params(const iact_scene_t* sc, const iact_sensor_t* sn, const WsLay
   return p;
 }
 
-int plan_adjoint(AdjK& p, const iact_sensor_t* sn, int block, size_t& smem, long long min_tiles) {
+int plan_adjoint(AdjK& p, const iact_sensor_t* sn, int block, size_t& smem, long long min_tiles,
+                 const iact_opts_t* opts, int default_tpw) {
   const int nw = block / 32;
   const int nch = (p.M + 31) / 32;
-  p.SB = std::max(1, std::min(p.S, nw));
-  int target = std::max(1, std::min(nw * 48, p.n_words ? 4096 / p.n_words : 1 << 30));
+  // opts: sources per tile and 32-ray tasks per warp per tile, as for the forward render
+  p.SB = std::max(1, std::min(p.S, (opts && opts->sources_per_cta > 0) ? opts->sources_per_cta : nw));
+  const int tpw = (opts && opts->tasks_per_warp > 0) ? opts->tasks_per_warp : default_tpw;
+  int target = std::max(1, std::min(nw * tpw, p.n_words ? 4096 / p.n_words : 1 << 30));
   for (;;) {
     p.CC = std::max(1, std::min(nch, std::max(1, target / p.SB)));
     p.FC = std::max(1, std::min(p.F, std::max(1, target / (p.SB * p.CC))));
@@ -201,7 +204,10 @@ int launch_backward(const iact_scene_t* sc, const iact_sensor_t* sn, int src_typ
     p.want_mgrad = (g_mrot || g_mpos || g_msurf) ? 1 : 0;
     const int block = (opts && opts->block_threads > 0) ? opts->block_threads : 256;
     size_t smem = 0;
-    rc = plan_adjoint(p, sn, block, smem, 8LL * std::max(device_info().sm_count, 1));
+    // larger tiles for response adjoints (4096 sources: 192 tasks per warp
+    // 4.18 ms, 48: 4.34 ms)
+    rc = plan_adjoint(p, sn, block, smem, 8LL * std::max(device_info().sm_count, 1), opts,
+                      mode == IACT_MODE_RESPONSE ? 192 : 48);
     if (rc) return rc;
     const bool soft = sn->type == IACT_SENSOR_SOFT_SQUARE || sn->type == IACT_SENSOR_SOFT_HEX;
     void* const* ev = opts ? opts->kernel_events : nullptr;

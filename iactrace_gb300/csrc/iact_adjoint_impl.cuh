@@ -630,6 +630,7 @@ __device__ __forceinline__ void adjoint_finish_item(int i, const double* gfacet,
 AdjK adjoint_params(const iact_scene_t* sc, const iact_sensor_t* sn, const WsLayout& L, char* w,
                     const float* sources, const float* values, const float* grad_out, int S, bool with_scale,
                     const iact_opts_t* opts);
-int plan_adjoint(AdjK& p, const iact_sensor_t* sn, int block, size_t& smem, long long min_tiles);
+int plan_adjoint(AdjK& p, const iact_sensor_t* sn, int block, size_t& smem, long long min_tiles,
+                 const iact_opts_t* opts = nullptr, int default_tpw = 48);
 
 }  // namespace iact

@@ -356,7 +356,15 @@ int plan_tiles(RenderK& p, int mode, int block, const iact_opts_t* opts, long lo
                                                : std::min(S, mode == IACT_MODE_RESPONSE ? std::max(1, nw / 2) : nw);
   SB = std::max(1, std::min(SB, S));
   const bool fixed = opts && (opts->tasks_per_warp > 0 || opts->facets_per_tile > 0);
-  const int tpw = (opts && opts->tasks_per_warp > 0) ? opts->tasks_per_warp : 48;
+  // response tiles flush SB full rows each: larger tiles flush less often
+  // (4096-source hard-hexagon response: 192 tasks per warp 3.23 ms, 96: 3.27,
+  // 48: 3.46). Hard pixels only: a soft sensor's FP32 shared-memory rows
+  // would then sum ~4x more ray taps per entry before each FP64 flush
+  // (rows-vs-image agreement 3e-6 instead of < 1e-6 on the 256-source
+  // soft-hexagon response).
+  const bool soft = p.sn.type == IACT_SENSOR_SOFT_SQUARE || p.sn.type == IACT_SENSOR_SOFT_HEX;
+  const int tpw = (opts && opts->tasks_per_warp > 0) ? opts->tasks_per_warp
+                                                     : ((mode == IACT_MODE_RESPONSE && !soft) ? 192 : 48);
   // warp tasks (32 rays each) per tile; candidate masks stay within 16 KiB
   int target = std::max(1, std::min(nw * tpw, p.n_words ? 4096 / p.n_words : 1 << 30));
   for (;;) {
