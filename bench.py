@@ -50,7 +50,8 @@ F_RAY = {"response": 537, "plain": 503, "cassegrain": 894, "batched": 537,
 
 # DRAM bytes (read + write) per launch of the workload's render kernel from
 # one ncu capture of the same kernel and workload (summaries under profiles/)
-TRAFFIC = {"response": (7.35e6, "profiles/k_render_response_matrix_dc380_hex2048.md"),
+TRAFFIC = {"response": (7.31e6, "profiles/k_render_response_matrix_dc380_hex2048.md"),
+           "plain": (12.21e6, "profiles/k_render_plain_forward_dc380_square960.md"),
            "cassegrain": (1.05e6, "profiles/k_render_cassegrain_61seg_square1024.md")}
 
 
