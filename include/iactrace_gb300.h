@@ -145,10 +145,13 @@ typedef struct {
 /* Optional launch knobs; NULL or zeros select the built-in defaults. */
 typedef struct {
   int32_t block_threads;    /* threads per CTA (multiple of 32)           */
-  int32_t sources_per_cta;  /* warps per CTA each own one source at a time */
+  int32_t sources_per_cta;  /* sources per work tile (0: half the warps of a
+                               CTA for RESPONSE renders, else all)       */
   int32_t facets_per_tile;  /* primary facets per work tile               */
   int32_t hist_mode;        /* 0 auto, 1 shared-memory rows, 2 global     */
-  int32_t tasks_per_warp;   /* 32-ray tasks per warp per work tile (0: 48) */
+  int32_t tasks_per_warp;   /* 32-ray tasks per warp per work tile (0: 192 for
+                               hard-pixel RESPONSE renders and RESPONSE
+                               adjoints, else 48)                        */
   int32_t flags;            /* IACT_FLAG_* bits                           */
   uint32_t seed;            /* jitter stream of EXTENDED sources            */
   /* optional cudaEvent_t pair recorded on `stream` right before and after
