@@ -66,6 +66,7 @@ struct iact_batch {
   std::vector<size_t> region, acc_off;
   struct Class {
     int soft = 0, stages = 0;
+    int axes = 0;  // every job's sensor is axis-aligned
     int jb = 0, nj = 0, n_tiles = 0;
     int tab_floats = 0, htab_elems = 0, hist_floats = 0;
     size_t smem = 0;

@@ -49,7 +49,9 @@ int launch_batch_prep(const BatchJob* jobs, int n_jobs, int gx, int backward, cu
   return check_cuda(cudaGetLastError(), "k_batch_prep launch");
 }
 
-template <int SRC, bool SOFT, int MODE, bool STAGES>
+// AX: every job of the launch has an axis-aligned sensor (plane hit without
+// the frame's dot products, as in k_render)
+template <int SRC, bool SOFT, int MODE, bool STAGES, bool AX = false>
 __global__ void __launch_bounds__(256, STAGES ? 3 : IACT_RENDER_MIN_CTAS) k_batch_render(const BatchK b) {
   extern __shared__ __align__(16) float smem[];
   __shared__ __align__(16) RenderK s_p;
@@ -101,7 +103,7 @@ __global__ void __launch_bounds__(256, STAGES ? 3 : IACT_RENDER_MIN_CTAS) k_batc
     Sink sink;
     sink.sh = p.rows_in_smem ? sh_hist : nullptr;
     sink.g = p.acc;
-    render_tile<SRC, SOFT, MODE, STAGES>(p, ob, mir, htab, sh_hist, sink, tile - s_begin, tmask);
+    render_tile<SRC, SOFT, MODE, STAGES, AX>(p, ob, mir, htab, sh_hist, sink, tile - s_begin, tmask);
   }
 }
 
@@ -121,22 +123,24 @@ size_t a256(size_t x) { return (x + 255) & ~(size_t)255; }
 using BatchKernel = void (*)(BatchK);
 
 template <int SRC, bool SOFT, int MODE>
-BatchKernel pick_stages(bool stages) {
+BatchKernel pick_stages(bool stages, bool axes) {
+  if constexpr (SRC != IACT_SRC_EXTENDED)
+    if (!stages && axes) return k_batch_render<SRC, SOFT, MODE, false, true>;
   return stages ? k_batch_render<SRC, SOFT, MODE, true> : k_batch_render<SRC, SOFT, MODE, false>;
 }
 template <int SRC, bool SOFT>
-BatchKernel pick_mode(int mode, bool stages) {
-  return mode == IACT_MODE_RESPONSE ? pick_stages<SRC, SOFT, IACT_MODE_RESPONSE>(stages)
-                                    : pick_stages<SRC, SOFT, IACT_MODE_IMAGE>(stages);
+BatchKernel pick_mode(int mode, bool stages, bool axes) {
+  return mode == IACT_MODE_RESPONSE ? pick_stages<SRC, SOFT, IACT_MODE_RESPONSE>(stages, axes)
+                                    : pick_stages<SRC, SOFT, IACT_MODE_IMAGE>(stages, axes);
 }
 template <int SRC>
-BatchKernel pick_soft(bool soft, int mode, bool stages) {
-  return soft ? pick_mode<SRC, true>(mode, stages) : pick_mode<SRC, false>(mode, stages);
+BatchKernel pick_soft(bool soft, int mode, bool stages, bool axes) {
+  return soft ? pick_mode<SRC, true>(mode, stages, axes) : pick_mode<SRC, false>(mode, stages, axes);
 }
-BatchKernel pick_kernel(int src_type, bool soft, int mode, bool stages) {
-  if (src_type == IACT_SRC_POINT) return pick_soft<IACT_SRC_POINT>(soft, mode, stages);
-  if (src_type == IACT_SRC_EXTENDED) return pick_soft<IACT_SRC_EXTENDED>(soft, mode, stages);
-  return pick_soft<IACT_SRC_PARALLEL>(soft, mode, stages);
+BatchKernel pick_kernel(int src_type, bool soft, int mode, bool stages, bool axes) {
+  if (src_type == IACT_SRC_POINT) return pick_soft<IACT_SRC_POINT>(soft, mode, stages, axes);
+  if (src_type == IACT_SRC_EXTENDED) return pick_soft<IACT_SRC_EXTENDED>(soft, mode, stages, axes);
+  return pick_soft<IACT_SRC_PARALLEL>(soft, mode, stages, axes);
 }
 
 bool is_soft(const iact_sensor_t& s) { return s.type == IACT_SENSOR_SOFT_SQUARE || s.type == IACT_SENSOR_SOFT_HEX; }
@@ -243,6 +247,8 @@ int iact_batch_create(const iact_job_t* jobs, int32_t n_jobs, int32_t source_typ
     iact_batch::Class C;
     C.soft = soft;
     C.stages = stages;
+    C.axes = 1;
+    for (int i : mem) C.axes &= rk[i].sn.axes;
     C.jb = (int)b->order.size();
     C.nj = (int)mem.size();
     // table and hexagon-table floors: the largest of the class
@@ -415,7 +421,7 @@ int iact_batch_prepare(iact_batch* b, void* workspace, size_t workspace_bytes, v
   if (rc) return rc;
   const DevInfo di = device_info();
   for (iact_batch::Class& C : b->classes) {
-    BatchKernel kern = pick_kernel(b->src_type, C.soft, b->mode, C.stages);
+    BatchKernel kern = pick_kernel(b->src_type, C.soft, b->mode, C.stages, C.axes);
     int per_sm = 0;
     rc = resident_ctas(reinterpret_cast<const void*>(kern), b->block, C.smem, &per_sm);
     if (rc) return rc;
@@ -468,7 +474,7 @@ int iact_batch_render(iact_batch* b, void* stream) {
     k.tab_floats = C.tab_floats;
     k.htab_elems = C.htab_elems;
     k.hist_floats = C.hist_floats;
-    pick_kernel(b->src_type, C.soft, b->mode, C.stages)<<<C.grid, b->block, C.smem, st>>>(k);
+    pick_kernel(b->src_type, C.soft, b->mode, C.stages, C.axes)<<<C.grid, b->block, C.smem, st>>>(k);
     rc = check_cuda(cudaGetLastError(), "k_batch_render launch");
     if (rc) return rc;
   }
