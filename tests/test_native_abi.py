@@ -148,3 +148,38 @@ def test_batch_planner_without_a_gpu(built):
     assert built.iact_batch_create(jobs, 3, N.SRC_POINT, N.MODE_IMAGE, ctypes.byref(opts),
                                    ctypes.byref(h)) == N.IACT_E_INVALID
     assert built.iact_batch_create(jobs, -1, N.SRC_POINT, N.MODE_IMAGE, None, ctypes.byref(h)) == N.IACT_E_INVALID
+
+
+def test_tile_defaults_without_a_gpu(built):
+    """Default work-tile sizes of the host planner (read back through the
+    batch planner, which plans on the host only), at 256 threads per CTA
+    and 100 facets x 256 samples x 64 sources: a hard-pixel response job
+    takes tiles of 192 warp tasks per warp (4 sources x 48 facets x 8
+    32-sample chunks: 16 x 3 tiles); a soft-pixel response job 48 (4 x 12 x
+    8: 16 x 9); an image job 48 (8 x 6 x 8: 8 x 17); an explicit
+    opts.tasks_per_warp wins."""
+    sc = _fake_scene(100, 256)
+    hard = _square(8)
+    soft = _square(8)
+    soft.type, soft.sigma, soft.kernel_size = N.SENSOR_SOFT_SQUARE, 0.1, 2
+
+    def tiles(sn, mode, tpw=0):
+        job = (N.IactJob * 1)()
+        job[0].scene, job[0].sensor = ctypes.pointer(sc), ctypes.pointer(sn)
+        job[0].sources = job[0].values = 0x20000
+        job[0].n_sources = 64
+        job[0].out = 0x30000
+        opts = N.IactOpts()
+        opts.tasks_per_warp = tpw
+        h = ctypes.c_void_p()
+        rc = built.iact_batch_create(job, 1, N.SRC_POINT, mode, ctypes.byref(opts), ctypes.byref(h))
+        assert rc == N.IACT_OK, built.iact_last_error()
+        info = (ctypes.c_int64 * 5)()
+        assert built.iact_batch_info(h, info, 5) == N.IACT_OK
+        built.iact_batch_destroy(h)
+        return int(info[1])
+
+    assert tiles(hard, N.MODE_RESPONSE) == 16 * 3
+    assert tiles(soft, N.MODE_RESPONSE) == 16 * 9
+    assert tiles(hard, N.MODE_IMAGE) == 8 * 17
+    assert tiles(hard, N.MODE_RESPONSE, tpw=48) == 16 * 9
