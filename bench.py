@@ -50,6 +50,11 @@ F_RAY = {"response": 537, "plain": 503, "cassegrain": 894, "batched": 537,
 
 # DRAM bytes (read + write) per launch of the workload's render kernel from
 # one ncu capture of the same kernel and workload (summaries under profiles/)
+# Shared-memory atomic wavefronts of the render kernel as a fraction of the
+# hardware's sustained peak (ncu l1tex__data_pipe_lsu_wavefronts_mem_shared_op_atom
+# .sum.pct_of_peak_sustained_elapsed), from the same captures: the atomic-bound
+# fraction of the histogram adds
+SHARED_ATOMIC = {"response": (0.124, "profiles/k_render_response_matrix_dc380_hex2048.md")}
 TRAFFIC = {"response": (7.31e6, "profiles/k_render_response_matrix_dc380_hex2048.md"),
            "plain": (12.21e6, "profiles/k_render_plain_forward_dc380_square960.md"),
            "cassegrain": (1.05e6, "profiles/k_render_cassegrain_61seg_square1024.md")}
@@ -776,6 +781,8 @@ def main():
                      "traffic": TRAFFIC[args.workload][0] if args.workload in TRAFFIC else None,
                      "traffic_unit": "bytes per launch (ncu dram__bytes_read + write)",
                      "traffic_source": TRAFFIC[args.workload][1] if args.workload in TRAFFIC else None,
+                     "shared_atomic_frac": SHARED_ATOMIC[args.workload][0] if args.workload in SHARED_ATOMIC
+                     else None,
                      "kernel": "k_render", "kernel_ms": kern_s * 1e3,
                      "flops_per_ray": F_RAY[args.workload],
                      "peak_source": "measured live: FP32 FMA-chain probe kernel (iact_probe_fma)"},
