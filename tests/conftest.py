@@ -30,3 +30,15 @@ def cuda(built):
         pytest.skip("no CUDA device")
     torch.cuda.set_device(0)
     return torch.device("cuda", 0)
+
+
+@pytest.fixture(scope="session")
+def reference_checkout():
+    """A checkout of GerritRo/iactrace for tests that read its data files
+    (the HESS YAML configurations): the directory named by
+    IACTRACE_REFERENCE, else a `reference` directory beside this
+    repository; skipped when neither holds the reference."""
+    for cand in (os.environ.get("IACTRACE_REFERENCE", ""), os.path.join(os.path.dirname(ROOT), "reference")):
+        if cand and os.path.isfile(os.path.join(cand, "iactrace", "__init__.py")):
+            return cand
+    pytest.skip("no checkout of the reference (set IACTRACE_REFERENCE)")

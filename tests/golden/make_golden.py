@@ -1,8 +1,8 @@
 #!/usr/bin/env python
 """Generate the golden fixtures of the render path from the reference itself.
 
-Runs GerritRo/iactrace's own Python source (from /root/reference) on the
-numpy stand-in for jax/equinox in tests/golden/jaxshim (JAX cannot be
+Runs GerritRo/iactrace's own Python source (a checkout named by the
+IACTRACE_REFERENCE environment variable) on the numpy stand-in for jax/equinox in tests/golden/jaxshim (JAX cannot be
 installed here), builds a few small scenes with the reference's API,
 renders them with the reference's render / render_debug /
 render_response_matrix, and stores inputs and outputs as .npz files beside
@@ -24,7 +24,11 @@ Cases:
                  sources at 1 km, square + hex cameras with edge bands and
                  the two soft-splat sensors
 
-Usage: python tests/golden/make_golden.py [--x64-only]
+The per-ray sensor-plane hits and values of the first sensor are stored
+(debug_pts, debug_vals), and for a hard first sensor also the pixel id the
+reference's own accumulate gives each hit (debug_pix, -1 for none).
+
+Usage: IACTRACE_REFERENCE=<checkout of GerritRo/iactrace> python tests/golden/make_golden.py [case ...]
 """
 from __future__ import annotations
 
@@ -36,7 +40,9 @@ import sys
 import time
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = "/root/reference"
+REF = os.environ.get("IACTRACE_REFERENCE", "")
+if not os.path.isdir(os.path.join(REF, "iactrace")):
+    sys.exit("set IACTRACE_REFERENCE to a checkout of GerritRo/iactrace (the directory holding iactrace/)")
 sys.path[:0] = [os.path.join(HERE, "jaxshim"), REF]
 X64 = os.environ.get("JAXSHIM_X64") == "1"
 
@@ -71,7 +77,7 @@ def scene_ct3():
     return tel, src, val, "point", [0, 1]
 
 
-def scene_cassegrain():
+def scene_cassegrain(sec_radius=1.2, theta_deg=(0.0, 0.4, 0.7, 0.9)):
     f = 10.0
     prim = AsphericSurface(curvature=1.0 / (2 * f), conic=-1.0, aspheric=jnp.array([2e-6, -1e-8]))
     # hyperbolic secondary: foci at the primary focus and 0.5 m behind the vertex
@@ -85,7 +91,7 @@ def scene_cassegrain():
         mirrors.append(Mirror(position=jnp.array([x, y, z0]), rotation=jnp.array([0.0, 0.0, 0.0]), surface=prim,
                               aperture=DiskAperture(0.9), offset=jnp.array([x, y]), optical_stage=0))
     mirrors.append(Mirror(position=jnp.array([0.0, 0.0, 6.0]), rotation=jnp.array([180.0, 0.0, 0.0]), surface=sec,
-                          aperture=DiskAperture(1.2), optical_stage=1))
+                          aperture=DiskAperture(sec_radius), optical_stage=1))
     groups = group_mirrors(mirrors)
     key = jax.random.key(7)
     integ = MCIntegrator(16)
@@ -99,7 +105,7 @@ def scene_cassegrain():
     cam = SquareSensor(position=[0.0, 0.0, -0.5], rotation=[0.0, 0.0, 0.0], width=24, height=24,
                        bounds=(-0.3, 0.3, -0.3, 0.3))
     tel = Telescope(mirror_groups=out, obstruction_groups=[], sensors=[cam], name="cass")
-    th = np.radians([0.0, 0.4, 0.7, 0.9])
+    th = np.radians(list(theta_deg))
     ph = np.radians([0.0, 30.0, 200.0, 300.0])
     d = np.stack([np.sin(th) * np.cos(ph), np.sin(th) * np.sin(ph), -np.cos(th)], 1)
     return tel, jnp.array(d), jnp.array([1.0, 2.0, 0.5, 1.5]), "parallel", [0]
@@ -241,6 +247,21 @@ def inject_samples(tel, f32_fixture):
     return eqx.tree_at(lambda t: t.mirror_groups, tel, groups)
 
 
+def ref_pixel_ids(sensor, pts):
+    """Per-ray pixel ids decided by the reference's own hard accumulate
+    (sensors/square.py:66-91, sensors/hexagonal.py:174-194): each hit alone
+    with value 1; -1 where it lands in no pixel (out of bounds, no table
+    entry, inside the edge band)."""
+    out = np.full(len(pts), -1, np.int32)
+    for i in range(len(pts)):
+        img = A(sensor.accumulate(jnp.array(pts[i:i + 1, 0]), jnp.array(pts[i:i + 1, 1]),
+                                  jnp.ones(1, dtype=pts.dtype))).reshape(-1)
+        nz = np.flatnonzero(img)
+        if nz.size:
+            out[i] = nz[0]
+    return out
+
+
 def run_case(name):
     t0 = time.time()
     tel, src, val, st, sensors = CASES[name]()
@@ -265,6 +286,8 @@ def run_case(name):
         if si == sensors[0]:
             pts, vals = render_debug(tel, src, val, st, si)
             rec["debug_pts"], rec["debug_vals"] = A(pts), A(vals)
+            if "Differentiable" not in type(tel.sensors[si]).__name__:
+                rec["debug_pix"] = ref_pixel_ids(tel.sensors[si], A(pts))
     out = os.path.join(HERE, f"{name}_{SUFFIX}.npz")
     np.savez_compressed(out, **rec)
     print(f"{name} ({SUFFIX}): {time.time() - t0:.1f} s -> {os.path.basename(out)} "

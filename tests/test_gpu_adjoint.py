@@ -17,6 +17,7 @@ import torch
 import iactrace_gb300 as it
 from iactrace_gb300 import Telescope, workloads as W
 
+import gradref
 import twin
 
 GRAD_TOL = 1e-4
@@ -33,75 +34,17 @@ def small_dish(camera, seed=2, n_samples=48, roughness=24.0):
     return tel.apply_roughness(roughness) if roughness else tel
 
 
-def stage_groups(tel):
-    return [g for g in tel.mirror_groups if g.optical_stage != 0]
-
-
 def gpu_grads(tel, src, val, st, g, mode="image"):
-    """GPU gradients of L = sum(g * out) w.r.t. every parameter block."""
-    grp = tel.mirror_groups[0]
-    leaves = {"rot": grp.rotations.clone().cuda().requires_grad_(True),
-              "pos": grp.positions.clone().cuda().requires_grad_(True),
-              "scale": grp.perturbation_scale.clone().cuda().requires_grad_(True),
-              "src": src.clone().cuda().requires_grad_(True), "val": val.clone().cuda().requires_grad_(True)}
-    groups = [grp.replace(rotations=leaves["rot"], positions=leaves["pos"], perturbation_scale=leaves["scale"])]
-    for i, sg in enumerate(stage_groups(tel)):
-        lv = {"mrot": sg.rotations.clone().cuda().requires_grad_(True),
-              "mpos": sg.positions.clone().cuda().requires_grad_(True),
-              "mc": torch.tensor(float(sg.curvature), device="cuda", requires_grad=True),
-              "mk": torch.tensor(float(sg.conic), device="cuda", requires_grad=True),
-              "masph": sg.aspheric.clone().cuda().requires_grad_(True)}
-        leaves.update({f"{k}{i}": v for k, v in lv.items()})
-        groups.append(sg.replace(rotations=lv["mrot"], positions=lv["mpos"], curvature=lv["mc"], conic=lv["mk"],
-                                 aspheric=lv["masph"]))
-    t2 = Telescope(groups, tel.obstruction_groups, tel.sensors)
-    fn = it.render_response_matrix if mode == "response" else it.render
-    out = fn(t2, leaves["src"], leaves["val"], st)
-    (out.double() * torch.as_tensor(g, device="cuda").reshape(out.shape)).sum().backward()
-    return {k: (v.grad.double().cpu().numpy() if v.grad is not None else np.zeros(v.shape)) for k, v in leaves.items()}
+    return gradref.gpu_grads(tel, src, val, st, g, mode)
 
 
 def twin_grads(tel, src, val, st, g, mode="image"):
     """Twin (FP64 autograd) gradients on the GPU's discrete decisions."""
-    pts, vals, pix, _ = it.render_debug(tel, src, val, st, extras=True)
-    sc, sn = twin.scene_of(tel, 0, st)
-    dec = {"pix": pix.cpu().numpy(), "alive": vals.cpu().numpy() != 0}
-    dec.update(twin.soft_base(sn, pts.cpu().numpy()))
-    grp = tel.mirror_groups[0]
-    params = {"rot": grp.rotations, "pos": grp.positions, "scale": grp.perturbation_scale, "src": src, "val": val}
-    params = {k: v.detach().double().clone().requires_grad_(True) for k, v in params.items()}
-    leaves = dict(params)
-    mirrors = []
-    for i, sg in enumerate(stage_groups(tel)):
-        m = {"rot": sg.rotations.double()[0].clone().requires_grad_(True),
-             "pos": sg.positions.double()[0].clone().requires_grad_(True),
-             "c": torch.tensor(float(sg.curvature), dtype=torch.float64, requires_grad=True),
-             "k": torch.tensor(float(sg.conic), dtype=torch.float64, requires_grad=True),
-             "asph": sg.aspheric.double().clone().requires_grad_(True),
-             "off": sg.offsets.double()[0]}
-        mirrors.append(m)
-        leaves.update({f"mrot{i}": m["rot"], f"mpos{i}": m["pos"], f"mc{i}": m["c"], f"mk{i}": m["k"],
-                       f"masph{i}": m["asph"]})
-    params["mirrors"] = mirrors
-    out = twin.render(sc, params, dec, sn, mode)
-    (out.reshape(-1) * torch.as_tensor(g, dtype=torch.float64).reshape(-1)).sum().backward()
-    return {k: v.grad.numpy() if v.grad is not None else np.zeros(v.shape) for k, v in leaves.items()}
+    return gradref.twin_grads(tel, src, val, st, g, gradref.gpu_debug(tel, src, val, st), mode)
 
 
 def compare(gpu, ref, tol=GRAD_TOL, skip=()):
-    errs = {}
-    for k in ref:
-        if k in skip:
-            continue
-        a, b = gpu[k].reshape(-1), ref[k].reshape(-1)
-        nb = np.linalg.norm(b)
-        if nb == 0:
-            assert np.linalg.norm(a) == 0, k
-            continue
-        errs[k] = float(np.linalg.norm(a - b) / nb)
-    bad = {k: e for k, e in errs.items() if e > tol}
-    assert not bad, f"relative errors above {tol}: {bad} (all: {errs})"
-    return errs
+    return gradref.compare(gpu, ref, tol, skip)
 
 
 @pytest.mark.parametrize("mode", ["image", "response"])

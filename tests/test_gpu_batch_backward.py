@@ -15,7 +15,7 @@ import torch
 import iactrace_gb300 as it
 from iactrace_gb300 import workloads as W
 
-from test_gpu_adjoint import gpu_grads
+from gradref import gpu_grads
 from test_gpu_batch import _mixed_jobs
 
 SAME_TOL = 1e-5

@@ -26,7 +26,7 @@ def test_extended_forward_matches_oracle(cuda):
     tel, src, val = pb["telescope"], pb["sources"], pb["values"]
     img = it.render(tel, src, val, "extended", seed=pb["seed"]).cpu().double().numpy()
     ref = O.render(tel, src.cpu(), val.cpu(), "extended", 0, seed=pb["seed"])
-    assert np.linalg.norm(img - ref) / np.linalg.norm(ref) < 1e-4
+    assert np.linalg.norm(img - ref) / np.linalg.norm(ref) < 1e-5  # soft hexagons: no edge flips
     # a different seed draws different jitter
     img2 = it.render(tel, src, val, "extended", seed=pb["seed"] + 1).cpu().double().numpy()
     assert np.linalg.norm(img2 - img) / np.linalg.norm(img) > 1e-3

@@ -196,7 +196,7 @@ def test_soft_sensors(cuda, kind):
     img = it.render(tel, src, torch.ones(8), "point").cpu().double().numpy().reshape(-1)
     ref = O.render(tel, src, torch.ones(8), "point").reshape(-1)
     err = np.linalg.norm(img - ref) / np.linalg.norm(ref)
-    assert err < 1e-4, err
+    assert err < IMG_TOL, err
 
 
 def test_empty_and_edge_inputs(cuda):

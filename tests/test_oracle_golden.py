@@ -4,7 +4,8 @@ GerritRo/iactrace on a numpy stand-in for jax/equinox).
 
   *_f32 fixtures: the reference in float32 (JAX's default). The FP32
     restatement must match ray by ray: sensor-plane hits within a few ulp,
-    pixel ids equal except within EDGE of a pixel edge, values within 1e-5.
+    pixel ids equal to the ids the reference's own accumulate gave its hits
+    (every ray), values within 1e-5.
   *_f64 fixtures: the reference in float64 on the same sampled arrays. The
     FP64 oracle must match to the float32 quantisation of the scene tables
     (the C ABI carries float32 geometry): hits within 1e-6 m.
@@ -53,6 +54,11 @@ def test_rays_match_reference(built, case, kind):
     # f32: one-ulp differences of sin/cos in the facet rotation tilt the normal by
     # ~6e-8 rad, i.e. ~2e-6 m after reflection over the 15 m focal length
     assert perr < (6e-6 if kind == "f32" else 1e-6), f"plane hits differ by {perr:.3g} m"
+    if "debug_pix" in fx:
+        # the reference's own per-ray pixel ids (its accumulate on its hits):
+        # the restatement at the same precision decides every ray alike
+        assert np.array_equal(d["pix"], fx["debug_pix"]), \
+            f"{int((d['pix'] != fx['debug_pix']).sum())} pixel ids differ from the reference's"
     zero = (ref_vals == 0) != (d["vals"] == 0)
     assert zero.sum() <= max(1, 1e-4 * zero.size), f"{zero.sum()} shadow/hit decisions differ"
     same = ~zero

@@ -138,11 +138,15 @@ def render(scene, params, decisions, sensor, mode="image"):
     scene: dict of fixed float64 tensors: points, normals, delta (F,M,3), weights (F,M),
       sensor plane R (3,3), position (3,), and the sensor constants.
     params: dict of tensors: rot (F,3), pos (F,3), scale (F,), src (S,3), val (S,),
-      optional mirrors: list of dicts (rot, pos, c, k, asph, off).
+      optional mirrors: list of dicts (rot, pos, c, k, asph, off). The chain
+      runs in the parameters' dtype: float64 for the twin proper, float32
+      for the same chain at the reference's default precision (what
+      jax.grad computes with x64 off).
     decisions: dict of numpy arrays over rays (f, s, m): pix (hard id or -1),
       alive (bool: unshadowed and every stage hit), base (soft: base pixel / hex (q, r)).
     """
-    p, n, dl, w = scene["points"], scene["normals"], scene["delta"], scene["weights"]
+    dt = params["val"].dtype  # float64 parameters: the FP64 twin; float32: the same chain in float32
+    p, n, dl, w = (scene[k].to(dt) for k in ("points", "normals", "delta", "weights"))
     F, M = w.shape
     S = params["src"].shape[0]
     R = euler(params["rot"])
@@ -183,14 +187,14 @@ def render(scene, params, decisions, sensor, mode="image"):
         val = val * torch.abs(c2)
         r = r - 2 * c2[..., None] * nwld
         o = pwld
-    Rs, C = scene["sensor_R"], scene["sensor_pos"]
+    Rs, C = scene["sensor_R"].to(dt), scene["sensor_pos"].to(dt)
     u1, u2, ns = Rs[:, 0], Rs[:, 1], Rs[:, 2]
     t = ((ns * C).sum() - (o * ns).sum(-1)) / (r * ns).sum(-1)
     op = o + t[..., None] * r - C
     x, y = (op * u1).sum(-1), (op * u2).sum(-1)
     P = sensor["n_pixels"]
     rows = S if mode == "response" else 1
-    out = torch.zeros(rows * P, dtype=D)
+    out = torch.zeros(rows * P, dtype=dt)
     s_idx = torch.arange(S)[None, :, None].expand(F, S, M).reshape(-1) if mode == "response" else None
     kind = sensor["kind"]
     if kind in ("square", "hex"):
@@ -218,8 +222,8 @@ def render(scene, params, decisions, sensor, mode="image"):
         gc, gs = sensor["gc"], sensor["gs"]
         xs, ys = x - sensor["off_x"], y - sensor["off_y"]
         xg, yg = gc * xs - gs * ys, gs * xs + gc * ys
-        q0 = torch.as_tensor(decisions["base_q"].reshape(F, S, M), dtype=D)
-        r0 = torch.as_tensor(decisions["base_r"].reshape(F, S, M), dtype=D)
+        q0 = torch.as_tensor(decisions["base_q"].reshape(F, S, M), dtype=dt)
+        r0 = torch.as_tensor(decisions["base_r"].reshape(F, S, M), dtype=dt)
         ddx = xg - sensor["hex_sx"] * (q0 + r0 / 2)
         ddy = yg - sensor["hex_sy"] * r0
         K = sensor["kernel_size"]
