@@ -238,8 +238,6 @@ def _launch(tel, sources, values, source_type, sensor_idx, mode, opts=None, seed
     if _needs_grad(tel, src, val):
         rot, pos, scale = primary_params(tel, device)
         ps = pack_scene(tel, device, tuple(t.detach().contiguous() for t in (rot, pos, scale)))
-        if ps.n_stages > 2:
-            raise NotImplementedError("gradients through more than two mirror stages are not available")
         mrot, mpos, msurf = _stage_params(tel, device)
         prim = stages_of(tel).get(0, [])
         if any(t.requires_grad for g in prim for t in (g.points, g.normals, g.perturbation_delta, g.weights)):

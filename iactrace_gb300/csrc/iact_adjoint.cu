@@ -13,9 +13,10 @@
 //   hard bins: d img[pix] / d val = 1 (pixel ids carry no gradient)
 //   soft bins: val * w_k(x, y) / sum_k w_k                 (square.py:144-172, hexagonal.py:264-315)
 //
-// Later mirror stages (core/render.py:44-115, at most two on this path)
-// are recorded during the re-trace and reversed with the implicit-function
-// derivative of their Newton root (stage_bwd). Shadow and hit masks are
+// Later mirror stages (core/render.py:44-115, any number) are recorded
+// during the re-trace (the last kAdjRing of them; earlier ones are re-traced
+// again when the reverse sweep reaches them) and reversed with the
+// implicit-function derivative of their Newton root (stage_bwd). Shadow and hit masks are
 // piecewise constant and carry no gradient, as in jax.grad. Gradients reach facet rotations (Euler degrees), facet
 // positions, facet roughness scales, source positions/directions and source
 // values. Each lane keeps running sums for its current facet and source;
@@ -35,7 +36,7 @@
 
 namespace iact {
 
-template <int SRC, bool SOFT, int MODE, bool STAGES, bool AX = false>
+template <int SRC, bool SOFT, int MODE, bool STAGES, bool AX = false, bool DEEP = false>
 __global__ void __launch_bounds__(256, STAGES ? 2 : (SOFT ? 3 : 4)) k_adjoint(const AdjK p) {
   extern __shared__ __align__(16) float smem[];
   __shared__ int s_tile;
@@ -59,7 +60,7 @@ __global__ void __launch_bounds__(256, STAGES ? 2 : (SOFT ? 3 : 4)) k_adjoint(co
     const int tile = s_tile;
     __syncthreads();
     if (tile >= p.n_tiles) break;
-    adjoint_tile<SRC, SOFT, MODE, STAGES, AX>(p, ob, mir, htab, mgrad, tmask, tile);
+    adjoint_tile<SRC, SOFT, MODE, STAGES, AX, DEEP>(p, ob, mir, htab, mgrad, tmask, tile);
   }
   if (STAGES) {
     __syncthreads();
@@ -82,9 +83,9 @@ __global__ void k_adjoint_finish(const double* gfacet, const double* gsrc, const
 
 namespace {
 
-template <int SRC, bool SOFT, int MODE, bool STAGES>
+template <int SRC, bool SOFT, int MODE, bool STAGES, bool DEEP = false>
 int run_adjoint(const AdjK& p, int block, size_t smem, cudaStream_t st) {
-  auto kern = k_adjoint<SRC, SOFT, MODE, STAGES>;
+  auto kern = k_adjoint<SRC, SOFT, MODE, STAGES, false, DEEP>;
   // hard pixels, single stage, axis-aligned sensor: a kernel whose plane hit
   // takes components instead of dot products with the sensor axes
   if constexpr (!SOFT && !STAGES && SRC != IACT_SRC_EXTENDED)
@@ -98,15 +99,18 @@ int run_adjoint(const AdjK& p, int block, size_t smem, cudaStream_t st) {
   return check_cuda(cudaGetLastError(), "k_adjoint launch");
 }
 
-template <int SRC, bool SOFT, bool STAGES>
+template <int SRC, bool SOFT, bool STAGES, bool DEEP = false>
 int adj_mode(int mode, const AdjK& p, int block, size_t smem, cudaStream_t st) {
-  return mode == IACT_MODE_RESPONSE ? run_adjoint<SRC, SOFT, IACT_MODE_RESPONSE, STAGES>(p, block, smem, st)
-                                    : run_adjoint<SRC, SOFT, IACT_MODE_IMAGE, STAGES>(p, block, smem, st);
+  return mode == IACT_MODE_RESPONSE ? run_adjoint<SRC, SOFT, IACT_MODE_RESPONSE, STAGES, DEEP>(p, block, smem, st)
+                                    : run_adjoint<SRC, SOFT, IACT_MODE_IMAGE, STAGES, DEEP>(p, block, smem, st);
 }
+// n_stages: later stages of the scene (0: primary only; above kAdjRing: the
+// kernels that re-trace stages which left the record ring)
 template <int SRC, bool SOFT>
-int adj_stages(bool stages, int mode, const AdjK& p, int block, size_t smem, cudaStream_t st) {
-  return stages ? adj_mode<SRC, SOFT, true>(mode, p, block, smem, st)
-                : adj_mode<SRC, SOFT, false>(mode, p, block, smem, st);
+int adj_stages(int n_stages, int mode, const AdjK& p, int block, size_t smem, cudaStream_t st) {
+  if (n_stages > kAdjRing) return adj_mode<SRC, SOFT, true, true>(mode, p, block, smem, st);
+  return n_stages > 0 ? adj_mode<SRC, SOFT, true>(mode, p, block, smem, st)
+                      : adj_mode<SRC, SOFT, false>(mode, p, block, smem, st);
 }
 
 }  // namespace
@@ -212,7 +216,7 @@ int launch_backward(const iact_scene_t* sc, const iact_sensor_t* sn, int src_typ
     const bool soft = sn->type == IACT_SENSOR_SOFT_SQUARE || sn->type == IACT_SENSOR_SOFT_HEX;
     void* const* ev = opts ? opts->kernel_events : nullptr;
     if (ev && ev[0]) cudaEventRecord(static_cast<cudaEvent_t>(ev[0]), st);
-    const bool stages = n_mir > 0;
+    const int stages = n_mir > 0 ? std::max(sc->n_stages, 1) : 0;
     if (src_type == IACT_SRC_POINT)
       rc = soft ? adj_stages<IACT_SRC_POINT, true>(stages, mode, p, block, smem, st)
                 : adj_stages<IACT_SRC_POINT, false>(stages, mode, p, block, smem, st);

@@ -173,7 +173,6 @@ __device__ __forceinline__ void soft_hex_bwd(const SensorK& s, const TT* table, 
   gy = -s.gs * gxg + s.gc * gyg;
 }
 
-constexpr int kMaxAdjStages = 2;
 
 // Adds each lane's stage-mirror gradient terms g (mirror j; j < 0: none)
 // into the CTA's shared sums. Warp-collective (all 32 lanes). When every
@@ -216,6 +215,61 @@ struct StageRec {
   V3 pl, nl;    // local hit point and unit normal
   float c2;     // r . n_world
 };
+
+// Forward of one later stage (core/render.py:44-115): the closest hit
+// (first index on ties, as argmin) over the mirrors of the stage that starts
+// at table index mi, for the ray (o, r) carrying val. Returns the table index
+// past the stage; hit tells whether any mirror of the stage was hit, and R
+// then holds the record of the reflection.
+__device__ __forceinline__ int stage_fwd(const float* mir, int n_mir, int mi, V3 o, V3 r, float val, StageRec& R,
+                                         bool& hit) {
+  const int stg = (int)mir[mi * kMirF + 22];
+  float best_t = __int_as_float(0x7f800000);
+  V3 bpl = mk(0.f, 0.f, 0.f), bnl = mk(0.f, 0.f, 0.f);
+  int bi = -1;
+  int mj = mi;
+  for (; mj < n_mir && (int)mir[mj * kMirF + 22] == stg; ++mj) {
+    const float* mm = mir + mj * kMirF;
+    const V3 pos = mk(mm[9], mm[10], mm[11]);
+    V3 pl, nl;
+    const float tt = mirror_hit(mm, rtmul(mm, o - pos), rtmul(mm, r), pl, nl);
+    if (tt < best_t) {
+      best_t = tt; bpl = pl; bnl = nl; bi = mj;
+    }
+  }
+  hit = best_t < kBig;
+  if (hit) {
+    R.o = o; R.r = r; R.val = val; R.j = bi; R.t = best_t; R.pl = bpl; R.nl = bnl;
+    R.c2 = dot(r, rmul(mir + bi * kMirF, bnl));
+  }
+  return mj;
+}
+
+// The ray after the reflection R records: o' = Rj pl + Pj, r' = r - 2 c2 n_w,
+// val' = val |c2|.
+__device__ __forceinline__ void stage_apply(const float* mir, const StageRec& R, V3& o, V3& r, float& val) {
+  const float* mm = mir + R.j * kMirF;
+  const V3 nw = rmul(mm, R.nl);
+  val = val * fabsf(R.c2);
+  o = rmul(mm, R.pl) + mk(mm[9], mm[10], mm[11]);
+  r = r - (2.f * R.c2) * nw;
+}
+
+// The record of later stage k of a ray that hit every stage, re-traced from
+// the primary reflection (o0, r0, val0): the reverse sweep's source for
+// stages that left the ring (scenes with more than kAdjRing stages).
+__device__ __forceinline__ void stage_retrace(const float* mir, int n_mir, int k, V3 o0, V3 r0, float val0,
+                                           StageRec& out) {
+  V3 o = o0, r = r0;
+  float val = val0;
+  int mi = 0;
+  for (int kk = 0; mi < n_mir; ++kk) {
+    bool hit;
+    mi = stage_fwd(mir, n_mir, mi, o, r, val, out, hit);
+    if (kk == k || !hit) return;
+    stage_apply(mir, out, o, r, val);
+  }
+}
 
 // Reverse of core/render.py:44-115 for one ray at one stage: from dL/d(o',
 // r', val') after the reflection to dL/d(o, r, val) before it, adding the
@@ -330,7 +384,10 @@ __device__ __forceinline__ void stage_bwd(const float* m, const StageRec& R, V3&
 // AX: the sensor's rotation is exactly the identity (p.sn.axes): the plane
 // hit takes components instead of dot products with the unit axes (the same
 // floats, as plane_hit<true>).
-template <int SRC, bool SOFT, int MODE, bool STAGES, bool AX = false>
+// DEEP: the scene has more than kAdjRing later stages; the reverse of a
+// stage that left the ring re-traces it (stage_retrace). Scenes with at most
+// kAdjRing stages take the kernels without that path.
+template <int SRC, bool SOFT, int MODE, bool STAGES, bool AX = false, bool DEEP = false>
 __device__ __forceinline__ void adjoint_tile(const AdjK& p, const Obst& ob, const float* mir, const short* htab,
                                              float* mgrad, uint32_t* tmask, int tile) {
   const SensorK& sn = p.sn;
@@ -407,8 +464,10 @@ __device__ __forceinline__ void adjoint_tile(const AdjK& p, const Obst& ob, cons
       const float c = dot(d, nn);
       const V3 r0 = d - (2.f * c) * nn;
       const float val0 = v * -c * iw;
-      // later stages, recorded for the reverse sweep (core/render.py:44-79)
-      StageRec rec[kMaxAdjStages];
+      // later stages, recorded for the reverse sweep (core/render.py:44-79):
+      // stage k's record in rec[k % kAdjRing]; the reverse sweep runs k
+      // downwards and overwrites a slot only after its stage is reversed
+      StageRec rec[kAdjRing];
       int nst = 0;
       bool alive = ok && !shadowed;
       V3 o = tp, r = r0;
@@ -416,35 +475,16 @@ __device__ __forceinline__ void adjoint_tile(const AdjK& p, const Obst& ob, cons
       if (STAGES) {
         int mi = 0;
         while (mi < p.n_mir) {
-          const int stg = (int)mir[mi * kMirF + 22];
-          float best_t = __int_as_float(0x7f800000);
-          V3 bpl = mk(0.f, 0.f, 0.f), bnl = mk(0.f, 0.f, 0.f);
-          int bi = -1;
-          int mj = mi;
-          for (; mj < p.n_mir && (int)mir[mj * kMirF + 22] == stg; ++mj) {
-            const float* mm = mir + mj * kMirF;
-            const V3 pos = mk(mm[9], mm[10], mm[11]);
-            V3 pl, nl;
-            const float tt = mirror_hit(mm, rtmul(mm, o - pos), rtmul(mm, r), pl, nl);
-            if (tt < best_t) {
-              best_t = tt; bpl = pl; bnl = nl; bi = mj;
-            }
-          }
-          const bool hit = best_t < kBig;
+          StageRec& R = rec[nst & (kAdjRing - 1)];
+          bool hit;
+          mi = stage_fwd(mir, p.n_mir, mi, o, r, val, R, hit);
           alive = alive && hit && !occluded(ob, o, r);
-          if (hit && nst < kMaxAdjStages) {
-            const float* mm = mir + bi * kMirF;
-            const V3 nw = rmul(mm, bnl);
-            StageRec& R = rec[nst++];
-            R.o = o; R.r = r; R.val = val; R.j = bi; R.t = best_t; R.pl = bpl; R.nl = bnl;
-            R.c2 = dot(r, nw);
-            val = val * fabsf(R.c2);
-            o = rmul(mm, bpl) + mk(mm[9], mm[10], mm[11]);
-            r = r - (2.f * R.c2) * nw;
+          if (hit) {
+            ++nst;
+            stage_apply(mir, R, o, r, val);
           } else {
             alive = false;
           }
-          mi = mj;
         }
       }
       const float ndotd = AX ? r.z : dot(r, ns);
@@ -482,7 +522,9 @@ __device__ __forceinline__ void adjoint_tile(const AdjK& p, const Obst& ob, cons
       if (STAGES && !p.want_mgrad && act) {  // the chain through the stages only
         for (int k = nst - 1; k >= 0; --k) {
           float gm[kMirGrad];
-          stage_bwd<false>(mir + rec[k].j * kMirF, rec[k], a, gr, gv0, gm);
+          StageRec& Rk = rec[k & (kAdjRing - 1)];
+          if (DEEP && k < nst - kAdjRing) stage_retrace(mir, p.n_mir, k, tp, r0, val0, Rk);  // left the ring
+          stage_bwd<false>(mir + Rk.j * kMirF, Rk, a, gr, gv0, gm);
         }
       }
       if (STAGES && p.want_mgrad) {  // warp-converged: the mirror sums are warp-collective
@@ -491,8 +533,10 @@ __device__ __forceinline__ void adjoint_tile(const AdjK& p, const Obst& ob, cons
           float gm[kMirGrad];
           int j = -1;
           if (act && k < nst) {
-            stage_bwd<true>(mir + rec[k].j * kMirF, rec[k], a, gr, gv0, gm);
-            j = rec[k].j;
+            StageRec& Rk = rec[k & (kAdjRing - 1)];
+            if (DEEP && k < nst - kAdjRing) stage_retrace(mir, p.n_mir, k, tp, r0, val0, Rk);  // left the ring
+            stage_bwd<true>(mir + Rk.j * kMirF, Rk, a, gr, gv0, gm);
+            j = Rk.j;
           } else {
 #pragma unroll
             for (int i = 0; i < kMirGrad; ++i) gm[i] = 0.f;

@@ -176,8 +176,9 @@ int iact_batch_create(const iact_job_t* jobs, int32_t n_jobs, int32_t source_typ
       return set_error(IACT_E_UNSUPPORTED, at + "response matrix larger than 2^31 entries");
     if (!J.out && acc_elems(J.sensor, J.n_sources, mode) > 0) return set_error(IACT_E_INVALID, at + "out is NULL");
     if (opts && (opts->flags & IACT_FLAG_BATCH_BACKWARD)) {
-      if (J.scene->n_stages > 2)
-        return set_error(IACT_E_UNSUPPORTED, at + "backward: at most 2 mirror stages after the primary");
+      if (J.scene->n_stages > kAdjRing)
+        return set_error(IACT_E_UNSUPPORTED, at + "backward: at most 2 mirror stages after the primary in a batch "
+                                                  "(iact_render_backward takes any number)");
       if (source_type == IACT_SRC_EXTENDED && J.g_sources)
         return set_error(IACT_E_UNSUPPORTED, at + "backward: no source gradients for extended sources");
       if (!J.grad_out && acc_elems(J.sensor, J.n_sources, mode) > 0)

@@ -177,8 +177,6 @@ int iact_render_backward(const iact_scene_t* scene, const iact_sensor_t* sensor,
   int rc = check_common(scene, sensor, source_type, sources, values, n_sources, IACT_MODE_BACKWARD, workspace,
                         workspace_bytes);
   if (rc) return rc;
-  if (scene->n_stages > 2)
-    return set_error(IACT_E_UNSUPPORTED, "iact_render_backward: at most 2 mirror stages after the primary");
   if (source_type == IACT_SRC_EXTENDED && g_sources)
     return set_error(IACT_E_UNSUPPORTED, "iact_render_backward: no source gradients for extended sources");
   if (!grad_out && acc_elems(sensor, n_sources, mode) > 0) return set_error(IACT_E_INVALID, "grad_out is NULL");

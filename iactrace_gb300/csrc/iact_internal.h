@@ -36,6 +36,11 @@ struct WsLayout {
 };
 constexpr int kFacetGrad = 13;  // per facet: dL/dR world-frame H (9), dL/dpos (3), dL/dscale (1)
 constexpr int kMirGrad = 22;    // per stage mirror: dL/dR (9), dL/dpos (3), dL/dc, dL/dk, dL/da (8)
+// Later-stage reflections the adjoint keeps per ray for its reverse sweep:
+// the last kAdjRing (a ring, a power of two); the reverse of an earlier
+// stage re-traces the ray from the primary to that stage. The batched
+// adjoint takes scenes of at most kAdjRing later stages.
+constexpr int kAdjRing = 2;
 WsLayout workspace_layout(const iact_scene_t* sc, size_t acc_elems, bool with_delta);
 size_t acc_elems(const iact_sensor_t* sn, int S, int mode);  // 0 for DEBUG
 WsLayout workspace_for(const iact_scene_t* sc, const iact_sensor_t* sn, int S, int mode);

@@ -217,7 +217,7 @@ int iact_render_debug(const iact_scene_t* scene, const iact_sensor_t* sensor,
                       void* workspace, size_t workspace_bytes, uint32_t seed,
                       void* stream);
 
-/* Adjoint of iact_render (mode IMAGE or RESPONSE), scenes with at most two
+/* Adjoint of iact_render (mode IMAGE or RESPONSE), through any number of
  * mirror stages after the primary: given grad_out = dL/d(out), writes
  * dL/d(facet rotations) [F,3] (per degree), dL/d(facet positions) [F,3],
  * dL/d(facet perturbation scales) [F], dL/d(sources) [S,3], dL/d(values)
