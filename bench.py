@@ -48,16 +48,41 @@ F_RAY = {"response": 537, "plain": 503, "cassegrain": 894, "batched": 537,
          "obstructed": 26 + 271 * 98 + 2 * 35 + 29 + 47 + 40 + 34 + 56}
 
 
-# DRAM bytes (read + write) per launch of the workload's render kernel from
-# one ncu capture of the same kernel and workload (summaries under profiles/)
-# Shared-memory atomic wavefronts of the render kernel as a fraction of the
-# hardware's sustained peak (ncu l1tex__data_pipe_lsu_wavefronts_mem_shared_op_atom
-# .sum.pct_of_peak_sustained_elapsed), from the same captures: the atomic-bound
-# fraction of the histogram adds
-SHARED_ATOMIC = {"response": (0.124, "profiles/k_render_response_matrix_dc380_hex2048.md")}
-TRAFFIC = {"response": (7.31e6, "profiles/k_render_response_matrix_dc380_hex2048.md"),
-           "plain": (12.21e6, "profiles/k_render_plain_forward_dc380_square960.md"),
-           "cassegrain": (1.05e6, "profiles/k_render_cassegrain_61seg_square1024.md")}
+# Figures from one ncu capture of each workload's render kernel (summaries
+# under profiles/, with the commands that made them): DRAM bytes (read +
+# write) per launch, shared-memory atomic wavefronts as a fraction of their
+# sustained peak (l1tex__data_pipe_lsu_wavefronts_mem_shared_op_atom.sum.
+# pct_of_peak_sustained_elapsed: the atomic-bound fraction of the histogram
+# adds), executed thread instructions per ray (smsp__inst_executed.sum x
+# average active threads per instruction / rays) and the FMA pipe's share of
+# its peak (sm__inst_executed_pipe_fma). Each records the digest of the
+# kernel sources it was taken on (source_digest() below); when the sources
+# have changed since, the figures are reported as stale and not used as the
+# roofline's traffic.
+CAPTURES = {}
+
+
+def source_digest() -> str:
+    """sha256 (16 hex digits) of the CUDA sources and the C ABI header."""
+    import hashlib
+    h = hashlib.sha256()
+    csrc = os.path.join(ROOT, "iactrace_gb300", "csrc")
+    files = sorted(os.path.join(csrc, f) for f in os.listdir(csrc) if f.endswith((".cu", ".cuh", ".h")))
+    for path in files + [os.path.join(ROOT, "include", "iactrace_gb300.h")]:
+        h.update(os.path.basename(path).encode())
+        with open(path, "rb") as f:
+            h.update(f.read())
+    return h.hexdigest()[:16]
+
+
+def capture_fields(workload):
+    """The capture record of `workload` and whether it matches the sources."""
+    cap = CAPTURES.get(workload)
+    if cap is None:
+        return None, None
+    current = cap["digest"] == source_digest()
+    rec = dict(cap, current=current)
+    return rec, current
 
 
 def _env_rank():
@@ -760,6 +785,20 @@ def main():
         e2e_ev[k][1].record(stream)
     torch.cuda.synchronize(dev)
     e2e_s = sum(a.elapsed_time(b) for a, b in e2e_ev) / 1e3 / args.steps
+    # the same call timed by the host clock, one call at a time: each step
+    # ends with a synchronize, so the host's own overhead (argument checks,
+    # the cached packing, launches, copies) and the synchronisation latency
+    # are inside the time, as a caller waiting for each result sees them
+    wall = []
+    for k in range(args.steps):
+        flush_buf.fill_(float(k))
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        o = fn(tel, src_pin.to(dev, non_blocking=True), val_pin.to(dev, non_blocking=True), stype)
+        out_pin.copy_(o, non_blocking=True)
+        torch.cuda.synchronize(dev)
+        wall.append(time.perf_counter() - t0)
+    wall_s = sorted(wall)[len(wall) // 2]
     clk = clocks.stop()
 
     t = torch.tensor([step_s, kern_s, e2e_s], device=dev, dtype=torch.float64)
@@ -769,6 +808,7 @@ def main():
 
     peak = fp32_peak_tflops(dev)
     achieved = F_RAY[args.workload] * rays / kern_s / 1e12
+    cap, cap_ok = capture_fields(args.workload)
     h2d = src_h.numel() * 4 + val_h.numel() * 4
     d2h = out.numel() * 4
     line = {
@@ -776,16 +816,23 @@ def main():
         "warmup": args.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scenes and sources)", "config": cfg,
         "e2e": {"value": rays * world / e2e_s, "unit": "rays/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3},
+                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3,
+                "timing": "CUDA events around each step's copies and call (host issue overlapped)",
+                "host_wall": {"value": rays * world / wall_s, "unit": "rays/s", "ms_per_step": wall_s * 1e3,
+                              "timing": "host clock around call + copies + synchronize, one step at a time "
+                                        "(median)"}},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-                     "traffic": TRAFFIC[args.workload][0] if args.workload in TRAFFIC else None,
+                     "traffic": cap["dram_bytes"] if cap_ok else None,
                      "traffic_unit": "bytes per launch (ncu dram__bytes_read + write)",
-                     "traffic_source": TRAFFIC[args.workload][1] if args.workload in TRAFFIC else None,
-                     "shared_atomic_frac": SHARED_ATOMIC[args.workload][0] if args.workload in SHARED_ATOMIC
-                     else None,
                      "kernel": "k_render", "kernel_ms": kern_s * 1e3,
                      "flops_per_ray": F_RAY[args.workload],
-                     "peak_source": "measured live: FP32 FMA-chain probe kernel (iact_probe_fma)"},
+                     "flops_note": "algorithmic: the reference's full evaluation per ray without early-out "
+                                   "(obstruction tests the bundle culling skips are counted)",
+                     "peak_source": "measured live: FP32 FMA-chain probe kernel (iact_probe_fma)",
+                     "executed": {k: cap[k] for k in ("thread_inst_per_ray", "fma_pipe", "issue_active",
+                                                      "shared_atomic_frac") if k in cap} if cap_ok else None,
+                     "capture": ({"profile": cap["profile"], "digest": cap["digest"], "current": cap_ok}
+                                 if cap else None)},
         "fwd_adjoint": fwdadj,
         "gpu_launches": 3 * args.steps,  # k_prep, k_render, k_finish per step
         **({"culling": culling} if culling else {}),

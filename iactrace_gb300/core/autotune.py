@@ -3,10 +3,12 @@
 Knobs: threads per CTA (block_threads), 32-ray tasks per warp per work tile
 (tasks_per_warp: rays each thread traces per tile) and histogram placement
 (hist_mode: FP32 shared-memory rows or direct FP64 global atomics). Every
-candidate is planned, run once and timed with CUDA events on the batch
-itself; the fastest is cached in memory and in a JSON file keyed by GPU,
-library ABI and the batch's shape signature (per job: facets, samples,
-sources, pixels, sensor kind, stage mirrors).
+candidate is planned, run once as a warm-up and then REPS more times, each
+timed with CUDA events on the batch itself; its time is the median of those
+runs (sub-millisecond launches vary by a few percent from run to run). The
+fastest is cached in memory and in a JSON file keyed by GPU, library ABI,
+the repetition count and the batch's shape signature (per job: facets,
+samples, sources, pixels, sensor kind, stage mirrors).
 
 Cache file: $IACTRACE_TUNE_CACHE, else ~/.cache/iactrace_gb300/tune.json.
 IACTRACE_TUNE=0 skips tuning (library defaults).
@@ -24,6 +26,7 @@ import torch
 from .. import _native as N
 
 CANDIDATES = [(b, t, h) for b in (256, 128) for t in (16, 32, 64) for h in (1, 2)]
+REPS = 5  # timed runs per candidate (median)
 _mem: dict = {}
 _lock = threading.Lock()
 
@@ -42,7 +45,7 @@ def make_opts(block, tasks, hist) -> N.IactOpts:
 def _key(batch) -> str:
     props = torch.cuda.get_device_properties(batch.device)
     sig = hashlib.sha1(repr(batch.signature).encode()).hexdigest()[:16]
-    return f"{props.name}|sm{props.multi_processor_count}|abi{N.load().iact_abi_version()}|batch|{sig}"
+    return f"{props.name}|sm{props.multi_processor_count}|abi{N.load().iact_abi_version()}|r{REPS}|batch|{sig}"
 
 
 def _load_file() -> dict:
@@ -67,7 +70,7 @@ def _store(key, value):
         pass  # an unwritable cache only costs re-tuning
 
 
-def time_candidate(batch, opts, reps: int = 3) -> float:
+def time_candidate(batch, opts, reps: int = REPS) -> float:
     """Median device time (ms) of the batch's launch sequence under `opts`."""
     h, ws = batch._create(opts)
     stream = torch.cuda.current_stream(batch.device)

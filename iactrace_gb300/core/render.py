@@ -16,9 +16,15 @@ from .. import _native as N
 from .scene import _join, pack_scene, primary_params, stages_of
 
 
+_HAVE_CUDA = False
+
+
 def _device():
-    if not torch.cuda.is_available():
-        raise RuntimeError("iactrace_gb300 renders on a CUDA device; none is available")
+    global _HAVE_CUDA
+    if not _HAVE_CUDA:
+        if not torch.cuda.is_available():
+            raise RuntimeError("iactrace_gb300 renders on a CUDA device; none is available")
+        _HAVE_CUDA = True
     return torch.device("cuda", torch.cuda.current_device())
 
 
@@ -224,6 +230,63 @@ def _opts_with_seed(opts, seed):
     return o
 
 
+def _state_key(tel, sensor):
+    """Identity of everything a forward launch packs: the telescope, its
+    mirror groups and every field of them (tensors by object and version
+    counter), the obstruction groups, the sensor and its fields. None when
+    some group tensor requires grad (the autograd path). Objects are held by
+    the telescope and the sensor, so their ids stay unique while cached."""
+    key = [id(tel), id(sensor)]
+    for g in tel.mirror_groups:
+        key.append(id(g))
+        for v in g.__dict__.values():
+            if isinstance(v, torch.Tensor):
+                if v.requires_grad:
+                    return None
+                key.append(id(v))
+                key.append(v._version)
+            else:
+                key.append(id(v))
+    key.append(-1)
+    key.extend(map(id, tel.obstruction_groups or ()))
+    key.append(-2)
+    for v in sensor.__dict__.values():
+        key.append(id(v))
+        if isinstance(v, torch.Tensor):
+            key.append(v._version)
+    return tuple(key)
+
+
+def _fast_forward(tel, sensor, sensor_idx, src, val, code, mode, shape, opts, device):
+    """Repeated forward calls on an unchanged telescope: the packed scene,
+    the facet transforms, the sensor descriptor and the workspace size come
+    from a per-telescope cache validated by _state_key, not from re-hashing
+    the tensor storages; the launch is then two allocations and one call.
+    Returns None when the cache does not apply."""
+    key = _state_key(tel, sensor)
+    if key is None:
+        return None
+    cache = tel.__dict__.setdefault("_fast", {})
+    ck = (device.index, sensor_idx, mode, int(src.shape[0]))
+    hit = cache.get(ck)
+    if hit is None or hit[0] != key:
+        ps = pack_scene(tel, device)
+        sdesc, keep = sensor.pack(device)
+        ws_bytes = max(ps.workspace_bytes(sdesc, int(src.shape[0]), mode), 256)
+        # after packing: the packing caches stored on the sensor are part of its fields
+        hit = (_state_key(tel, sensor), ps, (ps.facet_rot, ps.facet_pos, ps.facet_scale), sdesc, keep, ws_bytes)
+        cache[ck] = hit
+    _, ps, facets, sdesc, keep, ws_bytes = hit
+    ps.set_facets(*facets)  # a packed scene may be shared by telescopes with other facet transforms
+    out = torch.empty(shape, dtype=torch.float32, device=device)
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device=device)
+    stream = torch.cuda.current_stream(device).cuda_stream
+    N.check(N.load().iact_render(ctypes.byref(ps.desc), ctypes.byref(sdesc), code, src.data_ptr(), val.data_ptr(),
+                                 int(src.shape[0]), mode, out.data_ptr(), ws.data_ptr(), ws_bytes,
+                                 ctypes.byref(opts) if opts is not None else None, stream))
+    return out
+
+
 def _launch(tel, sources, values, source_type, sensor_idx, mode, opts=None, seed=0):
     device = _device()
     sensor = tel.sensors[sensor_idx]
@@ -235,6 +298,10 @@ def _launch(tel, sources, values, source_type, sensor_idx, mode, opts=None, seed
     if 0 not in stages_of(tel):  # core/render.py:197-199 empty telescope
         return torch.zeros(shape, device=device)
     code = source_code(source_type)
+    if not (torch.is_grad_enabled() and (src.requires_grad or val.requires_grad)):
+        out = _fast_forward(tel, sensor, sensor_idx, src, val, code, mode, shape, opts, device)
+        if out is not None:
+            return out
     if _needs_grad(tel, src, val):
         rot, pos, scale = primary_params(tel, device)
         ps = pack_scene(tel, device, tuple(t.detach().contiguous() for t in (rot, pos, scale)))

@@ -219,3 +219,31 @@ def test_large_sample_counts_ragged(cuda):
     check_image(tel, src, val, st)
     tel2, src2, val2, st2 = W.response_matrix(n_samples=45, n_side=5)
     check_image(tel2, src2, val2, st2, mode="response")
+
+
+def test_repeated_renders_follow_in_place_changes(cuda):
+    """Repeated render() calls on one telescope reuse its packed scene and
+    sensor descriptor; every in-place change still reaches the kernels: the
+    result equals a render of a freshly built telescope in the same state."""
+    from iactrace_gb300 import Telescope
+    tel, src, val, st = W.plain_forward(n_samples=64, n_sources=4)
+
+    def fresh():
+        groups = [g.replace(**{k: getattr(g, k).clone() for k in ("rotations", "positions", "weights")})
+                  for g in tel.mirror_groups]
+        cam = type(tel.sensors[0])([float(v) for v in tel.sensors[0].position], [0.0, 0.0, 0.0], 32, 30,
+                                   (-0.672, 0.672, -0.63, 0.63), edge_width=tel.sensors[0].edge_width)
+        return it.render(Telescope(groups, tel.obstruction_groups, [cam]), src, val, st)
+
+    a = it.render(tel, src, val, st)
+    assert torch.equal(it.render(tel, src, val, st), a) or float((it.render(tel, src, val, st) - a).abs().max()) < 1e-5
+    g = tel.mirror_groups[0]
+    with torch.no_grad():
+        g.rotations[:, 0] += 0.02
+        g.weights[:5] *= 3.0
+    tel.sensors[0].position[2] += 0.05
+    tel.sensors[0].edge_width = 0.002
+    b = it.render(tel, src, val, st)
+    ref = fresh()
+    assert float((b - a).abs().max()) > 1e-3 * float(a.abs().max())
+    assert float((b - ref).abs().max()) <= 1e-5 * float(ref.abs().max())

@@ -78,3 +78,37 @@ def test_packed_scene_rejects_non_finite_samples():
         assert "NaN" in str(e)
     else:
         raise AssertionError("a NaN normal was packed")
+
+
+def test_fast_launch_key_follows_every_change():
+    """The key that lets repeated renders skip packing changes with every
+    edit that must reach the kernels, and is None on the autograd path."""
+    from iactrace_gb300.core.render import _state_key
+    from iactrace_gb300.core import Cylinder, group_obstructions
+    tel, src, val, st = W.plain_forward(n_samples=8, n_sources=2)
+    cam = tel.sensors[0]
+    k0 = _state_key(tel, cam)
+    assert k0 is not None and _state_key(tel, cam) == k0
+    g = tel.mirror_groups[0]
+    with torch.no_grad():
+        g.rotations[3, 0] += 0.01  # facet transform in place
+    k1 = _state_key(tel, cam)
+    assert k1 != k0
+    with torch.no_grad():
+        g.weights[0, 0] *= 2.0  # sample array in place
+    k2 = _state_key(tel, cam)
+    assert k2 != k1
+    g.perturbation_scale = g.perturbation_scale + 1e-6  # field replaced
+    k3 = _state_key(tel, cam)
+    assert k3 != k2
+    cam.position[2] += 0.1  # sensor pose in place
+    k4 = _state_key(tel, cam)
+    assert k4 != k3
+    cam.edge_width = 0.003  # sensor setting
+    k5 = _state_key(tel, cam)
+    assert k5 != k4
+    tel.obstruction_groups = list(tel.obstruction_groups) + group_obstructions([Cylinder([0, 0, 1], [0, 0, 2], 0.1)])
+    k6 = _state_key(tel, cam)
+    assert k6 != k5
+    tel2 = tel.set_mirror_rotations(0, g.rotations.clone().requires_grad_(True))
+    assert _state_key(tel2, tel2.sensors[0]) is None
