@@ -59,7 +59,14 @@ F_RAY = {"response": 537, "plain": 503, "cassegrain": 894, "batched": 537,
 # kernel sources it was taken on (source_digest() below); when the sources
 # have changed since, the figures are reported as stale and not used as the
 # roofline's traffic.
-CAPTURES = {}
+CAPTURES = {
+    "response": {"digest": "d2266b36b17830db", "profile": "profiles/k_render_response_matrix_dc380_hex2048.md",
+                 "dram_bytes": 7.337e6, "shared_atomic_frac": 0.124, "thread_inst_per_ray": 219,
+                 "fma_pipe": 0.247, "issue_active": 0.834},
+    "plain": {"digest": "d2266b36b17830db", "profile": "profiles/k_render_plain_forward_dc380_square960.md",
+              "dram_bytes": 12.24e6, "shared_atomic_frac": 0.060, "thread_inst_per_ray": 210,
+              "fma_pipe": 0.200, "issue_active": 0.653},
+}
 
 
 def source_digest() -> str:

@@ -15,7 +15,11 @@
 // Rules of use:
 //   * The first call on each device looks up the array's device address
 //     (cudaGetSymbolAddress, with that device current) and caches it; make
-//     that first call before any stream capture on the device.
+//     that first call before any stream capture on the device. The cached
+//     address belongs to the device context it was looked up in: after a
+//     cudaDeviceReset the library's module is loaded again and the array may
+//     move, so a process that resets a device must not call this entry point
+//     on it again.
 //   * Every call on a device shares the one array. The render clears what
 //     must start at zero (tile counter, FP64 accumulator) and rewrites the
 //     rest each call, but two calls that overlap on the GPU (different

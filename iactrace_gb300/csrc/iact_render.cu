@@ -66,27 +66,17 @@ __global__ void __launch_bounds__(256, STAGES ? 3 : IACT_RENDER_MIN_CTAS) k_rend
   sink.g = p.acc;
 
   __syncthreads();
-  // Image mode: every tile adds into the same image row, so the FP32 row
-  // collects p.flush_every tiles (a bounded number of rays, as many as one
-  // tile of the default size) before it goes to the FP64 accumulator, and
-  // what is left goes at the end. Small tiles then balance a short launch
-  // without multiplying the FP64 flushes.
-  int pending = 0;
   for (;;) {
     if (threadIdx.x == 0) s_tile = atomicAdd(p.counter, 1);
     __syncthreads();
     const int tile = s_tile;
     if (tile >= p.n_tiles) break;
-    const bool flush = (MODE == IACT_MODE_RESPONSE) || (++pending >= p.flush_every);
-    if (flush) pending = 0;
     // single-stage scenes with an axis-aligned sensor (the common case) take
     // the plane hit without the frame's dot products; p.sn.axes is uniform.
     // Not for extended sources, whose kernels would spill with two tile bodies.
-    if (!STAGES && SRC != IACT_SRC_EXTENDED && p.sn.axes)
-      render_tile<SRC, SOFT, MODE, STAGES, true>(p, ob, mir, htab, sh_hist, sink, tile, tmask, flush);
-    else render_tile<SRC, SOFT, MODE, STAGES>(p, ob, mir, htab, sh_hist, sink, tile, tmask, flush);
+    if (!STAGES && SRC != IACT_SRC_EXTENDED && p.sn.axes) render_tile<SRC, SOFT, MODE, STAGES, true>(p, ob, mir, htab, sh_hist, sink, tile, tmask);
+    else render_tile<SRC, SOFT, MODE, STAGES>(p, ob, mir, htab, sh_hist, sink, tile, tmask);
   }
-  if (MODE == IACT_MODE_IMAGE && pending > 0 && p.rows_in_smem) flush_rows(p, sh_hist, 0, 1);
 }
 
 // FP64 accumulator -> FP32 output
@@ -378,7 +368,10 @@ int plan_tiles(RenderK& p, int mode, int block, const iact_opts_t* opts, long lo
   // warp tasks (32 rays each) per tile; candidate masks stay within 16 KiB
   int target = std::max(1, std::min(nw * tpw, p.n_words ? 4096 / p.n_words : 1 << 30));
   for (;;) {
-    const int CC = std::max(1, std::min(nch, std::max(1, target / SB)));
+    int CC = std::max(1, std::min(nch, std::max(1, target / SB)));
+    // split a facet's chunks evenly between its tiles (8 chunks in tiles of
+    // 6: 4 + 4, not 6 + 2; a 276-primitive scene 281 -> 250 us)
+    CC = (nch + (nch + CC - 1) / CC - 1) / ((nch + CC - 1) / CC);
     int FC = (opts && opts->facets_per_tile > 0) ? opts->facets_per_tile : std::max(1, target / (SB * CC));
     FC = std::max(1, std::min(FC, p.F));
     p.SB = SB; p.FC = FC; p.CC = CC;
@@ -437,7 +430,8 @@ int launch_render(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type,
   if (block % 32 || block > 256) return set_error(IACT_E_INVALID, "opts.block_threads must be a multiple of 32, <= 256");
   DevInfo di = device_info();
   // tiles per SM below which small launches shrink their tiles: each tile
-  // recomputes its candidate masks and ends with a barrier, so cheap rays
+  // recomputes its candidate masks and ends with a barrier and a flush of
+  // its histogram rows, so cheap rays
   // (single-stage scenes with few primitives) want fewer, larger tiles, and
   // costly or uneven rays (stage mirrors, many shadowing primitives) a finer
   // balance (measured: 1000-sample plain forward 7 % faster at 4 than at 8
@@ -446,10 +440,6 @@ int launch_render(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type,
   const long long tiles_per_sm = sc->n_mirrors > 0 ? 8 : (n_primitives(sc) > 32 ? 10 : 4);
   rc = plan_tiles(p, mode, block, opts, tiles_per_sm * std::max(di.sm_count, 1));
   if (rc) return rc;
-  // image mode: the FP32 row collects at most the rays of one default tile
-  // (48 warp tasks per warp) between FP64 flushes, whatever the tile size
-  const long long tile_rays = 32LL * p.SB * p.FC * p.CC;
-  p.flush_every = (int)std::max(1LL, (32LL * 48 * (block / 32)) / std::max(tile_rays, 1LL));
   const size_t mask_bytes = sizeof(uint32_t) * (size_t)p.n_words * p.SB * p.FC;
   const size_t budget = (size_t)std::min(di.smem_optin > 0 ? di.smem_optin : 49152, 200 * 1024) - mask_bytes;
   SmemPlan sp;

@@ -192,7 +192,6 @@ struct RenderK {
   uint32_t seed;  // jitter stream of extended sources
   const float4* B4;  // per facet bundle bounds (culling on)
   int n_words;       // 32-bit candidate-mask words per task; 0 = no culling
-  int flush_every;   // image mode: tiles per flush of the FP32 row to `acc` (0 or 1: every tile)
 };
 
 // Where hits go: FP32 shared-memory rows of the current tile, or the FP64
@@ -427,26 +426,9 @@ __device__ __forceinline__ void warp_masks(const float4* B4, const float* source
   __syncwarp();
 }
 
-// The tile's FP32 shared-memory rows (rows from `base`) into the FP64
-// accumulator, cleared for the next tile. CTA-collective; call after a
-// barrier that follows the last add.
-__device__ __forceinline__ void flush_rows(const RenderK& p, float* sh_hist, int base, int nrows) {
-  for (int i = threadIdx.x; i < nrows * p.P; i += blockDim.x) {
-    const float h = sh_hist[i];
-    if (h != 0.f) {
-      atomicAdd(p.acc + (size_t)base * p.P + i, (double)h);
-      sh_hist[i] = 0.f;
-    }
-  }
-}
-
-// flush: the tile ends with flush_rows (response tiles always: their rows
-// belong to the tile's sources; image tiles may leave the one image row to
-// collect further tiles, see k_render).
 template <int SRC, bool SOFT, int MODE, bool STAGES, bool AX = false>
 __device__ __forceinline__ void render_tile(const RenderK& p, const Obst& ob, const float* mir, const short* htab,
-                                            float* sh_hist, const Sink& sink, int tile, uint32_t* tmask,
-                                            bool flush = true) {
+                                            float* sh_hist, const Sink& sink, int tile, uint32_t* tmask) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5, nthr = blockDim.x;
   const int nch = (p.M + 31) >> 5;
   const int per_s = p.n_fchunk * p.n_cchunk;
@@ -522,9 +504,18 @@ __device__ __forceinline__ void render_tile(const RenderK& p, const Obst& ob, co
   }
   if (!SOFT && rl_key >= 0) sink.add(rl_key, rl_val);
   __syncthreads();
-  // this tile's FP32 rows -> FP64 accumulator, then clear for the next tile
-  if (p.rows_in_smem && (flush || MODE == IACT_MODE_RESPONSE))
-    flush_rows(p, sh_hist, (MODE == IACT_MODE_RESPONSE) ? s0 : 0, (MODE == IACT_MODE_RESPONSE) ? SBc : 1);
+  if (p.rows_in_smem) {
+    // this tile's FP32 rows -> FP64 accumulator, then clear for the next tile
+    const int base = (MODE == IACT_MODE_RESPONSE) ? s0 : 0;
+    const int nrows = (MODE == IACT_MODE_RESPONSE) ? SBc : 1;
+    for (int i = threadIdx.x; i < nrows * p.P; i += nthr) {
+      const float h = sh_hist[i];
+      if (h != 0.f) {
+        atomicAdd(p.acc + (size_t)base * p.P + i, (double)h);
+        sh_hist[i] = 0.f;
+      }
+    }
+  }
 
 }
 

@@ -197,8 +197,10 @@ int iact_render(const iact_scene_t* scene, const iact_sensor_t* sensor,
  * IACT_NOALLOC_SCRATCH_BYTES array inside the library, held by every GPU
  * that loads it until exit. Larger requests fail with IACT_E_UNSUPPORTED.
  * The first call per device resolves the array's address (make it before
- * any stream capture); calls overlapping on the GPU race on the shared
- * array. Arguments and results as iact_render. */
+ * any stream capture) and keeps it for the process: after a
+ * cudaDeviceReset of that device this entry point must not be called on it
+ * again. Calls overlapping on the GPU race on the shared array. Arguments
+ * and results as iact_render. */
 #define IACT_NOALLOC_SCRATCH_BYTES (16u << 20)
 int iact_render_noalloc(const iact_scene_t* scene, const iact_sensor_t* sensor,
                         int32_t source_type, const float* sources,

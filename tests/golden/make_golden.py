@@ -23,10 +23,16 @@ Cases:
                  (cylinder, box, sphere, oriented box, triangle), point
                  sources at 1 km, square + hex cameras with edge bands and
                  the two soft-splat sensors
+  seg_cassegrain the Cassegrain primary with a segmented secondary (three
+                 disk segments and a central hexagon cut from one
+                 hyperboloid: two mirror groups in stage 1), 4 parallel
+                 sources, square camera
 
 The per-ray sensor-plane hits and values of the first sensor are stored
 (debug_pts, debug_vals), and for a hard first sensor also the pixel id the
-reference's own accumulate gives each hit (debug_pix, -1 for none).
+reference's own accumulate gives each hit (debug_pix, -1 for none); for
+scenes with one later stage, the stage mirror each ray's closest hit takes
+(debug_hit_mirror, -1 for none).
 
 Usage: IACTRACE_REFERENCE=<checkout of GerritRo/iactrace> python tests/golden/make_golden.py [case ...]
 """
@@ -111,6 +117,36 @@ def scene_cassegrain(sec_radius=1.2, theta_deg=(0.0, 0.4, 0.7, 0.9)):
     return tel, jnp.array(d), jnp.array([1.0, 2.0, 0.5, 1.5]), "parallel", [0]
 
 
+def scene_seg_cassegrain():
+    """The Cassegrain primary with a segmented secondary: three disk
+    segments around the axis and a central hexagonal one, cut from one
+    hyperboloid (two mirror groups in stage 1), so the closest-hit choice
+    between mirrors of a stage decides every ray; 4 parallel sources."""
+    base, _, _, _, _ = scene_cassegrain()
+    f = 10.0
+    a, ch = 1.25, 5.25
+    sec = AsphericSurface(curvature=-a / (ch * ch - a * a), conic=-(ch / a) ** 2, aspheric=jnp.array([1e-4]))
+    segs = []
+    for k in range(3):
+        ang = math.radians(120 * k + 30)
+        x0, y0 = 0.7 * math.cos(ang), 0.7 * math.sin(ang)
+        z0 = float(A(sec._sag_raw(jnp.array(x0), jnp.array(y0))))
+        # the parent's frame is tipped by 180 deg (local y and z flip in the world)
+        segs.append(Mirror(position=jnp.array([x0, -y0, 6.0 - z0]), rotation=jnp.array([180.0, 0.0, 0.0]),
+                           surface=sec, aperture=DiskAperture(0.58), offset=jnp.array([x0, y0]), optical_stage=1))
+    rc = 0.34
+    hexv = [[rc * math.cos(math.radians(60 * k)), rc * math.sin(math.radians(60 * k))] for k in range(6)]
+    segs.append(Mirror(position=jnp.array([0.0, 0.0, 6.0]), rotation=jnp.array([180.0, 0.0, 0.0]), surface=sec,
+                       aperture=PolygonAperture(jnp.array(hexv)), optical_stage=1))
+    prim = [g for g in base.mirror_groups if g.optical_stage == 0]
+    tel = Telescope(mirror_groups=prim + group_mirrors(segs), obstruction_groups=[], sensors=base.sensors,
+                    name="cass_segmented")
+    th = np.radians([0.0, 0.25, 0.45, 0.6])
+    ph = np.radians([0.0, 75.0, 160.0, 250.0])
+    d = np.stack([np.sin(th) * np.cos(ph), np.sin(th) * np.sin(ph), -np.cos(th)], 1)
+    return tel, jnp.array(d), jnp.array([1.0, 2.0, 0.5, 1.5]), "parallel", [0]
+
+
 def _hex_points(n, pitch):
     pts = []
     for q in range(-6, 7):
@@ -167,7 +203,8 @@ def scene_dc_mixed():
     return tel, src, jnp.array([1.0, 0.6, 0.8]), "point", [0, 1, 2, 3]
 
 
-CASES = {"ct3_point": scene_ct3, "cass_parallel": scene_cassegrain, "dc_mixed": scene_dc_mixed}
+CASES = {"ct3_point": scene_ct3, "cass_parallel": scene_cassegrain, "dc_mixed": scene_dc_mixed,
+         "seg_cassegrain": scene_seg_cassegrain}
 
 
 # --------------------------------------------------------------- recording
@@ -262,6 +299,43 @@ def ref_pixel_ids(sensor, pts):
     return out
 
 
+def ref_hit_mirror(tel, src, st):
+    """Per ray (order facet, source, sample) the stage-1 mirror that the
+    reference's closest-hit choice takes (core/render.py:44-115): each
+    mirror's t from the reference's own _intersect_group on a one-mirror
+    group, the first of the minimal t in the scene's group and mirror order
+    (argmin within a group, strict `<` across groups), -1 without a hit
+    (t >= 1e10). Scenes with one later stage."""
+    from iactrace.core.reflection import reflect
+    from iactrace.core.render import _get_stages, _intersect_group
+    stages = _get_stages(tel.mirror_groups)
+    assert sorted(stages) == [0, 1]
+    data = [g.transform_to_world() for g in stages[0]]
+    tp_all = np.concatenate([A(d[0]) for d in data])
+    tn_all = np.concatenate([A(d[1]) for d in data])
+    singles = []
+    for g in stages[1]:
+        names = ["positions", "rotations", "offsets"] + (["radii"] if hasattr(g, "radii") else ["vertices"])
+        for j in range(len(g)):
+            singles.append(eqx.tree_at(lambda q: tuple(getattr(q, n) for n in names), g,
+                                       tuple(getattr(g, n)[j:j + 1] for n in names)))
+    srcs = A(src)
+    out = []
+    for f in range(tp_all.shape[0]):
+        tp, tn = jnp.array(tp_all[f]), jnp.array(tn_all[f])
+        for s in range(srcs.shape[0]):
+            if st == "point":
+                w = tp_all[f] - srcs[s][None, :]
+                d = jnp.array(w / np.linalg.norm(w, axis=-1, keepdims=True))
+            else:
+                d = jnp.array(np.broadcast_to(srcs[s], tp_all[f].shape))
+            r = jax.vmap(reflect)(d, tn)[0]
+            T = np.stack([A(_intersect_group(tp, r, g1)[0]) for g1 in singles])
+            best = np.argmin(T, axis=0)
+            out.append(np.where(T.min(axis=0) < 1e10, best, -1))
+    return np.concatenate(out).astype(np.int32)
+
+
 def run_case(name):
     t0 = time.time()
     tel, src, val, st, sensors = CASES[name]()
@@ -288,6 +362,8 @@ def run_case(name):
             rec["debug_pts"], rec["debug_vals"] = A(pts), A(vals)
             if "Differentiable" not in type(tel.sensors[si]).__name__:
                 rec["debug_pix"] = ref_pixel_ids(tel.sensors[si], A(pts))
+            if sorted({g.optical_stage for g in tel.mirror_groups}) == [0, 1]:
+                rec["debug_hit_mirror"] = ref_hit_mirror(tel, src, st)
     out = os.path.join(HERE, f"{name}_{SUFFIX}.npz")
     np.savez_compressed(out, **rec)
     print(f"{name} ({SUFFIX}): {time.time() - t0:.1f} s -> {os.path.basename(out)} "

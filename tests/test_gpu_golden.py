@@ -5,6 +5,8 @@ float64 runs on the same sampled arrays), through the C ABI.
 * float64 fixtures: plane hits, ray values and images (soft sensors to
   SOFT_TOL relative L2).
 * float32 fixtures (the reference at its own precision, JAX's default):
+  - per ray, the stage mirror of the closest hit equals the reference's
+    choice (segmented secondary: two mirror groups in one stage);
   - per ray, the GPU's hard pixel id equals the pixel id the reference's own
     accumulate gave its float32 hit, except for rays whose FP64 hit lies
     within EDGE_BAND = 4e-6 m of a pixel edge; the count of mismatches with
@@ -88,8 +90,14 @@ def test_gpu_pixel_ids_match_reference_float32(cuda, case):
     tel = FX.telescope(fx)
     src, val, st = FX.inputs(fx)
     si = FX.sensor_ids(fx)[0]
-    _, _, pix, _ = it.render_debug(tel, src, val, st, si, extras=True)
+    _, _, pix, hm = it.render_debug(tel, src, val, st, si, extras=True)
     pix = pix.cpu().numpy()
+    if "debug_hit_mirror" in fx:
+        # the stage mirror of each ray's closest hit (core/render.py:44-115)
+        hm = hm.cpu().numpy()
+        n_mm = int((hm != fx["debug_hit_mirror"]).sum())
+        print(f"{case}: {n_mm} of {hm.size} stage-mirror choices differ from the reference float32 run")
+        assert n_mm == 0
     ref = fx["debug_pix"]
     margin = O.render_debug(tel, src, val, st, si, "f64")["margin"]
     mism = pix != ref

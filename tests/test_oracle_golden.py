@@ -59,6 +59,10 @@ def test_rays_match_reference(built, case, kind):
         # the restatement at the same precision decides every ray alike
         assert np.array_equal(d["pix"], fx["debug_pix"]), \
             f"{int((d['pix'] != fx['debug_pix']).sum())} pixel ids differ from the reference's"
+    if "debug_hit_mirror" in fx:
+        # the stage mirror of each ray's closest hit, as the reference chose it
+        assert np.array_equal(d["hit_mirror"], fx["debug_hit_mirror"]), \
+            f"{int((d['hit_mirror'] != fx['debug_hit_mirror']).sum())} stage-mirror choices differ"
     zero = (ref_vals == 0) != (d["vals"] == 0)
     assert zero.sum() <= max(1, 1e-4 * zero.size), f"{zero.sum()} shadow/hit decisions differ"
     same = ~zero

@@ -26,6 +26,15 @@ pytestmark = pytest.mark.gpu
 IMG_TOL = 1e-5  # the image tolerance of the forward parity tests
 
 
+def _scratch_bytes():
+    """IACT_NOALLOC_SCRATCH_BYTES as the C header defines it."""
+    import os
+    import re
+    hdr = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "iactrace_gb300.h")
+    m = re.search(r"#define IACT_NOALLOC_SCRATCH_BYTES \((\d+)u << (\d+)\)", open(hdr).read())
+    return int(m.group(1)) << int(m.group(2))
+
+
 def _bind(lib):
     fn = lib.iact_render_noalloc
     fn.argtypes = [ctypes.POINTER(N.IactScene), ctypes.POINTER(N.IactSensor), ctypes.c_int32, ctypes.c_void_p,
@@ -82,4 +91,58 @@ def test_noalloc_rejects_work_beyond_its_scratch(cuda):
     assert rc == N.IACT_E_UNSUPPORTED
     assert b"scratch" in lib.iact_last_error()
     assert float(out.abs().sum()) == 0.0  # nothing was queued
+    del keep
+
+
+LIMIT = _scratch_bytes()
+
+
+def _largest_fitting_sources(lib, ps, sd, mode):
+    """The largest source count whose scratch fits the fixed array."""
+    def need(S):
+        size = ctypes.c_size_t(0)
+        N.check(lib.iact_workspace_size(ctypes.byref(ps.desc), ctypes.byref(sd), int(S), mode, ctypes.byref(size)))
+        return int(size.value)
+    lo, hi = 1, 1
+    while need(hi) <= LIMIT:
+        lo, hi = hi, hi * 2
+    while hi - lo > 1:
+        mid = (lo + hi) // 2
+        lo, hi = (mid, hi) if need(mid) <= LIMIT else (lo, mid)
+    return lo, need(lo), need(lo + 1)
+
+
+def test_noalloc_at_the_limit_with_options(cuda):
+    """A response render whose scratch just fits the array gives what
+    iact_render gives (also with non-default launch options: 128 threads per
+    CTA), and one source more is refused before anything is queued."""
+    lib = N.load()
+    fn = _bind(lib)
+    tel, _, _, st = W.plain_forward(n_samples=16, n_sources=1)
+    ps = pack_scene(tel, cuda)
+    sd, keep = tel.sensors[0].pack(cuda)
+    S, need, need_more = _largest_fitting_sources(lib, ps, sd, N.MODE_RESPONSE)
+    assert need <= LIMIT < need_more
+    assert need > LIMIT - 16 * 1024  # within one output row or so of the limit
+    src = W.point_sources_disk(S + 1, 2.5, 3).to(cuda).contiguous()
+    val = (torch.rand(S + 1, generator=torch.Generator().manual_seed(4)) + 0.5).to(cuda).contiguous()
+    P = tel.sensors[0].n_pixels
+    stream = torch.cuda.current_stream(cuda).cuda_stream
+    ref = _with_workspace(lib, ps, sd, st, src[:S], val[:S], N.MODE_RESPONSE, (S, P), stream).double().cpu().numpy()
+    opts = N.IactOpts()
+    opts.block_threads = 128
+    for o in (None, opts):
+        out = torch.full((S, P), float("nan"), device=cuda)
+        rc = fn(ctypes.byref(ps.desc), ctypes.byref(sd), source_code(st), src.data_ptr(), val.data_ptr(), S,
+                N.MODE_RESPONSE, out.data_ptr(), ctypes.byref(o) if o is not None else None, stream)
+        assert rc == N.IACT_OK, lib.iact_last_error()
+        got = out.double().cpu().numpy()
+        assert np.isfinite(got).all()
+        err = np.linalg.norm(got - ref) / np.linalg.norm(ref)
+        assert err <= IMG_TOL, f"opts {o is not None}: relative L2 {err:.3g} against iact_render"
+    out = torch.zeros((S + 1, P), device=cuda)
+    rc = fn(ctypes.byref(ps.desc), ctypes.byref(sd), source_code(st), src.data_ptr(), val.data_ptr(), S + 1,
+            N.MODE_RESPONSE, out.data_ptr(), None, stream)
+    assert rc == N.IACT_E_UNSUPPORTED
+    assert float(out.abs().sum()) == 0.0
     del keep
