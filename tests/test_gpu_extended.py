@@ -86,3 +86,24 @@ def test_alignment_graph_replay_matches_eager(cuda):
     graph = A.run(pb, steps=10, lr=4e-3, graph=True)
     assert np.allclose(graph["loss"], eager["loss"], rtol=1e-3), (graph["loss"], eager["loss"])
     assert np.allclose(graph["rms_mrad"], eager["rms_mrad"], rtol=1e-3)
+
+
+def test_alignment_recovers_tilts_where_identifiable(cuda):
+    """The adjoint drives the facet tilts to the truth when the image
+    determines them: with the camera 12 m below the focus, each facet's
+    spot lands apart from the others and moves with that facet's own tilt,
+    and Adam on the image loss recovers all tips and tilts (19 facets,
+    sigma 1 mrad). At the focus every facet's spot of a source falls on the
+    same place and the same run leaves the tilts unresolved."""
+    runs = {}
+    for z, cam in ((24.0, (64, 1.6)), (36.0, (64, 0.5))):
+        pb = A.problem(n_facets=19, n_samples=64, n_sources=4, sigma_true_mrad=1.0, camera_z=z, square_camera=cam,
+                       max_deg=0.3)
+        runs[z] = A.run(pb, steps=200, lr=2e-3)
+    h = runs[24.0]
+    print(f"defocused: loss {h['loss'][0]:.3e} -> {h['loss'][-1]:.3e}, rms tilt error "
+          f"{h['rms_mrad'][0]:.3f} -> {h['rms_mrad'][-1]:.4f} mrad; at the focus: rms "
+          f"{runs[36.0]['rms_mrad'][0]:.3f} -> {runs[36.0]['rms_mrad'][-1]:.3f} mrad")
+    assert h["rms_mrad"][-1] < 0.02 * h["rms_mrad"][0]
+    assert h["loss"][-1] < 1e-4 * h["loss"][0]
+    assert runs[36.0]["rms_mrad"][-1] > 0.5 * runs[36.0]["rms_mrad"][0]
