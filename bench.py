@@ -806,6 +806,21 @@ def main():
         torch.cuda.synchronize(dev)
         wall.append(time.perf_counter() - t0)
     wall_s = sorted(wall)[len(wall) // 2]
+    # the same call through a RenderPlan (copies in, render, copy out as one
+    # CUDA graph per call), host clock, one call at a time; the result lands
+    # in the plan's pinned buffer
+    plan = it.RenderPlan(tel, S, stype, mode=mode)
+    for _ in range(2):
+        plan(src_h, val_h, copy=False)
+    pw = []
+    for k in range(args.steps):
+        flush_buf.fill_(float(k))
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        plan(src_h, val_h, copy=False)
+        pw.append(time.perf_counter() - t0)
+    plan_s = sorted(pw)[len(pw) // 2]
+    del plan
     clk = clocks.stop()
 
     t = torch.tensor([step_s, kern_s, e2e_s], device=dev, dtype=torch.float64)
@@ -827,7 +842,10 @@ def main():
                 "timing": "CUDA events around each step's copies and call (host issue overlapped)",
                 "host_wall": {"value": rays * world / wall_s, "unit": "rays/s", "ms_per_step": wall_s * 1e3,
                               "timing": "host clock around call + copies + synchronize, one step at a time "
-                                        "(median)"}},
+                                        "(median)"},
+                "plan_host_wall": {"value": rays * world / plan_s, "unit": "rays/s", "ms_per_step": plan_s * 1e3,
+                                   "timing": "RenderPlan: copies in, render, copy out replayed as one CUDA graph "
+                                             "per call; host clock, one call at a time (median)"}},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                      "traffic": cap["dram_bytes"] if cap_ok else None,
                      "traffic_unit": "bytes per launch (ncu dram__bytes_read + write)",
