@@ -66,6 +66,9 @@ CAPTURES = {
     "plain": {"digest": "d2266b36b17830db", "profile": "profiles/k_render_plain_forward_dc380_square960.md",
               "dram_bytes": 12.24e6, "shared_atomic_frac": 0.060, "thread_inst_per_ray": 210,
               "fma_pipe": 0.200, "issue_active": 0.653},
+    "cassegrain": {"digest": "d2266b36b17830db", "profile": "profiles/k_render_cassegrain_61seg_square1024.md",
+                   "dram_bytes": 1.049e6, "shared_atomic_frac": 0.026, "thread_inst_per_ray": 941,
+                   "fma_pipe": 0.390, "issue_active": 0.738},
 }
 
 
