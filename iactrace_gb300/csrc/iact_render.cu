@@ -477,18 +477,22 @@ int launch_debug(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type, 
   const int block = 256;
   const int grid = (int)std::min<long long>((n + block - 1) / block, 1 << 20);
   const bool stages = sc->n_mirrors > 0;
-  if (smem > 48 * 1024) return set_error(IACT_E_UNSUPPORTED, "scene tables too large for the debug kernel");
+  const DevInfo di = device_info();
+  // tables of up to IACT_MAX_OBSTRUCTIONS primitives exceed the 48 KiB a
+  // kernel gets without opting in; resident_ctas opts in
+  if (smem > (size_t)std::max(di.smem_optin, 48 * 1024))
+    return set_error(IACT_E_UNSUPPORTED, "scene tables exceed the shared memory of an SM");
   p.seed = seed;
-  if (src_type == IACT_SRC_POINT) {
-    if (stages) k_debug<IACT_SRC_POINT, true><<<grid, block, smem, st>>>(p, pts, vals, pix, hit_mirror);
-    else k_debug<IACT_SRC_POINT, false><<<grid, block, smem, st>>>(p, pts, vals, pix, hit_mirror);
-  } else if (src_type == IACT_SRC_EXTENDED) {
-    if (stages) k_debug<IACT_SRC_EXTENDED, true><<<grid, block, smem, st>>>(p, pts, vals, pix, hit_mirror);
-    else k_debug<IACT_SRC_EXTENDED, false><<<grid, block, smem, st>>>(p, pts, vals, pix, hit_mirror);
-  } else {
-    if (stages) k_debug<IACT_SRC_PARALLEL, true><<<grid, block, smem, st>>>(p, pts, vals, pix, hit_mirror);
-    else k_debug<IACT_SRC_PARALLEL, false><<<grid, block, smem, st>>>(p, pts, vals, pix, hit_mirror);
-  }
+  void (*kern)(const RenderK, float*, float*, int32_t*, int32_t*);
+  if (src_type == IACT_SRC_POINT) kern = stages ? k_debug<IACT_SRC_POINT, true> : k_debug<IACT_SRC_POINT, false>;
+  else if (src_type == IACT_SRC_EXTENDED)
+    kern = stages ? k_debug<IACT_SRC_EXTENDED, true> : k_debug<IACT_SRC_EXTENDED, false>;
+  else kern = stages ? k_debug<IACT_SRC_PARALLEL, true> : k_debug<IACT_SRC_PARALLEL, false>;
+  int per_sm = 0;
+  rc = resident_ctas(reinterpret_cast<const void*>(kern), block, smem, &per_sm);
+  if (rc) return rc;
+  if (per_sm < 1) return set_error(IACT_E_UNSUPPORTED, "debug kernel does not fit on an SM with these tables");
+  kern<<<grid, block, smem, st>>>(p, pts, vals, pix, hit_mirror);
   return check_cuda(cudaGetLastError(), "k_debug launch");
 }
 

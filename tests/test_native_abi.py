@@ -183,3 +183,23 @@ def test_tile_defaults_without_a_gpu(built):
     assert tiles(soft, N.MODE_RESPONSE) == 16 * 9
     assert tiles(hard, N.MODE_IMAGE) == 8 * 17
     assert tiles(hard, N.MODE_RESPONSE, tpw=48) == 16 * 9
+
+
+def test_size_limits_are_validated(built):
+    """The documented maxima pass and one more is refused, before any GPU
+    work: IACT_MAX_OBSTRUCTIONS primitives, IACT_MAX_STAGE_MIRRORS stage
+    mirrors, 2^30 primary samples."""
+    sn, sz = _square(), ctypes.c_size_t(0)
+
+    def ws(sc):
+        return built.iact_workspace_size(ctypes.byref(sc), ctypes.byref(sn), 1, N.MODE_IMAGE, ctypes.byref(sz))
+
+    assert ws(_fake_scene(4, 8, n_cyl=N.IACT_MAX_OBSTRUCTIONS)) == N.IACT_OK
+    assert ws(_fake_scene(4, 8, n_cyl=N.IACT_MAX_OBSTRUCTIONS + 1)) == N.IACT_E_UNSUPPORTED
+    assert b"IACT_MAX_OBSTRUCTIONS" in built.iact_last_error()
+    for n, rc in ((N.IACT_MAX_STAGE_MIRRORS, N.IACT_OK), (N.IACT_MAX_STAGE_MIRRORS + 1, N.IACT_E_UNSUPPORTED)):
+        sc = _fake_scene(4, 8)
+        sc.n_mirrors, sc.n_stages, sc.mirrors = n, 1, 0x10000
+        assert ws(sc) == rc, n
+    assert ws(_fake_scene(1 << 15, 1 << 15)) == N.IACT_OK
+    assert ws(_fake_scene(1 << 15, (1 << 15) + 1)) == N.IACT_E_UNSUPPORTED
