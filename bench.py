@@ -60,13 +60,13 @@ F_RAY = {"response": 537, "plain": 503, "cassegrain": 894, "batched": 537,
 # have changed since, the figures are reported as stale and not used as the
 # roofline's traffic.
 CAPTURES = {
-    "response": {"digest": "d2266b36b17830db", "profile": "profiles/k_render_response_matrix_dc380_hex2048.md",
+    "response": {"digest": "666267296bfba4c6", "profile": "profiles/k_render_response_matrix_dc380_hex2048.md",
                  "dram_bytes": 7.337e6, "shared_atomic_frac": 0.124, "thread_inst_per_ray": 219,
                  "fma_pipe": 0.247, "issue_active": 0.834},
-    "plain": {"digest": "d2266b36b17830db", "profile": "profiles/k_render_plain_forward_dc380_square960.md",
+    "plain": {"digest": "666267296bfba4c6", "profile": "profiles/k_render_plain_forward_dc380_square960.md",
               "dram_bytes": 12.24e6, "shared_atomic_frac": 0.060, "thread_inst_per_ray": 210,
               "fma_pipe": 0.200, "issue_active": 0.653},
-    "cassegrain": {"digest": "d2266b36b17830db", "profile": "profiles/k_render_cassegrain_61seg_square1024.md",
+    "cassegrain": {"digest": "666267296bfba4c6", "profile": "profiles/k_render_cassegrain_61seg_square1024.md",
                    "dram_bytes": 1.049e6, "shared_atomic_frac": 0.026, "thread_inst_per_ray": 941,
                    "fma_pipe": 0.390, "issue_active": 0.738},
 }
