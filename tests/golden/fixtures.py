@@ -10,7 +10,7 @@ import numpy as np
 import torch
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-CASES = ("ct3_point", "cass_parallel", "dc_mixed", "seg_cassegrain")
+CASES = ("ct3_point", "cass_parallel", "dc_mixed", "seg_cassegrain", "tilted_cams")
 
 
 def path(case: str, kind: str) -> str:

@@ -23,6 +23,9 @@ Cases:
                  (cylinder, box, sphere, oriented box, triangle), point
                  sources at 1 km, square + hex cameras with edge bands and
                  the two soft-splat sensors
+  tilted_cams    the 19-facet dish imaged by tilted and rolled square and
+                 hexagonal cameras (general plane-hit form; hexagon centres
+                 rotated by 10 deg), hard with edge bands and soft
   seg_cassegrain the Cassegrain primary with a segmented secondary (three
                  disk segments and a central hexagon cut from one
                  hyperboloid: two mirror groups in stage 1), 4 parallel
@@ -147,6 +150,37 @@ def scene_seg_cassegrain():
     return tel, jnp.array(d), jnp.array([1.0, 2.0, 0.5, 1.5]), "parallel", [0]
 
 
+def scene_tilted_cams():
+    """The 19-facet Davies-Cotton dish of dc_mixed (two cylinders and the
+    camera box as obstructions) imaged by tilted and rolled cameras: the
+    sensor frame is not the world's, so the plane hit takes the general
+    form, and the hexagonal camera's centres are rotated by 10 deg (a grid
+    rotation the detection must find); hard sensors with edge bands and the
+    two soft sensors; point sources at 1 km."""
+    base, src, val, st, _ = scene_dc_mixed()
+    obst = group_obstructions([
+        Cylinder([1.8, 1.0, 0.5], [0.4, 0.2, 8.3], 0.04),
+        Cylinder([-1.8, 1.0, 0.5], [-0.4, 0.2, 8.3], 0.04),
+        Box([-0.35, -0.3, 8.0], [0.35, 0.3, 8.9]),
+    ])
+    f = 8.0
+    c, sn = math.cos(math.radians(10.0)), math.sin(math.radians(10.0))
+    hp = _hex_points(91, 0.03)
+    hex_centers = np.stack([c * hp[:, 0] - sn * hp[:, 1], sn * hp[:, 0] + c * hp[:, 1]], 1)
+    rs, rh = [2.0, -1.5, 25.0], [-1.5, 1.0, 40.0]
+    sensors = [
+        SquareSensor(position=[0.01, -0.02, f], rotation=rs, width=20, height=16, bounds=(-0.3, 0.3, -0.24, 0.24),
+                     edge_width=0.002),
+        HexagonalSensor(position=[-0.01, 0.015, f], rotation=rh, hex_centers=jnp.array(hex_centers), edge_width=0.001),
+        DifferentiableSquareSensor(position=[0.01, -0.02, f], rotation=rs, width=20, height=16,
+                                   bounds=(-0.3, 0.3, -0.24, 0.24), sigma=0.4, kernel_size=2),
+        DifferentiableHexagonalSensor(position=[-0.01, 0.015, f], rotation=rh, hex_centers=jnp.array(hex_centers),
+                                      sigma=0.5, kernel_size=1),
+    ]
+    tel = Telescope(mirror_groups=base.mirror_groups, obstruction_groups=obst, sensors=sensors, name="dc19_tilted")
+    return tel, src, val, st, [0, 1, 2, 3]
+
+
 def _hex_points(n, pitch):
     pts = []
     for q in range(-6, 7):
@@ -204,7 +238,7 @@ def scene_dc_mixed():
 
 
 CASES = {"ct3_point": scene_ct3, "cass_parallel": scene_cassegrain, "dc_mixed": scene_dc_mixed,
-         "seg_cassegrain": scene_seg_cassegrain}
+         "seg_cassegrain": scene_seg_cassegrain, "tilted_cams": scene_tilted_cams}
 
 
 # --------------------------------------------------------------- recording

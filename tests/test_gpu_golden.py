@@ -111,6 +111,50 @@ def test_gpu_pixel_ids_match_reference_float32(cuda, case):
     assert n_out == 0, f"{n_out} pixel ids differ from the reference's away from pixel edges"
 
 
+def _flip_counts(tel, src, val, st, si):
+    """Pixel flips against the FP64 oracle's decisions: GPU, float32 restatement."""
+    import oracle.oracle as O
+    _, gv, gpix, _ = it.render_debug(tel, src, val, st, si, extras=True)
+    gpix, alive = gpix.cpu().numpy(), gv.cpu().numpy() != 0
+    d64 = O.render_debug(tel, src, val, st, si, "f64")
+    d32 = O.render_debug(tel, src, val, st, si, "f32")
+    return int(((gpix != d64["pix"]) & alive).sum()), int(((d32["pix"] != d64["pix"]) & (d32["vals"] != 0)).sum())
+
+
+@pytest.mark.parametrize("case", FX.CASES)
+def test_gpu_response_matrices_match_reference(cuda, case):
+    """Per-source rows (render_response_matrix, core/render.py:271-324)
+    against the reference's own float64 response matrices, where the
+    fixtures hold them (small sensors): soft sensors to SOFT_TOL; hard ones
+    no further from them than the reference's float32 matrices, or by edge
+    flips of single rays as in the image test."""
+    if not os.path.exists(FX.path(case, "f64")):
+        pytest.skip("fixture not generated")
+    f64, f32 = FX.load(case, "f64"), FX.load(case, "f32")
+    tel = FX.telescope(f32)
+    src, val, st = FX.inputs(f32)
+    sens = json.loads(str(f32["sensors_json"]))
+    n = 0
+    for si in FX.sensor_ids(f32):
+        if f"response_{si}" not in f64:
+            continue
+        ref64 = f64[f"response_{si}"].astype(np.float64)
+        ref32 = f32[f"response_{si}"].astype(np.float64)
+        R = it.render_response_matrix(tel, src, val, st, si).cpu().double().numpy()
+        scale = np.linalg.norm(ref64)
+        e_gpu, e_32 = np.linalg.norm(R - ref64) / scale, np.linalg.norm(ref32 - ref64) / scale
+        msg = f"{case} sensor {si}: response matrix against the reference float64: GPU {e_gpu:.3g}, float32 {e_32:.3g}"
+        print(msg)
+        n += 1
+        if "Differentiable" in sens[si]["class"]:
+            assert e_gpu < SOFT_TOL, msg
+        elif e_gpu > e_32 + RAW_SLACK:
+            n_gpu, n_32 = _flip_counts(tel, src, val, st, si)
+            assert n_gpu <= n_32 + FLIP_SLACK, f"{msg}; pixel flips GPU {n_gpu}, float32 {n_32}"
+    if n == 0:
+        pytest.skip("no response matrices in this fixture")
+
+
 @pytest.mark.parametrize("case", FX.CASES)
 def test_gpu_raw_image_error_within_reference_float32(cuda, case):
     """Per sensor: raw relative L2 against the FP64 oracle's image of the

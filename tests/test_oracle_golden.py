@@ -105,7 +105,7 @@ def test_images_match_reference(built, case, kind):
             assert np.linalg.norm(R - Rr) / np.linalg.norm(Rr) < tol
 
 
-@pytest.mark.parametrize("case", ["ct3_point", "dc_mixed"])
+@pytest.mark.parametrize("case", ["ct3_point", "dc_mixed", "tilted_cams"])
 def test_hex_sensor_construction_matches_reference(case):
     """Our float32 grid detection and lookup table equal the reference's
     (float32 run: JAX's default precision)."""
