@@ -79,6 +79,38 @@ __global__ void __launch_bounds__(256, STAGES ? 3 : IACT_RENDER_MIN_CTAS) k_rend
   }
 }
 
+// k_render for the common hard-pixel case (render_tile_hard): the host picks
+// it when the launch qualifies (single stage, point or parallel sources,
+// axis-aligned sensor, rows and hexagon table in shared memory, at most one
+// candidate word). Same shared-memory layout as k_render.
+template <int SRC, int MODE, bool HEX>
+__global__ void __launch_bounds__(256, IACT_RENDER_MIN_CTAS) k_render_hard(const RenderK p) {
+  extern __shared__ __align__(16) float smem[];
+  __shared__ int s_tile;
+  const int tab_n = (p.n_table_floats + 3) & ~3;
+  const int htab_n = HEX ? ((p.sn.table_q * p.sn.table_r + 7) & ~7) : 0;  // int16 entries
+  float* tab = smem;
+  short* htab = reinterpret_cast<short*>(smem + tab_n);
+  float* sh_hist = smem + tab_n + htab_n / 2;
+  const int hist_n = p.rows_in_smem * p.P;
+  uint32_t* tmask = reinterpret_cast<uint32_t*>(sh_hist + hist_n);
+  const int nthr = blockDim.x;
+
+  for (int i = threadIdx.x; i < p.n_table_floats; i += nthr) tab[i] = p.tables[i];
+  for (int i = threadIdx.x; i < htab_n; i += nthr)
+    htab[i] = (short)(i < p.sn.table_q * p.sn.table_r ? p.hex_table[i] : -1);
+  for (int i = threadIdx.x; i < hist_n; i += nthr) sh_hist[i] = 0.f;
+  const Obst ob = make_obst(tab, p.n_cyl, p.n_box, p.n_sph, p.n_obox, p.n_tri);
+  __syncthreads();
+  for (;;) {
+    if (threadIdx.x == 0) s_tile = atomicAdd(p.counter, 1);
+    __syncthreads();
+    const int tile = s_tile;
+    if (tile >= p.n_tiles) break;
+    render_tile_hard<SRC, MODE, HEX>(p, ob, htab, sh_hist, tile, tmask);
+  }
+}
+
 // FP64 accumulator -> FP32 output
 __global__ void __launch_bounds__(256) k_finish(const double* __restrict__ acc, float* __restrict__ out, size_t n) {
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
@@ -274,9 +306,9 @@ int resident_ctas(const void* kern, int block, size_t smem, int* per_sm) {
   return IACT_OK;
 }
 
-template <int SRC, bool SOFT, int MODE, bool STAGES>
-int run_render(RenderK p, int block, size_t smem, cudaStream_t st, void* const* ev) {
-  auto kern = k_render<SRC, SOFT, MODE, STAGES>;
+// one persistent launch of a render kernel: as many CTAs as are resident
+int run_persistent(void (*kern)(const RenderK), RenderK p, int block, size_t smem, cudaStream_t st,
+                   void* const* ev) {
   int per_sm = 0;
   int rc = resident_ctas(reinterpret_cast<const void*>(kern), block, smem, &per_sm);
   if (rc) return rc;
@@ -289,6 +321,30 @@ int run_render(RenderK p, int block, size_t smem, cudaStream_t st, void* const* 
   rc = check_cuda(cudaGetLastError(), "k_render launch");
   if (ev && ev[1]) cudaEventRecord(static_cast<cudaEvent_t>(ev[1]), st);
   return rc;
+}
+
+template <int SRC, bool SOFT, int MODE, bool STAGES>
+int run_render(RenderK p, int block, size_t smem, cudaStream_t st, void* const* ev) {
+  return run_persistent(k_render<SRC, SOFT, MODE, STAGES>, p, block, smem, st, ev);
+}
+
+// the common hard-pixel case (k_render_hard)
+int run_render_hard(int src_type, int mode, bool hex, RenderK p, int block, size_t smem, cudaStream_t st,
+                    void* const* ev) {
+  void (*kern)(const RenderK);
+  if (src_type == IACT_SRC_POINT) {
+    if (mode == IACT_MODE_RESPONSE)
+      kern = hex ? k_render_hard<IACT_SRC_POINT, IACT_MODE_RESPONSE, true> : k_render_hard<IACT_SRC_POINT, IACT_MODE_RESPONSE, false>;
+    else
+      kern = hex ? k_render_hard<IACT_SRC_POINT, IACT_MODE_IMAGE, true> : k_render_hard<IACT_SRC_POINT, IACT_MODE_IMAGE, false>;
+  } else {
+    if (mode == IACT_MODE_RESPONSE)
+      kern = hex ? k_render_hard<IACT_SRC_PARALLEL, IACT_MODE_RESPONSE, true>
+                 : k_render_hard<IACT_SRC_PARALLEL, IACT_MODE_RESPONSE, false>;
+    else
+      kern = hex ? k_render_hard<IACT_SRC_PARALLEL, IACT_MODE_IMAGE, true> : k_render_hard<IACT_SRC_PARALLEL, IACT_MODE_IMAGE, false>;
+  }
+  return run_persistent(kern, p, block, smem, st, ev);
 }
 
 template <int SRC, bool SOFT, int MODE>
@@ -453,7 +509,12 @@ int launch_render(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type,
   const bool stages = sc->n_mirrors > 0;
   void* const* ev = opts ? opts->kernel_events : nullptr;
   p.seed = opts ? opts->seed : 0u;
-  if (src_type == IACT_SRC_POINT) rc = dispatch_soft<IACT_SRC_POINT>(soft, mode, stages, p, block, smem, st, ev);
+  const bool hard_common = !soft && !stages && (src_type == IACT_SRC_POINT || src_type == IACT_SRC_PARALLEL) &&
+                           p.sn.axes && p.rows_in_smem > 0 &&
+                           (sn->type == IACT_SENSOR_SQUARE || (sn->type == IACT_SENSOR_HEX && p.hex_in_smem)) &&
+                           (p.n_words == 1 || n_primitives(sc) == 0);
+  if (hard_common) rc = run_render_hard(src_type, mode, sn->type == IACT_SENSOR_HEX, p, block, smem, st, ev);
+  else if (src_type == IACT_SRC_POINT) rc = dispatch_soft<IACT_SRC_POINT>(soft, mode, stages, p, block, smem, st, ev);
   else if (src_type == IACT_SRC_EXTENDED) rc = dispatch_soft<IACT_SRC_EXTENDED>(soft, mode, stages, p, block, smem, st, ev);
   else rc = dispatch_soft<IACT_SRC_PARALLEL>(soft, mode, stages, p, block, smem, st, ev);
   if (rc) return rc;

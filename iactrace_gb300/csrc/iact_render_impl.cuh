@@ -519,4 +519,161 @@ __device__ __forceinline__ void render_tile(const RenderK& p, const Obst& ob, co
 
 }
 
+// core/render.py:21-41 for one ray against the set bits of one 32-bit
+// candidate word (primitives 0..31 of the unified index space).
+__device__ __forceinline__ bool shadow_word(const Obst& ob, uint32_t m, V3 o, V3 d) {
+  bool sh = false;
+#pragma unroll 1
+  while (m) {
+    int k = __ffs(m) - 1;
+    m &= m - 1u;
+    if (k < ob.n_cyl) {
+      sh |= cyl_shadows(ob.cyl + k * kCylF, o, d);
+      continue;
+    }
+    k -= ob.n_cyl;
+    if (k < ob.n_box) {
+      sh |= box_shadows(ob.box + k * kBoxF, o, d);
+      continue;
+    }
+    k -= ob.n_box;
+    if (k < ob.n_sph) {
+      sh |= sph_shadows(ob.sph + k * kSphF, o, d);
+      continue;
+    }
+    k -= ob.n_sph;
+    if (k < ob.n_obox) {
+      sh |= obox_shadows(ob.obox + k * kOboxF, o, d);
+      continue;
+    }
+    k -= ob.n_obox;
+    sh |= tri_shadows(ob.tri + k * kTriF, o, d);
+  }
+  return sh;
+}
+
+// Hard-pixel tile body of the common case: a single-stage scene, point or
+// parallel sources, a sensor whose rotation is the identity, histogram rows
+// (and, for hexagons, the lookup table) in shared memory, and at most 32
+// shadowing primitives (one candidate word per (source, facet) pair; no
+// primitives at all also qualifies). It evaluates what render_tile<SRC,
+// false, MODE, false, true> does with the same floating-point operations in
+// the same order (core/render.py:118-157, sensors/square.py:66-91,
+// sensors/hexagonal.py:174-194), so every ray bins to the same pixel with
+// the same value. What differs is the control flow around them:
+//   * the sensor kind and the placement of the table and the rows are
+//     compile-time, not tested per ray;
+//   * source, value, candidate word and sample pointers are loaded once per
+//     (source, facet) pair, not per 32-ray task;
+//   * lanes past the last sample trace the facet's last sample with value 0
+//     instead of branching around the ray;
+//   * the run-length merge of the hits is selects plus one predicated
+//     shared-memory add, and the hexagon cell cache takes the full binning
+//     when any lane of the warp misses it (a warp vote), without a divergent
+//     branch.
+template <int SRC, int MODE, bool HEX>
+__device__ __forceinline__ void render_tile_hard(const RenderK& p, const Obst& ob, const short* htab,
+                                                 float* sh_hist, int tile, uint32_t* tmask) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5, nthr = blockDim.x;
+  const int nch = (p.M + 31) >> 5;
+  const int per_s = p.n_fchunk * p.n_cchunk;
+  const int sblk = tile / per_s;
+  const int fc = (tile - sblk * per_s) / p.n_cchunk;
+  const int cc = tile - sblk * per_s - fc * p.n_cchunk;
+  const int s0 = sblk * p.SB, f0 = fc * p.FC, c0 = cc * p.CC;
+  const int SBc = min(p.SB, p.S - s0), FCc = min(p.FC, p.F - f0), CCc = min(p.CC, nch - c0);
+
+  int rl_key = -1;  // run-length merged hit of this lane
+  float rl_val = 0.f;
+  HexCache hc = {3.0e38f, 3.0e38f, -1};  // last hexagon of this lane
+  const int T = SBc * FCc * CCc;
+  const int tb = (warp * T) / nw, te = ((warp + 1) * T) / nw;
+  if (p.n_words) warp_masks<SRC>(p.B4, p.sources, p.n_words, ob, s0, f0, FCc, CCc, tb, te, tmask);
+  // tasks t = (pair q = (source sl, facet fl), chunk cl), chunk fastest
+  int q = tb / CCc;
+  int sl = q / FCc, fl = q - sl * FCc;
+  int cl = tb - q * CCc;
+  const int mlast = p.M - 1;
+  for (int t = tb; t < te;) {
+    const int s = s0 + sl, f = f0 + fl;
+    const int ce = min(CCc, cl + (te - t));
+    t += ce - cl;
+    const V3 src = mk(__ldg(p.sources + 3 * s), __ldg(p.sources + 3 * s + 1), __ldg(p.sources + 3 * s + 2));
+    const float v = __ldg(p.values + s);
+    const uint32_t word = p.n_words ? tmask[q] : 0u;
+    const float4* P4f = p.P4 + (size_t)f * p.M;
+    const float4* N4f = p.N4 + (size_t)f * p.M;
+    const int rowbase = (MODE == IACT_MODE_RESPONSE) ? sl * p.P : 0;
+    for (; cl < ce; ++cl) {
+      const int m = (c0 + cl) * 32 + lane;
+      const bool act = m < p.M;
+      const int mi = act ? m : mlast;
+      const float4 P = __ldg(P4f + mi), N = __ldg(N4f + mi);
+      const V3 tp = mk(P.x, P.y, P.z), tn = mk(N.x, N.y, N.z);
+      V3 d;
+      if (SRC == IACT_SRC_POINT) {
+        V3 dd = tp - src;  // dirs = normalize(tp - src)
+        d = rsqrtf(dot(dd, dd)) * dd;
+      } else {
+        d = src;
+      }
+      bool sh = false;
+      if (word) sh = shadow_word(ob, word, tp, mk(-d.x, -d.y, -d.z));  // warp-uniform
+      const float c = dot(d, tn);                                       // core/reflection.py:5-20
+      const V3 r = d - (2.f * c) * tn;
+      float val = (v * -c * P.w) * (sh ? 0.f : 1.f);  // values * cos / tw * shadow
+      val = act ? val : 0.f;
+      float x, y;
+      plane_hit<true>(p.sn, tp, r, x, y);
+      int pix;
+      if (HEX) {
+        const float ex = x - hc.cx, ey = y - hc.cy;
+        const bool in = ex * ex + ey * ey < p.sn.hex_lim2;
+        pix = hc.pid;
+        if (__any_sync(kFull, !in)) {
+          float xg, yg, qi, ri;
+          hex_axial(p.sn, x, y, xg, yg, qi, ri);
+          const int pf = hex_lookup(p.sn, htab, qi, ri);
+          float hcx, hcy;
+          hex_centre(p.sn, qi, ri, hcx, hcy);
+          const float hd = hex_norm(__fsub_rn(xg, hcx), __fsub_rn(yg, hcy), p.sn.inv_inr);
+          // grid -> sensor frame: x - off_x = gc xg + gs yg, y - off_y = -gs xg + gc yg
+          const float ncx = p.sn.off_x + (p.sn.gc * hcx + p.sn.gs * hcy);
+          const float ncy = p.sn.off_y + (p.sn.gc * hcy - p.sn.gs * hcx);
+          hc.cx = in ? hc.cx : ncx;
+          hc.cy = in ? hc.cy : ncy;
+          hc.pid = in ? hc.pid : pf;
+          pix = in ? pix : ((hd > p.sn.edge_threshold) ? -1 : pf);
+        }
+      } else {
+        pix = bin_square(p.sn, x, y);
+      }
+      const bool dep = (pix >= 0) & (val != 0.f);
+      const int key = rowbase + pix;
+      const bool same = key == rl_key;
+      if (dep & !same & (rl_key >= 0)) atomicAdd(sh_hist + rl_key, rl_val);
+      rl_val = dep ? (same ? rl_val + val : val) : rl_val;
+      rl_key = dep ? key : rl_key;
+    }
+    cl = 0;
+    ++q;
+    if (++fl == FCc) {
+      fl = 0;
+      ++sl;
+    }
+  }
+  if (rl_key >= 0) atomicAdd(sh_hist + rl_key, rl_val);
+  __syncthreads();
+  // this tile's FP32 rows -> FP64 accumulator, then clear for the next tile
+  const int base = (MODE == IACT_MODE_RESPONSE) ? s0 : 0;
+  const int nrows = (MODE == IACT_MODE_RESPONSE) ? SBc : 1;
+  for (int i = threadIdx.x; i < nrows * p.P; i += nthr) {
+    const float h = sh_hist[i];
+    if (h != 0.f) {
+      atomicAdd(p.acc + (size_t)base * p.P + i, (double)h);
+      sh_hist[i] = 0.f;
+    }
+  }
+}
+
 }  // namespace iact
