@@ -31,6 +31,8 @@ struct WsLayout {
   size_t b4;       // float4 [F] facet bundle centre, radius (scenes with obstructions)
   size_t n_b4;     // entries of b4 (0: no obstructions, no culling)
   size_t acc;      // double: [rows * P] render accumulator, or the gradient buckets
+  size_t masks;    // uint32 [S * F] candidate word per (source, facet) pair (renders of <= 32 primitives)
+  size_t n_masks;  // entries of masks (0: none)
   size_t total;
   int n_table_floats;
 };
@@ -41,7 +43,10 @@ constexpr int kMirGrad = 22;    // per stage mirror: dL/dR (9), dL/dpos (3), dL/
 // stage re-traces the ray from the primary to that stage. The batched
 // adjoint takes scenes of at most kAdjRing later stages.
 constexpr int kAdjRing = 2;
-WsLayout workspace_layout(const iact_scene_t* sc, size_t acc_elems, bool with_delta);
+WsLayout workspace_layout(const iact_scene_t* sc, size_t acc_elems, bool with_delta, size_t mask_words = 0);
+// candidate words a forward render of S sources keeps per (source, facet)
+// pair: S * F for scenes of 1..32 shadowing primitives, else 0
+size_t pair_mask_words(const iact_scene_t* sc, int S);
 size_t acc_elems(const iact_sensor_t* sn, int S, int mode);  // 0 for DEBUG
 WsLayout workspace_for(const iact_scene_t* sc, const iact_sensor_t* sn, int S, int mode);
 

@@ -79,21 +79,37 @@ __global__ void __launch_bounds__(256, STAGES ? 3 : IACT_RENDER_MIN_CTAS) k_rend
   }
 }
 
+// Candidate word of every (source, facet) pair of a render (scenes of 1..32
+// primitives) for k_render_hard, after the prep launch wrote the facet
+// bounds and the tables.
+template <int SRC>
+__global__ void __launch_bounds__(256) k_masks(const RenderK p, uint32_t* out) {
+  extern __shared__ __align__(16) float smem[];
+  for (int i = threadIdx.x; i < p.n_table_floats; i += blockDim.x) smem[i] = p.tables[i];
+  __syncthreads();
+  const Obst ob = make_obst(smem, p.n_cyl, p.n_box, p.n_sph, p.n_obox, p.n_tri);
+  pair_masks<SRC>(p, ob, (long long)blockIdx.x * blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x, out);
+}
+
 // k_render for the common hard-pixel case (render_tile_hard): the host picks
 // it when the launch qualifies (single stage, point or parallel sources,
-// axis-aligned sensor, rows and hexagon table in shared memory, at most one
-// candidate word). Same shared-memory layout as k_render.
+// axis-aligned sensor, rows and hexagon table in shared memory, candidate
+// words per pair from k_masks). Shared memory: tables, hexagon table, rows.
+// A response tile flushes its rows; an image's one row is flushed every
+// p.flush_tiles tiles and when the CTA runs out of tiles, so small image
+// tiles (balance) cost no flush each.
 template <int SRC, int MODE, bool HEX>
 __global__ void __launch_bounds__(256, IACT_RENDER_MIN_CTAS) k_render_hard(const RenderK p) {
   extern __shared__ __align__(16) float smem[];
-  __shared__ int s_tile;
+  // tile index, double-buffered: an image tile ends without a barrier, so
+  // thread 0 may fetch the next index while a slow warp still reads this one
+  __shared__ int s_tile[2];
   const int tab_n = (p.n_table_floats + 3) & ~3;
   const int htab_n = HEX ? ((p.sn.table_q * p.sn.table_r + 7) & ~7) : 0;  // int16 entries
   float* tab = smem;
   short* htab = reinterpret_cast<short*>(smem + tab_n);
   float* sh_hist = smem + tab_n + htab_n / 2;
   const int hist_n = p.rows_in_smem * p.P;
-  uint32_t* tmask = reinterpret_cast<uint32_t*>(sh_hist + hist_n);
   const int nthr = blockDim.x;
 
   for (int i = threadIdx.x; i < p.n_table_floats; i += nthr) tab[i] = p.tables[i];
@@ -102,12 +118,16 @@ __global__ void __launch_bounds__(256, IACT_RENDER_MIN_CTAS) k_render_hard(const
   for (int i = threadIdx.x; i < hist_n; i += nthr) sh_hist[i] = 0.f;
   const Obst ob = make_obst(tab, p.n_cyl, p.n_box, p.n_sph, p.n_obox, p.n_tri);
   __syncthreads();
-  for (;;) {
-    if (threadIdx.x == 0) s_tile = atomicAdd(p.counter, 1);
+  for (int it = 0;; ++it) {  // it = tiles this CTA has rendered
+    if (threadIdx.x == 0) s_tile[it & 1] = atomicAdd(p.counter, 1);
     __syncthreads();
-    const int tile = s_tile;
+    const int tile = s_tile[it & 1];
+    if (MODE == IACT_MODE_IMAGE && it > 0 && (tile >= p.n_tiles || it % p.flush_tiles == 0)) {
+      flush_rows(p, sh_hist, 0, 1);
+      __syncthreads();
+    }
     if (tile >= p.n_tiles) break;
-    render_tile_hard<SRC, MODE, HEX>(p, ob, htab, sh_hist, tile, tmask);
+    render_tile_hard<SRC, MODE, HEX>(p, ob, htab, sh_hist, tile);
   }
 }
 
@@ -306,6 +326,22 @@ int resident_ctas(const void* kern, int block, size_t smem, int* per_sm) {
   return IACT_OK;
 }
 
+// candidate words of all (source, facet) pairs (k_masks), tables staged in
+// shared memory
+int launch_masks(int src_type, const RenderK& p, uint32_t* out, cudaStream_t st) {
+  const long long n = (long long)p.S * p.F;
+  if (n <= 0) return IACT_OK;
+  const size_t smem = sizeof(float) * (size_t)std::max(p.n_table_floats, 1);
+  void (*kern)(const RenderK, uint32_t*) =
+      src_type == IACT_SRC_POINT ? k_masks<IACT_SRC_POINT> : k_masks<IACT_SRC_PARALLEL>;
+  int per_sm = 0;
+  int rc = resident_ctas(reinterpret_cast<const void*>(kern), 256, smem, &per_sm);
+  if (rc) return rc;
+  const int grid = (int)std::min<long long>((n + 255) / 256, 65535);
+  kern<<<grid, 256, smem, st>>>(p, out);
+  return check_cuda(cudaGetLastError(), "k_masks launch");
+}
+
 // one persistent launch of a render kernel: as many CTAs as are resident
 int run_persistent(void (*kern)(const RenderK), RenderK p, int block, size_t smem, cudaStream_t st,
                    void* const* ev) {
@@ -364,7 +400,12 @@ int dispatch_soft(bool soft, int mode, bool stages, RenderK p, int block, size_t
               : dispatch_mode<SRC, false>(mode, stages, p, block, smem, st, ev);
 }
 
-WsLayout workspace_layout(const iact_scene_t* sc, size_t acc_elems, bool with_delta) {
+size_t pair_mask_words(const iact_scene_t* sc, int S) {
+  const int np = n_primitives(sc);
+  return (np > 0 && np <= 32) ? (size_t)std::max(S, 0) * (size_t)std::max(sc->n_facets, 0) : 0;
+}
+
+WsLayout workspace_layout(const iact_scene_t* sc, size_t acc_elems, bool with_delta, size_t mask_words) {
   WsLayout L;
   TableOffsets to = table_offsets(sc->n_cyl, sc->n_box, sc->n_sph, sc->n_obox, sc->n_tri, sc->n_mirrors);
   L.n_table_floats = to.total;
@@ -385,6 +426,9 @@ WsLayout workspace_layout(const iact_scene_t* sc, size_t acc_elems, bool with_de
   off = align256(off + sizeof(float4) * L.n_b4);
   L.acc = off;
   off = align256(off + sizeof(double) * acc_elems);
+  L.masks = off;
+  L.n_masks = mask_words;
+  off = align256(off + sizeof(uint32_t) * mask_words);
   L.total = off;
   return L;
 }
@@ -399,7 +443,7 @@ WsLayout workspace_for(const iact_scene_t* sc, const iact_sensor_t* sn, int S, i
   if (mode == IACT_MODE_BACKWARD)
     return workspace_layout(sc, (size_t)std::max(sc->n_facets, 0) * kFacetGrad + (size_t)std::max(S, 0) * 4 +
                                     (size_t)std::max(sc->n_mirrors, 0) * kMirGrad, true);
-  return workspace_layout(sc, acc_elems(sn, S, mode), false);
+  return workspace_layout(sc, acc_elems(sn, S, mode), false, pair_mask_words(sc, S));
 }
 
 int plan_tiles(RenderK& p, int mode, int block, const iact_opts_t* opts, long long min_tiles) {
@@ -468,7 +512,7 @@ int launch_render(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type,
                   const iact_opts_t* opts, cudaStream_t st) {
   (void)ws_bytes;
   const size_t n_acc = acc_elems(sn, S, mode);
-  const WsLayout L = workspace_layout(sc, n_acc, false);
+  const WsLayout L = workspace_layout(sc, n_acc, false, pair_mask_words(sc, S));
   char* w = static_cast<char*>(ws);
   int rc;
   if (S == 0 || sc->n_facets == 0 || sc->n_samples == 0) {
@@ -493,30 +537,62 @@ int launch_render(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type,
   // balance (measured: 1000-sample plain forward 7 % faster at 4 than at 8
   // per SM, the Cassegrain forward 13 % slower; 276-primitive scene 320 us
   // at 5 tiles per SM, 256 us at 10)
-  const long long tiles_per_sm = sc->n_mirrors > 0 ? 8 : (n_primitives(sc) > 32 ? 10 : 4);
-  rc = plan_tiles(p, mode, block, opts, tiles_per_sm * std::max(di.sm_count, 1));
-  if (rc) return rc;
-  const size_t mask_bytes = sizeof(uint32_t) * (size_t)p.n_words * p.SB * p.FC;
-  const size_t budget = (size_t)std::min(di.smem_optin > 0 ? di.smem_optin : 49152, 200 * 1024) - mask_bytes;
-  SmemPlan sp;
-  rc = plan_smem(sn, L.n_table_floats, p.SB, mode, opts ? opts->hist_mode : 0, budget, 0, 0, sp);
-  if (rc) return rc;
-  p.hex_in_smem = sp.hex_in_smem;
-  p.rows_in_smem = sp.rows_in_smem;
-  const size_t smem = sp.tab_bytes + sp.htab_bytes + sp.hist_bytes + mask_bytes;
-
   const bool soft = (sn->type == IACT_SENSOR_SOFT_SQUARE || sn->type == IACT_SENSOR_SOFT_HEX);
   const bool stages = sc->n_mirrors > 0;
+  // the common hard-pixel case runs k_render_hard, with the candidate word of
+  // every (source, facet) pair from k_masks
+  const bool hard = !soft && !stages && (src_type == IACT_SRC_POINT || src_type == IACT_SRC_PARALLEL) &&
+                    p.sn.axes && (sn->type == IACT_SENSOR_SQUARE || sn->type == IACT_SENSOR_HEX) &&
+                    (p.n_words == 1 || n_primitives(sc) == 0) && !(opts && opts->hist_mode == 2);
+  // image renders of k_render_hard keep their FP32 row across tiles and need
+  // no masks per tile, so their tiles are smaller (balance at the end of a
+  // launch: 1000-sample plain forward 51.5 us at 12 tiles per SM vs 57.4 at
+  // 16 and 56.2 at 4)
+  const long long tiles_per_sm =
+      (hard && mode == IACT_MODE_IMAGE) ? 12 : (sc->n_mirrors > 0 ? 8 : (n_primitives(sc) > 32 ? 10 : 4));
+  rc = plan_tiles(p, mode, block, opts, tiles_per_sm * std::max(di.sm_count, 1));
+  if (rc) return rc;
+  const size_t smem_max = (size_t)std::min(di.smem_optin > 0 ? di.smem_optin : 49152, 200 * 1024);
+  SmemPlan sp;
+  bool use_hard = false;
+  size_t smem = 0;
+  if (hard) {
+    rc = plan_smem(sn, L.n_table_floats, p.SB, mode, opts ? opts->hist_mode : 0, smem_max, 0, 0, sp);
+    if (rc) return rc;
+    use_hard = sp.rows_in_smem > 0 && (sn->type == IACT_SENSOR_SQUARE || sp.hex_in_smem);
+    smem = sp.tab_bytes + sp.htab_bytes + sp.hist_bytes;
+  }
+  if (!use_hard) {  // k_render: candidate masks of a tile's tasks in shared memory
+    const size_t mask_bytes = sizeof(uint32_t) * (size_t)p.n_words * p.SB * p.FC;
+    rc = plan_smem(sn, L.n_table_floats, p.SB, mode, opts ? opts->hist_mode : 0, smem_max - mask_bytes, 0, 0, sp);
+    if (rc) return rc;
+    smem = sp.tab_bytes + sp.htab_bytes + sp.hist_bytes + mask_bytes;
+  }
+  p.hex_in_smem = sp.hex_in_smem;
+  p.rows_in_smem = sp.rows_in_smem;
+
   void* const* ev = opts ? opts->kernel_events : nullptr;
   p.seed = opts ? opts->seed : 0u;
-  const bool hard_common = !soft && !stages && (src_type == IACT_SRC_POINT || src_type == IACT_SRC_PARALLEL) &&
-                           p.sn.axes && p.rows_in_smem > 0 &&
-                           (sn->type == IACT_SENSOR_SQUARE || (sn->type == IACT_SENSOR_HEX && p.hex_in_smem)) &&
-                           (p.n_words == 1 || n_primitives(sc) == 0);
-  if (hard_common) rc = run_render_hard(src_type, mode, sn->type == IACT_SENSOR_HEX, p, block, smem, st, ev);
-  else if (src_type == IACT_SRC_POINT) rc = dispatch_soft<IACT_SRC_POINT>(soft, mode, stages, p, block, smem, st, ev);
-  else if (src_type == IACT_SRC_EXTENDED) rc = dispatch_soft<IACT_SRC_EXTENDED>(soft, mode, stages, p, block, smem, st, ev);
-  else rc = dispatch_soft<IACT_SRC_PARALLEL>(soft, mode, stages, p, block, smem, st, ev);
+  if (use_hard) {
+    // the kernel events (profiling) bracket the masks and the render
+    if (ev && ev[0]) cudaEventRecord(static_cast<cudaEvent_t>(ev[0]), st);
+    if (p.n_words) {
+      p.gmask = reinterpret_cast<const uint32_t*>(w + L.masks);
+      rc = launch_masks(src_type, p, reinterpret_cast<uint32_t*>(w + L.masks), st);
+      if (rc) return rc;
+    }
+    // an image row sums about 16k rays between flushes to the FP64 accumulator
+    const int tile_tasks = p.SB * p.FC * p.CC;
+    p.flush_tiles = std::max(1, 512 / std::max(tile_tasks, 1));
+    void* const ev_end[2] = {nullptr, ev ? ev[1] : nullptr};
+    rc = run_render_hard(src_type, mode, sn->type == IACT_SENSOR_HEX, p, block, smem, st, ev_end);
+  } else if (src_type == IACT_SRC_POINT) {
+    rc = dispatch_soft<IACT_SRC_POINT>(soft, mode, stages, p, block, smem, st, ev);
+  } else if (src_type == IACT_SRC_EXTENDED) {
+    rc = dispatch_soft<IACT_SRC_EXTENDED>(soft, mode, stages, p, block, smem, st, ev);
+  } else {
+    rc = dispatch_soft<IACT_SRC_PARALLEL>(soft, mode, stages, p, block, smem, st, ev);
+  }
   if (rc) return rc;
   const int fb = (int)std::min<size_t>((n_acc + 255) / 256, 4096);
   k_finish<<<std::max(fb, 1), 256, 0, st>>>(p.acc, out, n_acc);

@@ -192,6 +192,8 @@ struct RenderK {
   uint32_t seed;  // jitter stream of extended sources
   const float4* B4;  // per facet bundle bounds (culling on)
   int n_words;       // 32-bit candidate-mask words per task; 0 = no culling
+  const uint32_t* gmask;  // k_render_hard: candidate word per (source, facet) pair [S * F], or null (no primitives)
+  int flush_tiles;        // k_render_hard, IMAGE mode: tiles between flushes of the FP32 row
 };
 
 // Where hits go: FP32 shared-memory rows of the current tile, or the FP64
@@ -395,6 +397,25 @@ __device__ __forceinline__ void bundle_axis(V3 src, float sigma, V3 c, float R0,
 // mask[t * nw + w]. One lane per (task, 32-primitive word): the task's
 // bundle is decoded once and its word assembled in a register; no
 // CTA-wide barrier (each warp reads only its own tasks' masks).
+// Candidate word w (primitives 32w..32w+31) of the pair (source s, facet f).
+template <int SRC>
+__device__ __forceinline__ uint32_t mask_word(const float4* B4, const float* sources, const Obst& ob, int s, int f,
+                                              int w) {
+  const int np = ob.n_cyl + ob.n_box + ob.n_sph + ob.n_obox + ob.n_tri;
+  constexpr int SS = (SRC == IACT_SRC_EXTENDED) ? 4 : 3;
+  const float4 B = __ldg(B4 + f);
+  Bundle bd;
+  bd.c = mk(B.x, B.y, B.z);
+  bd.R0 = B.w;
+  const V3 src = mk(__ldg(sources + SS * s), __ldg(sources + SS * s + 1), __ldg(sources + SS * s + 2));
+  bundle_axis<SRC>(src, SRC == IACT_SRC_EXTENDED ? __ldg(sources + SS * s + 3) : 0.f, bd.c, bd.R0, bd.u, bd.dlt);
+  uint32_t word = 0u;
+  const int k1 = min(np, 32 * w + 32);
+  for (int k = 32 * w; k < k1; ++k)
+    if (prim_may_hit(ob, k, bd)) word |= 1u << (k & 31);
+  return word;
+}
+
 template <int SRC>
 // Candidate masks of the (source, facet) pairs of this warp's tasks
 // [tb, te) (tasks are ordered (source, facet, chunk): a pair's CCc chunk
@@ -404,24 +425,11 @@ template <int SRC>
 // writes the same words.
 __device__ __forceinline__ void warp_masks(const float4* B4, const float* sources, int nw, const Obst& ob,
                                            int s0, int f0, int FCc, int CCc, int tb, int te, uint32_t* mask) {
-  const int np = ob.n_cyl + ob.n_box + ob.n_sph + ob.n_obox + ob.n_tri;
-  constexpr int SS = (SRC == IACT_SRC_EXTENDED) ? 4 : 3;
   const int pb = tb / CCc, pe = (te + CCc - 1) / CCc;
   for (int i = pb * nw + (threadIdx.x & 31); i < pe * nw; i += 32) {
     const int q = i / nw, w = i - q * nw;
     const int sl = q / FCc, fl = q - sl * FCc;
-    const int s = s0 + sl;
-    const float4 B = __ldg(B4 + f0 + fl);
-    Bundle bd;
-    bd.c = mk(B.x, B.y, B.z);
-    bd.R0 = B.w;
-    const V3 src = mk(__ldg(sources + SS * s), __ldg(sources + SS * s + 1), __ldg(sources + SS * s + 2));
-    bundle_axis<SRC>(src, SRC == IACT_SRC_EXTENDED ? __ldg(sources + SS * s + 3) : 0.f, bd.c, bd.R0, bd.u, bd.dlt);
-    uint32_t word = 0u;
-    const int k1 = min(np, 32 * w + 32);
-    for (int k = 32 * w; k < k1; ++k)
-      if (prim_may_hit(ob, k, bd)) word |= 1u << (k & 31);
-    mask[i] = word;
+    mask[i] = mask_word<SRC>(B4, sources, ob, s0 + sl, f0 + fl, w);
   }
   __syncwarp();
 }
@@ -519,6 +527,31 @@ __device__ __forceinline__ void render_tile(const RenderK& p, const Obst& ob, co
 
 }
 
+// FP32 shared-memory rows [nrows, P] -> FP64 accumulator rows from `base`,
+// then cleared (all threads of the CTA, after a barrier).
+__device__ __forceinline__ void flush_rows(const RenderK& p, float* sh_hist, int base, int nrows) {
+  for (int i = threadIdx.x; i < nrows * p.P; i += blockDim.x) {
+    const float h = sh_hist[i];
+    if (h != 0.f) {
+      atomicAdd(p.acc + (size_t)base * p.P + i, (double)h);
+      sh_hist[i] = 0.f;
+    }
+  }
+}
+
+// Candidate words of the (source, facet) pairs i of a render [S * F], one
+// thread per pair (the scene has at most 32 primitives): the bundle test of
+// warp_masks, once per pair for the whole launch.
+template <int SRC>
+__device__ __forceinline__ void pair_masks(const RenderK& p, const Obst& ob, long long i0, long long stride,
+                                           uint32_t* out) {
+  const long long n = (long long)p.S * p.F;
+  for (long long i = i0; i < n; i += stride) {
+    const int s = (int)(i / p.F), f = (int)(i - (long long)s * p.F);
+    out[i] = mask_word<SRC>(p.B4, p.sources, ob, s, f, 0);
+  }
+}
+
 // core/render.py:21-41 for one ray against the set bits of one 32-bit
 // candidate word (primitives 0..31 of the unified index space).
 __device__ __forceinline__ bool shadow_word(const Obst& ob, uint32_t m, V3 o, V3 d) {
@@ -567,14 +600,14 @@ __device__ __forceinline__ bool shadow_word(const Obst& ob, uint32_t m, V3 o, V3
 //     (source, facet) pair, not per 32-ray task;
 //   * lanes past the last sample trace the facet's last sample with value 0
 //     instead of branching around the ray;
-//   * the run-length merge of the hits is selects plus one predicated
-//     shared-memory add, and the hexagon cell cache takes the full binning
+//   * the run-length merge of the hits keeps two keys per lane and is
+//     selects plus one predicated shared-memory add, and the hexagon cell cache takes the full binning
 //     when any lane of the warp misses it (a warp vote), without a divergent
 //     branch.
 template <int SRC, int MODE, bool HEX>
 __device__ __forceinline__ void render_tile_hard(const RenderK& p, const Obst& ob, const short* htab,
-                                                 float* sh_hist, int tile, uint32_t* tmask) {
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5, nthr = blockDim.x;
+                                                 float* sh_hist, int tile) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   const int nch = (p.M + 31) >> 5;
   const int per_s = p.n_fchunk * p.n_cchunk;
   const int sblk = tile / per_s;
@@ -583,12 +616,14 @@ __device__ __forceinline__ void render_tile_hard(const RenderK& p, const Obst& o
   const int s0 = sblk * p.SB, f0 = fc * p.FC, c0 = cc * p.CC;
   const int SBc = min(p.SB, p.S - s0), FCc = min(p.FC, p.F - f0), CCc = min(p.CC, nch - c0);
 
-  int rl_key = -1;  // run-length merged hit of this lane
-  float rl_val = 0.f;
+  // run-length merged hits of this lane: two (key, value) slots, slot 0 the
+  // newest key; a third key flushes slot 1 (a lane whose rays alternate
+  // between two pixels adds nothing until a third appears)
+  int rl_key = -1, rk1 = -1;
+  float rl_val = 0.f, rv1 = 0.f;
   HexCache hc = {3.0e38f, 3.0e38f, -1};  // last hexagon of this lane
   const int T = SBc * FCc * CCc;
   const int tb = (warp * T) / nw, te = ((warp + 1) * T) / nw;
-  if (p.n_words) warp_masks<SRC>(p.B4, p.sources, p.n_words, ob, s0, f0, FCc, CCc, tb, te, tmask);
   // tasks t = (pair q = (source sl, facet fl), chunk cl), chunk fastest
   int q = tb / CCc;
   int sl = q / FCc, fl = q - sl * FCc;
@@ -600,15 +635,14 @@ __device__ __forceinline__ void render_tile_hard(const RenderK& p, const Obst& o
     t += ce - cl;
     const V3 src = mk(__ldg(p.sources + 3 * s), __ldg(p.sources + 3 * s + 1), __ldg(p.sources + 3 * s + 2));
     const float v = __ldg(p.values + s);
-    const uint32_t word = p.n_words ? tmask[q] : 0u;
-    const float4* P4f = p.P4 + (size_t)f * p.M;
-    const float4* N4f = p.N4 + (size_t)f * p.M;
+    const uint32_t word = p.gmask ? __ldg(p.gmask + (size_t)s * p.F + f) : 0u;  // pair's candidates (k_masks)
+    const int fbase = f * p.M;  // first sample of the facet (F * M < 2^30)
     const int rowbase = (MODE == IACT_MODE_RESPONSE) ? sl * p.P : 0;
     for (; cl < ce; ++cl) {
       const int m = (c0 + cl) * 32 + lane;
       const bool act = m < p.M;
-      const int mi = act ? m : mlast;
-      const float4 P = __ldg(P4f + mi), N = __ldg(N4f + mi);
+      const int mi = fbase + (act ? m : mlast);
+      const float4 P = __ldg(p.P4 + mi), N = __ldg(p.N4 + mi);
       const V3 tp = mk(P.x, P.y, P.z), tn = mk(N.x, N.y, N.z);
       V3 d;
       if (SRC == IACT_SRC_POINT) {
@@ -650,10 +684,15 @@ __device__ __forceinline__ void render_tile_hard(const RenderK& p, const Obst& o
       }
       const bool dep = (pix >= 0) & (val != 0.f);
       const int key = rowbase + pix;
-      const bool same = key == rl_key;
-      if (dep & !same & (rl_key >= 0)) atomicAdd(sh_hist + rl_key, rl_val);
-      rl_val = dep ? (same ? rl_val + val : val) : rl_val;
-      rl_key = dep ? key : rl_key;
+      const bool in0 = key == rl_key, in1 = key == rk1;
+      const bool nk = dep & !in0 & !in1;
+      if (nk & (rk1 >= 0)) atomicAdd(sh_hist + rk1, rv1);
+      rl_val = (dep & in0) ? rl_val + val : rl_val;
+      rv1 = (dep & in1) ? rv1 + val : rv1;
+      rk1 = nk ? rl_key : rk1;
+      rv1 = nk ? rl_val : rv1;
+      rl_key = nk ? key : rl_key;
+      rl_val = nk ? val : rl_val;
     }
     cl = 0;
     ++q;
@@ -663,16 +702,11 @@ __device__ __forceinline__ void render_tile_hard(const RenderK& p, const Obst& o
     }
   }
   if (rl_key >= 0) atomicAdd(sh_hist + rl_key, rl_val);
-  __syncthreads();
-  // this tile's FP32 rows -> FP64 accumulator, then clear for the next tile
-  const int base = (MODE == IACT_MODE_RESPONSE) ? s0 : 0;
-  const int nrows = (MODE == IACT_MODE_RESPONSE) ? SBc : 1;
-  for (int i = threadIdx.x; i < nrows * p.P; i += nthr) {
-    const float h = sh_hist[i];
-    if (h != 0.f) {
-      atomicAdd(p.acc + (size_t)base * p.P + i, (double)h);
-      sh_hist[i] = 0.f;
-    }
+  if (rk1 >= 0) atomicAdd(sh_hist + rk1, rv1);
+  if (MODE == IACT_MODE_RESPONSE) {
+    // this tile's FP32 rows -> FP64 accumulator, then clear for the next tile
+    __syncthreads();
+    flush_rows(p, sh_hist, s0, SBc);
   }
 }
 

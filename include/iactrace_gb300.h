@@ -151,11 +151,15 @@ typedef struct {
   int32_t hist_mode;        /* 0 auto, 1 shared-memory rows, 2 global     */
   int32_t tasks_per_warp;   /* 32-ray tasks per warp per work tile (0: 192 for
                                hard-pixel RESPONSE renders and RESPONSE
-                               adjoints, else 48)                        */
+                               adjoints, else 48, halved for small launches
+                               down to 4 tiles per SM, 12 for hard-pixel
+                               IMAGE renders of at most 32 primitives)   */
   int32_t flags;            /* IACT_FLAG_* bits                           */
   uint32_t seed;            /* jitter stream of EXTENDED sources            */
   /* optional cudaEvent_t pair recorded on `stream` right before and after
-   * the render kernel (profiling); NULL to skip */
+   * the render kernel (profiling; for hard-pixel renders of at most 32
+   * primitives the window also holds the candidate-mask launch before it);
+   * NULL to skip */
   void* kernel_events[2];
 } iact_opts_t;
 
