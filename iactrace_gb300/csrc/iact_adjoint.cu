@@ -69,6 +69,32 @@ __global__ void __launch_bounds__(256, STAGES ? 2 : (SOFT ? 3 : 4)) k_adjoint(co
   }
 }
 
+// k_adjoint for the common hard-pixel case (adjoint_tile_hard): the host
+// picks it when the backward qualifies. Shared memory: tables and hexagon
+// table. Tiles end without a barrier, so the tile index is double-buffered.
+template <int SRC, int MODE, bool HEX>
+__global__ void __launch_bounds__(256, 4) k_adjoint_hard(const AdjK p) {
+  extern __shared__ __align__(16) float smem[];
+  __shared__ int s_tile[2];
+  const int tab_n = (p.n_table_floats + 3) & ~3;
+  const int htab_n = HEX ? ((p.sn.table_q * p.sn.table_r + 7) & ~7) : 0;
+  float* tab = smem;
+  short* htab = reinterpret_cast<short*>(smem + tab_n);
+  const int nthr = blockDim.x;
+  for (int i = threadIdx.x; i < p.n_table_floats; i += nthr) tab[i] = p.tables[i];
+  for (int i = threadIdx.x; i < htab_n; i += nthr)
+    htab[i] = (short)(i < p.sn.table_q * p.sn.table_r ? p.hex_table[i] : -1);
+  const Obst ob = make_obst(tab, p.n_cyl, p.n_box, p.n_sph, p.n_obox, p.n_tri);
+  __syncthreads();
+  for (int it = 0;; ++it) {
+    if (threadIdx.x == 0) s_tile[it & 1] = atomicAdd(p.counter, 1);
+    __syncthreads();
+    const int tile = s_tile[it & 1];
+    if (tile >= p.n_tiles) break;
+    adjoint_tile_hard<SRC, MODE, HEX>(p, ob, htab, tile);
+  }
+}
+
 __global__ void k_adjoint_mirrors(const double* gmir, const iact_mirror_t* mirrors, int n_mir, float* g_rot,
                                   float* g_pos, float* g_surf) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -111,6 +137,44 @@ int adj_stages(int n_stages, int mode, const AdjK& p, int block, size_t smem, cu
   if (n_stages > kAdjRing) return adj_mode<SRC, SOFT, true, true>(mode, p, block, smem, st);
   return n_stages > 0 ? adj_mode<SRC, SOFT, true>(mode, p, block, smem, st)
                       : adj_mode<SRC, SOFT, false>(mode, p, block, smem, st);
+}
+
+// the common hard-pixel case (k_adjoint_hard)
+int run_adjoint_hard(int src_type, int mode, bool hex, const AdjK& p, int block, size_t smem, cudaStream_t st) {
+  void (*kern)(const AdjK);
+  if (src_type == IACT_SRC_POINT) {
+    if (mode == IACT_MODE_RESPONSE)
+      kern = hex ? k_adjoint_hard<IACT_SRC_POINT, IACT_MODE_RESPONSE, true> : k_adjoint_hard<IACT_SRC_POINT, IACT_MODE_RESPONSE, false>;
+    else
+      kern = hex ? k_adjoint_hard<IACT_SRC_POINT, IACT_MODE_IMAGE, true> : k_adjoint_hard<IACT_SRC_POINT, IACT_MODE_IMAGE, false>;
+  } else {
+    if (mode == IACT_MODE_RESPONSE)
+      kern = hex ? k_adjoint_hard<IACT_SRC_PARALLEL, IACT_MODE_RESPONSE, true>
+                 : k_adjoint_hard<IACT_SRC_PARALLEL, IACT_MODE_RESPONSE, false>;
+    else
+      kern = hex ? k_adjoint_hard<IACT_SRC_PARALLEL, IACT_MODE_IMAGE, true>
+                 : k_adjoint_hard<IACT_SRC_PARALLEL, IACT_MODE_IMAGE, false>;
+  }
+  int per_sm = 0;
+  const int rc = resident_ctas(reinterpret_cast<const void*>(kern), block, smem, &per_sm);
+  if (rc) return rc;
+  if (per_sm < 1) return set_error(IACT_E_UNSUPPORTED, "adjoint kernel does not fit on an SM");
+  const int grid = std::max(1, std::min(p.n_tiles, per_sm * device_info().sm_count));
+  kern<<<grid, block, smem, st>>>(p);
+  return check_cuda(cudaGetLastError(), "k_adjoint launch");
+}
+
+// the render parameters k_masks reads, from the adjoint's
+RenderK mask_params(const AdjK& a) {
+  RenderK r;
+  memset(&r, 0, sizeof(r));
+  r.S = a.S; r.F = a.F; r.M = a.M; r.P = a.P;
+  r.sources = a.sources; r.values = a.values;
+  r.tables = a.tables; r.n_table_floats = a.n_table_floats;
+  r.n_cyl = a.n_cyl; r.n_box = a.n_box; r.n_sph = a.n_sph; r.n_obox = a.n_obox; r.n_tri = a.n_tri;
+  r.B4 = a.B4;
+  r.n_words = a.n_words;
+  return r;
 }
 
 }  // namespace
@@ -217,7 +281,24 @@ int launch_backward(const iact_scene_t* sc, const iact_sensor_t* sn, int src_typ
     void* const* ev = opts ? opts->kernel_events : nullptr;
     if (ev && ev[0]) cudaEventRecord(static_cast<cudaEvent_t>(ev[0]), st);
     const int stages = n_mir > 0 ? std::max(sc->n_stages, 1) : 0;
-    if (src_type == IACT_SRC_POINT)
+    // the common hard-pixel case: k_adjoint_hard with the candidate word of
+    // every (source, facet) pair from k_masks (inside the kernel events)
+    const bool hard = !soft && n_mir == 0 && (src_type == IACT_SRC_POINT || src_type == IACT_SRC_PARALLEL) &&
+                      p.sn.axes && !g_scale && !g_samples &&
+                      (sn->type == IACT_SENSOR_SQUARE || (sn->type == IACT_SENSOR_HEX && p.hex_in_smem)) &&
+                      ((p.n_words == 1 && L.n_masks > 0) || n_primitives(sc) == 0);
+    if (hard) {
+      if (p.n_words) {
+        p.gmask = reinterpret_cast<const uint32_t*>(w + L.masks);
+        rc = launch_masks(src_type, mask_params(p), reinterpret_cast<uint32_t*>(w + L.masks), st);
+        if (rc) return rc;
+      }
+      const size_t hsmem = sizeof(float) * (size_t)((p.n_table_floats + 3) & ~3) +
+                           (sn->type == IACT_SENSOR_HEX
+                                ? sizeof(short) * (((size_t)sn->table_q * sn->table_r + 7) & ~(size_t)7)
+                                : 0);
+      rc = run_adjoint_hard(src_type, mode, sn->type == IACT_SENSOR_HEX, p, block, hsmem, st);
+    } else if (src_type == IACT_SRC_POINT)
       rc = soft ? adj_stages<IACT_SRC_POINT, true>(stages, mode, p, block, smem, st)
                 : adj_stages<IACT_SRC_POINT, false>(stages, mode, p, block, smem, st);
     else if (src_type == IACT_SRC_EXTENDED)

@@ -35,6 +35,7 @@ struct AdjK {
   int n_words;       // 32-bit candidate-mask words per task; 0 = no culling
   float* gsamp;      // optional [F*M, 7]: per sample dL/d(world point, perturbed normal, 1/weight)
   int want_mgrad;    // stage-mirror parameter gradients requested (gmir)
+  const uint32_t* gmask;  // k_adjoint_hard: candidate word per (source, facet) pair [S * F], or null
 };
 
 // Per-lane running sums of one (facet, source) stream of rays.
@@ -591,6 +592,159 @@ __device__ __forceinline__ void adjoint_tile(const AdjK& p, const Obst& ob, cons
   // warp-uniform: every lane ran the same task range
   if (cur_f >= 0) flush_facet(acc, p.gfacet, cur_f);
   if (cur_s >= 0) flush_src(acc, p.gsrc, cur_s);
+}
+
+// flush_facet without the roughness-scale sum (hard-pixel adjoint, no D4)
+__device__ __forceinline__ void flush_facet_hard(Acc& a, double* gfacet, int f) {
+  double* dst = gfacet + (size_t)f * kFacetGrad;
+  float v[12];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) v[i] = a.H[i];
+  v[9] = a.gp[0]; v[10] = a.gp[1]; v[11] = a.gp[2];
+#pragma unroll
+  for (int i = 0; i < 12; ++i) {
+    const float t = warp_sum(v[i]);
+    if ((threadIdx.x & 31) == 0 && t != 0.f) atomicAdd(dst + i, (double)t);
+  }
+#pragma unroll
+  for (int i = 0; i < 9; ++i) a.H[i] = 0.f;
+  a.gp[0] = a.gp[1] = a.gp[2] = 0.f;
+}
+
+// Hard-pixel adjoint tile of the common case: a single-stage scene, point or
+// parallel sources, a sensor whose rotation is the identity, the hexagon
+// table in shared memory, candidate words per (source, facet) pair from
+// k_masks, and no roughness-scale or per-sample gradients. The arithmetic is
+// adjoint_tile<SRC, false, MODE, false, true>'s (pixel ids are constants, so
+// only the value path carries gradient back to the reflection and the
+// direction); the sensor kind and table placement are compile-time, lanes
+// past the last sample run the facet's last sample with no contribution,
+// per-pair values are loaded once per pair, and a warp's tasks run facet by
+// facet (source next, chunk fastest): the per-source sums (4 values) are
+// reduced at every pair change and the per-facet sums (13 values) only when
+// the facet changes.
+template <int SRC, int MODE, bool HEX>
+__device__ __forceinline__ void adjoint_tile_hard(const AdjK& p, const Obst& ob, const short* htab, int tile) {
+  const SensorK& sn = p.sn;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  const int nch = (p.M + 31) >> 5;
+  Acc acc;
+  acc_zero_facet(acc);
+  acc_zero_src(acc);
+  const int per_s = p.n_fchunk * p.n_cchunk;
+  const int sblk = tile / per_s;
+  const int fc = (tile - sblk * per_s) / p.n_cchunk;
+  const int cc = tile - sblk * per_s - fc * p.n_cchunk;
+  const int s0 = sblk * p.SB, f0 = fc * p.FC, c0 = cc * p.CC;
+  const int SBc = min(p.SB, p.S - s0), FCc = min(p.FC, p.F - f0), CCc = min(p.CC, nch - c0);
+  const int T = SBc * FCc * CCc;
+  const int tb = (warp * T) / nw, te = ((warp + 1) * T) / nw;
+  // tasks t = (facet fl, source sl, chunk cl), chunk fastest
+  int q = tb / CCc;  // pair index fl * SBc + sl
+  int fl = q / SBc, sl = q - fl * SBc;
+  int cl = tb - q * CCc;
+  int cur_f = -1;
+  HexCache hc = {3.0e38f, 3.0e38f, -1};  // last hexagon of this lane
+  const int mlast = p.M - 1;
+  for (int t = tb; t < te;) {
+    const int s = s0 + sl, f = f0 + fl;
+    const int ce = min(CCc, cl + (te - t));
+    t += ce - cl;
+    if (f != cur_f) {
+      if (cur_f >= 0) flush_facet_hard(acc, p.gfacet, cur_f);
+      cur_f = f;
+    }
+    const V3 src = mk(__ldg(p.sources + 3 * s), __ldg(p.sources + 3 * s + 1), __ldg(p.sources + 3 * s + 2));
+    const float v = __ldg(p.values + s);
+    const V3 fpos = mk(__ldg(p.facet_pos + 3 * f), __ldg(p.facet_pos + 3 * f + 1), __ldg(p.facet_pos + 3 * f + 2));
+    const uint32_t word = p.gmask ? __ldg(p.gmask + (size_t)s * p.F + f) : 0u;
+    const int rowbase = (MODE == IACT_MODE_RESPONSE) ? s * p.P : 0;
+    const int fbase = f * p.M;
+    for (; cl < ce; ++cl) {
+      const int m = (c0 + cl) * 32 + lane;
+      const bool ok = m < p.M;
+      const int si = fbase + (ok ? m : mlast);
+      const float4 P4 = __ldg(p.P4 + si), N4 = __ldg(p.N4 + si);
+      const V3 tp = mk(P4.x, P4.y, P4.z), nn = mk(N4.x, N4.y, N4.z);
+      const float iw = P4.w;
+      // ---- forward re-trace
+      V3 d, w;
+      float inv_len = 0.f;
+      if (SRC == IACT_SRC_POINT) {
+        w = tp - src;
+        inv_len = rsqrtf(dot(w, w));
+        d = inv_len * w;
+      } else {
+        d = src;
+      }
+      bool shadowed = false;
+      if (word) shadowed = shadow_word(ob, word, tp, mk(-d.x, -d.y, -d.z));  // warp-uniform
+      const float c = dot(d, nn);
+      const V3 r = d - (2.f * c) * nn;
+      const float ndotd = r.z;
+      const bool parallel = fabsf(ndotd) < 1e-10f;
+      const float inv_nd = rcp_a(parallel ? 1.f : ndotd);
+      const float tpl = (sn.pos[2] - tp.z) * inv_nd;
+      const bool hit_plane = !parallel && (tpl > 0.f);
+      const float x = hit_plane ? (tp.x + tpl * r.x) - sn.pos[0] : kBig;
+      const float y = hit_plane ? (tp.y + tpl * r.y) - sn.pos[1] : kBig;
+      // ---- reverse of the deposit: d img[pix] / d val = 1
+      int pix;
+      if (HEX) {
+        const float ex = x - hc.cx, ey = y - hc.cy;
+        const bool in = ex * ex + ey * ey < sn.hex_lim2;
+        pix = hc.pid;
+        if (__any_sync(kFull, !in)) {
+          float xg, yg, qi, ri;
+          hex_axial(sn, x, y, xg, yg, qi, ri);
+          const int pf = hex_lookup(sn, htab, qi, ri);
+          float hcx, hcy;
+          hex_centre(sn, qi, ri, hcx, hcy);
+          const float hd = hex_norm(__fsub_rn(xg, hcx), __fsub_rn(yg, hcy), sn.inv_inr);
+          const float ncx = sn.off_x + (sn.gc * hcx + sn.gs * hcy);
+          const float ncy = sn.off_y + (sn.gc * hcy - sn.gs * hcx);
+          hc.cx = in ? hc.cx : ncx;
+          hc.cy = in ? hc.cy : ncy;
+          hc.pid = in ? hc.pid : pf;
+          pix = in ? pix : ((hd > sn.edge_threshold) ? -1 : pf);
+        }
+      } else {
+        pix = bin_square(sn, x, y);
+      }
+      const bool alive = ok && !shadowed && (pix >= 0);
+      const float gv0 = alive ? __ldg(p.grad_out + rowbase + pix) : 0.f;
+      if (gv0 == 0.f) continue;
+      // val = v (-c) iw ; r = d - 2 c n' (nothing flows back through the hit point)
+      const float dLdc = -gv0 * v * iw;
+      const V3 b = dLdc * d;    // dL/dn'
+      const V3 gd = dLdc * nn;  // dL/dd
+      V3 a, gs;
+      if (SRC == IACT_SRC_POINT) {
+        const V3 gw = inv_len * (gd - dot(d, gd) * d);  // d = w/|w|
+        a = gw;
+        gs = mk(-gw.x, -gw.y, -gw.z);
+      } else {
+        a = mk(0.f, 0.f, 0.f);
+        gs = gd;
+      }
+      // facet buckets: H += a (tp - pos)^T + b n'^T ; dL/dpos = a
+      const V3 pr = tp - fpos;
+      acc.H[0] += a.x * pr.x + b.x * nn.x; acc.H[1] += a.x * pr.y + b.x * nn.y; acc.H[2] += a.x * pr.z + b.x * nn.z;
+      acc.H[3] += a.y * pr.x + b.y * nn.x; acc.H[4] += a.y * pr.y + b.y * nn.y; acc.H[5] += a.y * pr.z + b.y * nn.z;
+      acc.H[6] += a.z * pr.x + b.z * nn.x; acc.H[7] += a.z * pr.y + b.z * nn.y; acc.H[8] += a.z * pr.z + b.z * nn.z;
+      acc.gp[0] += a.x; acc.gp[1] += a.y; acc.gp[2] += a.z;
+      acc.gsrc[0] += gs.x; acc.gsrc[1] += gs.y; acc.gsrc[2] += gs.z;
+      acc.gv += gv0 * -c * iw;
+    }
+    flush_src(acc, p.gsrc, s);  // the next pair has another source (or this warp ends)
+    cl = 0;
+    ++q;
+    if (++sl == SBc) {
+      sl = 0;
+      ++fl;
+    }
+  }
+  if (cur_f >= 0) flush_facet_hard(acc, p.gfacet, cur_f);
 }
 
 // Per facet: dL/dR = H R, then dL/d(tip, tilt, rot) in degrees with

@@ -442,7 +442,7 @@ size_t acc_elems(const iact_sensor_t* sn, int S, int mode) {
 WsLayout workspace_for(const iact_scene_t* sc, const iact_sensor_t* sn, int S, int mode) {
   if (mode == IACT_MODE_BACKWARD)
     return workspace_layout(sc, (size_t)std::max(sc->n_facets, 0) * kFacetGrad + (size_t)std::max(S, 0) * 4 +
-                                    (size_t)std::max(sc->n_mirrors, 0) * kMirGrad, true);
+                                    (size_t)std::max(sc->n_mirrors, 0) * kMirGrad, true, pair_mask_words(sc, S));
   return workspace_layout(sc, acc_elems(sn, S, mode), false, pair_mask_words(sc, S));
 }
 

@@ -196,6 +196,11 @@ struct RenderK {
   int flush_tiles;        // k_render_hard, IMAGE mode: tiles between flushes of the FP32 row
 };
 
+// candidate words of all (source, facet) pairs of p into out[S * F]
+// (k_masks, iact_render.cu): the scene has 1..32 primitives, B4 and the
+// tables are written
+int launch_masks(int src_type, const RenderK& p, uint32_t* out, cudaStream_t st);
+
 // Where hits go: FP32 shared-memory rows of the current tile, or the FP64
 // global accumulator. The choice is uniform over the CTA.
 struct Sink {
