@@ -67,6 +67,7 @@ struct iact_batch {
   struct Class {
     int soft = 0, stages = 0;
     int axes = 0;  // every job's sensor is axis-aligned
+    int hard = 0;  // k_batch_render_hard: 1 square, 2 hexagonal sensors; 0 k_batch_render
     int jb = 0, nj = 0, n_tiles = 0;
     int tab_floats = 0, htab_elems = 0, hist_floats = 0;
     size_t smem = 0;
@@ -79,6 +80,9 @@ struct iact_batch {
   std::vector<Class> classes;
   size_t off_counter = 0, off_jobs = 0, off_acc = 0, acc_bytes = 0, total = 0;
   long long tiles = 0, a_tiles = 0, rays = 0, max_fm = 0, max_out = 0, max_fs = 0;  // max_fm: (facet, chunk) units
+  long long max_pairs = 0;  // largest S * F among jobs with candidate words (k_batch_masks), 0: none
+  size_t mask_smem = 0;     // k_batch_masks: largest table of those jobs (bytes)
+  int mask_gx = 1;
   // prepare
   char* ws = nullptr;
   std::vector<iact::BatchJob> table;

@@ -107,6 +107,82 @@ __global__ void __launch_bounds__(256, STAGES ? 3 : IACT_RENDER_MIN_CTAS) k_batc
   }
 }
 
+// Candidate word of every (source, facet) pair of the jobs that render with
+// k_batch_render_hard (grid.y = job; jobs without a mask area skip).
+template <int SRC>
+__global__ void __launch_bounds__(256) k_batch_masks(const BatchJob* __restrict__ jobs) {
+  extern __shared__ __align__(16) float smem[];
+  const RenderK& p = jobs[blockIdx.y].rk;
+  if (!p.gmask) return;  // uniform over the CTA
+  for (int i = threadIdx.x; i < p.n_table_floats; i += blockDim.x) smem[i] = p.tables[i];
+  __syncthreads();
+  const Obst ob = make_obst(smem, p.n_cyl, p.n_box, p.n_sph, p.n_obox, p.n_tri);
+  pair_masks<SRC>(p, ob, (long long)blockIdx.x * blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x,
+                  const_cast<uint32_t*>(p.gmask));
+}
+
+// k_batch_render for a class whose jobs all take the hard-pixel tile body
+// (render_tile_hard: single stage, point or parallel sources, axis-aligned
+// sensors of one kind, rows and hexagon tables in shared memory, candidate
+// words per pair from k_batch_masks). An image job's row is flushed when the
+// CTA moves to another job, every flush_tiles tiles and at the end; the tile
+// index is double-buffered because image tiles end without a barrier.
+template <int SRC, int MODE, bool HEX>
+__global__ void __launch_bounds__(256, IACT_RENDER_MIN_CTAS) k_batch_render_hard(const BatchK b) {
+  extern __shared__ __align__(16) float smem[];
+  __shared__ __align__(16) RenderK s_p;
+  __shared__ int s_tile[2], s_job[2], s_begin[2];
+  float* tab = smem;
+  short* htab = reinterpret_cast<short*>(smem + b.tab_floats);
+  float* sh_hist = smem + b.tab_floats + b.htab_elems / 2;
+  const int nthr = blockDim.x;
+  for (int i = threadIdx.x; i < b.hist_floats; i += nthr) sh_hist[i] = 0.f;
+  int cur = -1, since = 0;
+  for (int it = 0;; ++it) {
+    const int k = it & 1;
+    if (threadIdx.x == 0) {
+      const int t = atomicAdd(b.counter, 1);
+      s_tile[k] = t;
+      if (t < b.n_tiles) {
+        int lo = 0, hi = b.n_jobs - 1;  // last job whose first tile is <= t
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (b.jobs[mid].tile_begin <= t) lo = mid;
+          else hi = mid - 1;
+        }
+        s_job[k] = lo;
+        s_begin[k] = b.jobs[lo].tile_begin;
+      }
+    }
+    __syncthreads();  // every warp is past its previous tile
+    const int tile = s_tile[k];
+    const int j = tile < b.n_tiles ? s_job[k] : -1;
+    if (MODE == IACT_MODE_IMAGE && since > 0 && (j != cur || since >= s_p.flush_tiles)) {
+      flush_rows(s_p, sh_hist, 0, 1);
+      since = 0;
+      __syncthreads();
+    }
+    if (tile >= b.n_tiles) break;
+    if (j != cur) {
+      const int* src = reinterpret_cast<const int*>(&b.jobs[j].rk);
+      int* dst = reinterpret_cast<int*>(&s_p);
+      for (int i = threadIdx.x; i < (int)(sizeof(RenderK) / 4); i += nthr) dst[i] = src[i];
+      __syncthreads();
+      for (int i = threadIdx.x; i < s_p.n_table_floats; i += nthr) tab[i] = s_p.tables[i];
+      if (HEX) {
+        const int nq = s_p.sn.table_q * s_p.sn.table_r;
+        const int n8 = (nq + 7) & ~7;
+        for (int i = threadIdx.x; i < n8; i += nthr) htab[i] = (short)(i < nq ? s_p.hex_table[i] : -1);
+      }
+      __syncthreads();
+      cur = j;
+    }
+    const Obst ob = make_obst(tab, s_p.n_cyl, s_p.n_box, s_p.n_sph, s_p.n_obox, s_p.n_tri);
+    render_tile_hard<SRC, MODE, HEX>(s_p, ob, htab, sh_hist, tile - s_begin[k]);
+    ++since;
+  }
+}
+
 __global__ void __launch_bounds__(256) k_batch_finish(const BatchJob* __restrict__ jobs) {
   const BatchJob& J = jobs[blockIdx.y];
   const double* acc = J.rk.acc;
@@ -144,6 +220,24 @@ BatchKernel pick_kernel(int src_type, bool soft, int mode, bool stages, bool axe
 }
 
 bool is_soft(const iact_sensor_t& s) { return s.type == IACT_SENSOR_SOFT_SQUARE || s.type == IACT_SENSOR_SOFT_HEX; }
+
+template <int SRC, int MODE>
+BatchKernel pick_hard_hex(bool hex) {
+  return hex ? k_batch_render_hard<SRC, MODE, true> : k_batch_render_hard<SRC, MODE, false>;
+}
+// the class kernel: k_batch_render_hard for hard classes (hard = 1 square,
+// 2 hexagonal sensors), else k_batch_render
+BatchKernel class_kernel(int src_type, int mode, const iact_batch::Class& C) {
+  if (C.hard) {
+    const bool hex = C.hard == 2;
+    if (src_type == IACT_SRC_POINT)
+      return mode == IACT_MODE_RESPONSE ? pick_hard_hex<IACT_SRC_POINT, IACT_MODE_RESPONSE>(hex)
+                                        : pick_hard_hex<IACT_SRC_POINT, IACT_MODE_IMAGE>(hex);
+    return mode == IACT_MODE_RESPONSE ? pick_hard_hex<IACT_SRC_PARALLEL, IACT_MODE_RESPONSE>(hex)
+                                      : pick_hard_hex<IACT_SRC_PARALLEL, IACT_MODE_IMAGE>(hex);
+  }
+  return pick_kernel(src_type, C.soft, mode, C.stages, C.axes);
+}
 
 }  // namespace
 }  // namespace iact
@@ -213,7 +307,7 @@ int iact_batch_create(const iact_job_t* jobs, int32_t n_jobs, int32_t source_typ
   for (int i = 0; i < n_jobs; ++i) {
     // the backward layout holds the forward's arrays too (plus deltas and buckets)
     lay[i] = backward ? workspace_for(&b->scenes[i], &b->sensors[i], jobs[i].n_sources, IACT_MODE_BACKWARD)
-                      : workspace_layout(&b->scenes[i], 0, false);
+                      : workspace_layout(&b->scenes[i], 0, false, pair_mask_words(&b->scenes[i], jobs[i].n_sources));
     rk[i] = base_params(&b->scenes[i], &b->sensors[i], lay[i], nullptr, jobs[i].sources, jobs[i].values,
                         jobs[i].n_sources);
     rk[i].seed = jobs[i].seed;
@@ -284,6 +378,19 @@ int iact_batch_create(const iact_job_t* jobs, int32_t n_jobs, int32_t source_typ
       return set_error(IACT_E_UNSUPPORTED, "iact_batch_create: more than 2^31 tiles in one class");
     }
     C.n_tiles = (int)tile;
+    // the hard-pixel tile body when every job of the class qualifies
+    {
+      const int kind = b->sensors[mem[0]].type;
+      bool hard = !soft && !stages && (source_type == IACT_SRC_POINT || source_type == IACT_SRC_PARALLEL) &&
+                  (kind == IACT_SENSOR_SQUARE || kind == IACT_SENSOR_HEX);
+      for (int i : mem)
+        hard = hard && b->sensors[i].type == kind && rk[i].sn.axes && rk[i].rows_in_smem > 0 &&
+               (kind == IACT_SENSOR_SQUARE || rk[i].hex_in_smem) &&
+               ((rk[i].n_words == 1 && lay[i].n_masks > 0) || n_primitives(&b->scenes[i]) == 0);
+      C.hard = hard ? (kind == IACT_SENSOR_HEX ? 2 : 1) : 0;
+      if (hard)  // an image row sums about 16k rays between flushes
+        for (int i : mem) rk[i].flush_tiles = std::max(1, 512 / std::max(rk[i].SB * rk[i].FC * rk[i].CC, 1));
+    }
     C.tab_floats = (int)(tab_floor / sizeof(float));
     C.htab_elems = (int)(htab_floor / sizeof(short));
     C.hist_floats = (int)(hist / sizeof(float));
@@ -366,6 +473,8 @@ int iact_batch_prepare(iact_batch* b, void* workspace, size_t workspace_bytes, v
   char* ws = static_cast<char*>(workspace);
   const int n_jobs = (int)b->jobs.size();
   std::vector<BatchJob> table(n_jobs);
+  b->max_pairs = 0;
+  b->mask_smem = 0;
   for (int ci = 0; ci < (int)b->classes.size(); ++ci) {
     const iact_batch::Class& C = b->classes[ci];
     int tile = 0, atile = 0;
@@ -381,6 +490,11 @@ int iact_batch_prepare(iact_batch* b, void* workspace, size_t workspace_bytes, v
       J.rk.counter = reinterpret_cast<int*>(base + b->lay[i].counter);
       J.rk.acc = reinterpret_cast<double*>(ws + b->off_acc + b->acc_off[pos]);
       J.rk.B4 = b->lay[i].n_b4 ? reinterpret_cast<const float4*>(base + b->lay[i].b4) : nullptr;
+      if (C.hard && J.rk.n_words) {  // candidate words per pair (k_batch_masks)
+        J.rk.gmask = reinterpret_cast<const uint32_t*>(base + b->lay[i].masks);
+        b->max_pairs = std::max(b->max_pairs, (long long)J.rk.S * J.rk.F);
+        b->mask_smem = std::max(b->mask_smem, sizeof(float) * (size_t)std::max(J.rk.n_table_floats, 1));
+      }
       J.pk = prep_params(&b->scenes[i], b->lay[i], base, false);
       J.out = b->jobs[i].out;
       J.n_out = (long long)acc_elems(&b->sensors[i], b->jobs[i].n_sources, b->mode);
@@ -421,8 +535,16 @@ int iact_batch_prepare(iact_batch* b, void* workspace, size_t workspace_bytes, v
                     "upload job table");
   if (rc) return rc;
   const DevInfo di = device_info();
+  if (b->max_pairs > 0) {
+    int per_sm = 0;
+    rc = resident_ctas(reinterpret_cast<const void*>(b->src_type == IACT_SRC_POINT ? k_batch_masks<IACT_SRC_POINT>
+                                                                                    : k_batch_masks<IACT_SRC_PARALLEL>),
+                       256, b->mask_smem, &per_sm);
+    if (rc) return rc;
+    b->mask_gx = (int)std::max<long long>(1, std::min<long long>((b->max_pairs + 255) / 256, 1024));
+  }
   for (iact_batch::Class& C : b->classes) {
-    BatchKernel kern = pick_kernel(b->src_type, C.soft, b->mode, C.stages, C.axes);
+    BatchKernel kern = class_kernel(b->src_type, b->mode, C);
     int per_sm = 0;
     rc = resident_ctas(reinterpret_cast<const void*>(kern), b->block, C.smem, &per_sm);
     if (rc) return rc;
@@ -464,6 +586,14 @@ int iact_batch_render(iact_batch* b, void* stream) {
   }
   void* const* ev = b->opts.kernel_events;
   if (ev[0]) cudaEventRecord(static_cast<cudaEvent_t>(ev[0]), st);
+  if (b->max_pairs > 0) {  // candidate words of the hard classes' jobs (inside the kernel events)
+    if (b->src_type == IACT_SRC_POINT)
+      k_batch_masks<IACT_SRC_POINT><<<dim3(b->mask_gx, n_jobs), 256, b->mask_smem, st>>>(jobs);
+    else
+      k_batch_masks<IACT_SRC_PARALLEL><<<dim3(b->mask_gx, n_jobs), 256, b->mask_smem, st>>>(jobs);
+    rc = check_cuda(cudaGetLastError(), "k_batch_masks launch");
+    if (rc) return rc;
+  }
   for (int ci = 0; ci < (int)b->classes.size(); ++ci) {
     const iact_batch::Class& C = b->classes[ci];
     if (C.n_tiles == 0) continue;
@@ -475,7 +605,7 @@ int iact_batch_render(iact_batch* b, void* stream) {
     k.tab_floats = C.tab_floats;
     k.htab_elems = C.htab_elems;
     k.hist_floats = C.hist_floats;
-    pick_kernel(b->src_type, C.soft, b->mode, C.stages, C.axes)<<<C.grid, b->block, C.smem, st>>>(k);
+    class_kernel(b->src_type, b->mode, C)<<<C.grid, b->block, C.smem, st>>>(k);
     rc = check_cuda(cudaGetLastError(), "k_batch_render launch");
     if (rc) return rc;
   }
@@ -489,7 +619,7 @@ int iact_batch_render(iact_batch* b, void* stream) {
 
 int iact_batch_info(const iact_batch* b, int64_t* out, int32_t n) {
   if (!b || !out) return set_error(IACT_E_INVALID, "iact_batch_info: NULL argument");
-  int launches = (b->max_fm > 0 ? 1 : 0) + (b->max_out > 0 ? 1 : 0), alaunches = 0;
+  int launches = (b->max_fm > 0 ? 1 : 0) + (b->max_out > 0 ? 1 : 0) + (b->max_pairs > 0 ? 1 : 0), alaunches = 0;
   for (const auto& C : b->classes) launches += C.n_tiles > 0 ? 1 : 0;
   if (b->backward) {
     alaunches = 2;  // prep (+ bucket zeroing), finish
