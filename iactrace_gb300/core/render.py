@@ -170,6 +170,18 @@ class RenderFunction(torch.autograd.Function):
         return (None, *g, *gm, *gs)
 
 
+_EMPTY = {}
+
+
+def _empty(shape, device):
+    """A cached zero-size float32 tensor (placeholders for absent inputs)."""
+    key = (tuple(shape), str(device))
+    t = _EMPTY.get(key)
+    if t is None:
+        t = _EMPTY[key] = torch.zeros(shape, device=device)
+    return t
+
+
 def _as_t(x, device):
     # python numbers become device fills (no host-to-device copy)
     return x.to(device=device, dtype=torch.float32) if isinstance(x, torch.Tensor) else \
@@ -191,8 +203,8 @@ def _stage_params(tel, device):
             surf = torch.cat([_as_t(g.curvature, device).reshape(1), _as_t(g.conic, device).reshape(1), a])
             surfs.append(surf[None, :].expand(n, 2 + N.IACT_MAX_ASPH))
     if not rots:
-        z = torch.zeros((0, 3), device=device)
-        return z, z, torch.zeros((0, 2 + N.IACT_MAX_ASPH), device=device)
+        z = _empty((0, 3), device)
+        return z, z, _empty((0, 2 + N.IACT_MAX_ASPH), device)
     return torch.cat(rots), torch.cat(poss), torch.cat(surfs)
 
 
@@ -257,26 +269,53 @@ def _state_key(tel, sensor):
     return tuple(key)
 
 
+def _object_ids(tel, sensor):
+    """Identities of the objects _state_key covers (C-level map/tuple work):
+    the telescope, the sensor, the mirror groups and their field values, the
+    obstruction groups and the sensor's field values."""
+    gs = tel.mirror_groups
+    return (id(tel), id(sensor), tuple(map(id, gs)), tuple(tuple(map(id, g.__dict__.values())) for g in gs),
+            tuple(map(id, tel.obstruction_groups or ())), tuple(map(id, sensor.__dict__.values())))
+
+
+def _tensor_fields(tel, sensor):
+    """The tensors among the mirror groups' and the sensor's fields."""
+    return tuple(v for g in tel.mirror_groups for v in g.__dict__.values() if isinstance(v, torch.Tensor)) + \
+        tuple(v for v in sensor.__dict__.values() if isinstance(v, torch.Tensor))
+
+
 def _fast_forward(tel, sensor, sensor_idx, src, val, code, mode, shape, opts, device):
     """Repeated forward calls on an unchanged telescope: the packed scene,
     the facet transforms, the sensor descriptor and the workspace size come
-    from a per-telescope cache validated by _state_key, not from re-hashing
-    the tensor storages; the launch is then two allocations and one call.
-    Returns None when the cache does not apply."""
-    key = _state_key(tel, sensor)
-    if key is None:
-        return None
+    from a per-telescope cache, not from re-hashing the tensor storages; the
+    launch is then two allocations and one call. A cache entry is valid
+    while the objects _state_key covers are the same (their identities) and
+    its tensors are unchanged (version counters) and need no gradient, which
+    is _state_key's condition checked without rebuilding its key. Returns
+    None when the cache does not apply."""
     cache = tel.__dict__.setdefault("_fast", {})
     ck = (device.index, sensor_idx, mode, int(src.shape[0]))
     hit = cache.get(ck)
-    if hit is None or hit[0] != key:
+    if hit is not None and hit[0] == _object_ids(tel, sensor):
+        tens = hit[1]
+        if any(t.requires_grad for t in tens):
+            return None
+        if tuple(t._version for t in tens) != hit[2]:
+            hit = None
+    else:
+        hit = None
+    if hit is None:
+        if _state_key(tel, sensor) is None:
+            return None
         ps = pack_scene(tel, device)
         sdesc, keep = sensor.pack(device)
         ws_bytes = max(ps.workspace_bytes(sdesc, int(src.shape[0]), mode), 256)
         # after packing: the packing caches stored on the sensor are part of its fields
-        hit = (_state_key(tel, sensor), ps, (ps.facet_rot, ps.facet_pos, ps.facet_scale), sdesc, keep, ws_bytes)
+        tens = _tensor_fields(tel, sensor)
+        hit = (_object_ids(tel, sensor), tens, tuple(t._version for t in tens), ps,
+               (ps.facet_rot, ps.facet_pos, ps.facet_scale), sdesc, keep, ws_bytes)
         cache[ck] = hit
-    _, ps, facets, sdesc, keep, ws_bytes = hit
+    ps, facets, sdesc, keep, ws_bytes = hit[3:]
     ps.set_facets(*facets)  # a packed scene may be shared by telescopes with other facet transforms
     out = torch.empty(shape, dtype=torch.float32, device=device)
     ws = torch.empty(ws_bytes, dtype=torch.uint8, device=device)
@@ -310,8 +349,8 @@ def _launch(tel, sources, values, source_type, sensor_idx, mode, opts=None, seed
         if any(t.requires_grad for g in prim for t in (g.points, g.normals, g.perturbation_delta, g.weights)):
             spts, snrm, sdlt, swts = primary_samples(tel, device)
         else:  # sample arrays are constants: nothing to carry
-            spts = snrm = sdlt = torch.zeros((0, 0, 3), device=device)
-            swts = torch.zeros((0, 0), device=device)
+            spts = snrm = sdlt = _empty((0, 0, 3), device)
+            swts = _empty((0, 0), device)
         return RenderFunction.apply((ps, sensor, code, mode, shape, opts), rot, pos, scale, src, val,
                                     mrot, mpos, msurf, spts, snrm, sdlt, swts)
     ps = pack_scene(tel, device)

@@ -220,11 +220,14 @@ def primary_params(tel, device):
     if not prim:
         z = torch.zeros((0, 3), device=device)
         return z, z, torch.zeros(0, device=device)
-    # a fresh tensor even for one group: autograd then accumulates a leaf's
-    # gradient behind an op of the calling stream (a leaf handed to the render
-    # directly would tie its creation stream into a captured backward)
-    cat = lambda name, w: torch.cat([getattr(g, name).reshape(len(g), w) if w else getattr(g, name).reshape(-1)
-                                     for g in prim]).to(device=device, dtype=torch.float32)
+    # a new autograd node even for one group (a view, which launches nothing):
+    # autograd then accumulates a leaf's gradient behind an op of the calling
+    # stream (a leaf handed to the render directly would tie its creation
+    # stream into a captured backward)
+    def cat(name, w):
+        ts = [getattr(g, name).reshape(len(g), w) if w else getattr(g, name).reshape(-1) for g in prim]
+        t = torch.cat(ts) if len(ts) > 1 else ts[0].view(ts[0].shape)
+        return t.to(device=device, dtype=torch.float32)
     return cat("rotations", 3), cat("positions", 3), cat("perturbation_scale", 0)
 
 

@@ -112,3 +112,37 @@ def test_fast_launch_key_follows_every_change():
     assert k6 != k5
     tel2 = tel.set_mirror_rotations(0, g.rotations.clone().requires_grad_(True))
     assert _state_key(tel2, tel2.sensors[0]) is None
+
+
+def test_fast_launch_validation_sees_what_the_key_sees():
+    """The per-call check of the fast forward path (object identities plus
+    the version counters of the tensor fields) changes whenever _state_key
+    does, for each kind of edit."""
+    from iactrace_gb300.core.render import _object_ids, _state_key, _tensor_fields
+    from iactrace_gb300.core import Cylinder, group_obstructions
+    tel, src, val, st = W.plain_forward(n_samples=8, n_sources=2)
+    cam = tel.sensors[0]
+
+    def check():
+        return _object_ids(tel, cam), tuple(t._version for t in _tensor_fields(tel, cam))
+
+    c0, k0 = check(), _state_key(tel, cam)
+    assert check() == c0
+    g = tel.mirror_groups[0]
+    def rotate():
+        with torch.no_grad():
+            g.rotations[3, 0] += 0.01  # facet transform in place
+
+    edits = [
+        rotate,
+        lambda: setattr(g, "perturbation_scale", g.perturbation_scale + 1e-6),
+        lambda: cam.position.__setitem__(2, cam.position[2] + 0.1),
+        lambda: setattr(cam, "edge_width", 0.003),
+        lambda: setattr(tel, "obstruction_groups",
+                        list(tel.obstruction_groups) + group_obstructions([Cylinder([0, 0, 1], [0, 0, 2], 0.1)])),
+    ]
+    for edit in edits:
+        edit()
+        c1, k1 = check(), _state_key(tel, cam)
+        assert k1 != k0 and c1 != c0
+        c0, k0 = c1, k1
