@@ -312,8 +312,10 @@ int launch_backward(const iact_scene_t* sc, const iact_sensor_t* sn, int src_typ
   }
   const int n = std::max(F, S);
   if (n > 0) {
-    k_adjoint_finish<<<(n + 255) / 256, 256, 0, st>>>(gfacet, gsrc, sc->facet_rot, F, S, g_rot, g_pos, g_scale,
-                                                        g_src, g_val);
+    // FP64 trigonometry per facet (GB300: 2 FP64 FMAs per clock per SM):
+    // one warp per block spreads the facets over the SMs
+    k_adjoint_finish<<<(n + 31) / 32, 32, 0, st>>>(gfacet, gsrc, sc->facet_rot, F, S, g_rot, g_pos, g_scale,
+                                                      g_src, g_val);
     rc = check_cuda(cudaGetLastError(), "k_adjoint_finish launch");
     if (rc) return rc;
   }

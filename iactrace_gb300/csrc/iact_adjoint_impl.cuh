@@ -750,11 +750,11 @@ __device__ __forceinline__ void adjoint_tile_hard(const AdjK& p, const Obst& ob,
 // Per facet: dL/dR = H R, then dL/d(tip, tilt, rot) in degrees with
 // R = Rz(rot) Ry(tilt) Rx(tip) (core/transforms.py:72-107); per source the
 // FP64 sums to float.
-__device__ __forceinline__ void euler_grads(const double* G, const float* deg, double* out) {
+// cs = (cos, sin) of tip, tilt and rot in radians
+__device__ __forceinline__ void euler_grads_cs(const double* G, const double* cs, double* out) {
   // dL/d(tip, tilt, rot) per degree from dL/dR, R = Rz(rot) Ry(tilt) Rx(tip)
   const double k = 0.017453292519943295;
-  const double a = deg[0] * k, b = deg[1] * k, c = deg[2] * k;
-  const double ca = cos(a), sa = sin(a), cb = cos(b), sb = sin(b), cc = cos(c), sc = sin(c);
+  const double ca = cs[0], sa = cs[1], cb = cs[2], sb = cs[3], cc = cs[4], sc = cs[5];
   const double Rx[9] = {1, 0, 0, 0, ca, -sa, 0, sa, ca}, dRx[9] = {0, 0, 0, 0, -sa, -ca, 0, ca, -sa};
   const double Ry[9] = {cb, 0, sb, 0, 1, 0, -sb, 0, cb}, dRy[9] = {-sb, 0, cb, 0, 0, 0, -cb, 0, -sb};
   const double Rz[9] = {cc, -sc, 0, sc, cc, 0, 0, 0, 1}, dRz[9] = {-sc, -cc, 0, cc, -sc, 0, 0, 0, 0};
@@ -777,6 +777,15 @@ __device__ __forceinline__ void euler_grads(const double* G, const float* deg, d
   for (int j = 0; j < 9; ++j) out[2] += G[j] * D[j];
   for (int j = 0; j < 3; ++j) out[j] *= k;
 }
+__device__ __forceinline__ void euler_cs(const float* deg, double* cs) {
+  const double k = 0.017453292519943295;
+  for (int j = 0; j < 3; ++j) sincos(deg[j] * k, &cs[2 * j + 1], &cs[2 * j]);
+}
+__device__ __forceinline__ void euler_grads(const double* G, const float* deg, double* out) {
+  double cs[6];
+  euler_cs(deg, cs);
+  euler_grads_cs(G, cs, out);
+}
 
 __device__ __forceinline__ void adjoint_mirror_item(int i, const double* gmir, const iact_mirror_t* mirrors,
                                                     float* g_rot, float* g_pos, float* g_surf) {
@@ -796,10 +805,10 @@ __device__ __forceinline__ void adjoint_finish_item(int i, const double* gfacet,
                                                     float* g_scale, float* g_src, float* g_val) {
   if (i < F) {
     const double* h = gfacet + (size_t)i * kFacetGrad;
-    const double k = 0.017453292519943295;
     // dL/dR = H R with R the facet rotation
-    const double a = facet_rot[3 * i] * k, b = facet_rot[3 * i + 1] * k, c = facet_rot[3 * i + 2] * k;
-    const double ca = cos(a), sa = sin(a), cb = cos(b), sb = sin(b), cc = cos(c), sc = sin(c);
+    double cs[6];
+    euler_cs(facet_rot + 3 * i, cs);
+    const double ca = cs[0], sa = cs[1], cb = cs[2], sb = cs[3], cc = cs[4], sc = cs[5];
     const double R[9] = {cc * cb, cc * sb * sa - sc * ca, cc * sb * ca + sc * sa,
                          sc * cb, sc * sb * sa + cc * ca, sc * sb * ca - cc * sa,
                          -sb, cb * sa, cb * ca};
@@ -807,7 +816,7 @@ __device__ __forceinline__ void adjoint_finish_item(int i, const double* gfacet,
     for (int r = 0; r < 3; ++r)
       for (int q = 0; q < 3; ++q) G[3 * r + q] = h[3 * r] * R[q] + h[3 * r + 1] * R[3 + q] + h[3 * r + 2] * R[6 + q];
     double out[3];
-    euler_grads(G, facet_rot + 3 * i, out);
+    euler_grads_cs(G, cs, out);
     if (g_rot)
       for (int j = 0; j < 3; ++j) g_rot[3 * i + j] = (float)out[j];
     if (g_pos)

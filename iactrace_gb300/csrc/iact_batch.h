@@ -43,8 +43,6 @@ struct BatchK {
                     // the tile's candidate masks follow it
 };
 
-// the batched adjoint kernel of a template class (iact_batched_adjoint.cu)
-const void* batch_adjoint_kernel(int src_type, bool soft, int mode, bool stages);
 // k_batch_prep over every job (backward: the backward prep and zeroed
 // gradient buckets) (iact_batched.cu)
 int launch_batch_prep(const BatchJob* jobs, int n_jobs, int gx, int backward, cudaStream_t st);
@@ -67,7 +65,8 @@ struct iact_batch {
   struct Class {
     int soft = 0, stages = 0;
     int axes = 0;  // every job's sensor is axis-aligned
-    int hard = 0;  // k_batch_render_hard: 1 square, 2 hexagonal sensors; 0 k_batch_render
+    int hard = 0;    // k_batch_render_hard: 1 square, 2 hexagonal sensors; 0 k_batch_render
+    int a_hard = 0;  // k_batch_adjoint_hard (hard class, no roughness-scale gradients)
     int jb = 0, nj = 0, n_tiles = 0;
     int tab_floats = 0, htab_elems = 0, hist_floats = 0;
     size_t smem = 0;
@@ -88,3 +87,10 @@ struct iact_batch {
   std::vector<iact::BatchJob> table;
   int prep_gx = 1, fin_gx = 1, afin_gx = 1;
 };
+
+namespace iact {
+// the batched adjoint kernel of a template class (iact_batched_adjoint.cu)
+const void* batch_adjoint_kernel(int src_type, int mode, const iact_batch::Class& C);
+// k_batch_masks over the jobs of the hard classes (iact_batched.cu)
+int launch_batch_masks(const iact_batch* b, const BatchJob* jobs, int n_jobs, cudaStream_t st);
+}  // namespace iact

@@ -244,6 +244,14 @@ BatchKernel class_kernel(int src_type, int mode, const iact_batch::Class& C) {
 
 using namespace iact;
 
+int iact::launch_batch_masks(const iact_batch* b, const BatchJob* jobs, int n_jobs, cudaStream_t st) {
+  if (b->src_type == IACT_SRC_POINT)
+    k_batch_masks<IACT_SRC_POINT><<<dim3(b->mask_gx, n_jobs), 256, b->mask_smem, st>>>(jobs);
+  else
+    k_batch_masks<IACT_SRC_PARALLEL><<<dim3(b->mask_gx, n_jobs), 256, b->mask_smem, st>>>(jobs);
+  return check_cuda(cudaGetLastError(), "k_batch_masks launch");
+}
+
 extern "C" {
 
 int iact_batch_create(const iact_job_t* jobs, int32_t n_jobs, int32_t source_type, int32_t mode,
@@ -388,6 +396,9 @@ int iact_batch_create(const iact_job_t* jobs, int32_t n_jobs, int32_t source_typ
                (kind == IACT_SENSOR_SQUARE || rk[i].hex_in_smem) &&
                ((rk[i].n_words == 1 && lay[i].n_masks > 0) || n_primitives(&b->scenes[i]) == 0);
       C.hard = hard ? (kind == IACT_SENSOR_HEX ? 2 : 1) : 0;
+      bool a_hard = hard && backward;
+      for (int i : mem) a_hard = a_hard && !jobs[i].g_facet_scale;
+      C.a_hard = a_hard ? 1 : 0;
       if (hard)  // an image row sums about 16k rays between flushes
         for (int i : mem) rk[i].flush_tiles = std::max(1, 512 / std::max(rk[i].SB * rk[i].FC * rk[i].CC, 1));
     }
@@ -515,6 +526,7 @@ int iact_batch_prepare(iact_batch* b, void* workspace, size_t workspace_bytes, v
         a.gsrc = a.gfacet + (size_t)a.F * kFacetGrad;
         a.gmir = a.gsrc + (size_t)a.S * 4;
         a.want_mgrad = (U.g_mirror_rot || U.g_mirror_pos || U.g_mirror_surface) ? 1 : 0;
+        a.gmask = C.a_hard ? J.rk.gmask : nullptr;  // the forward's candidate words (k_batch_masks)
         J.pkb = prep_params(&b->scenes[i], b->lay[i], base, U.g_facet_scale != nullptr);
         J.gr.g_rot = U.g_facet_rot; J.gr.g_pos = U.g_facet_pos; J.gr.g_scale = U.g_facet_scale;
         J.gr.g_src = U.g_sources; J.gr.g_val = U.g_values;
@@ -552,13 +564,13 @@ int iact_batch_prepare(iact_batch* b, void* workspace, size_t workspace_bytes, v
     C.grid = std::max(1, std::min(C.n_tiles, per_sm * di.sm_count));
     if (b->backward) {
       per_sm = 0;
-      rc = resident_ctas(batch_adjoint_kernel(b->src_type, C.soft, b->mode, C.stages), b->block, C.a_smem, &per_sm);
+      rc = resident_ctas(batch_adjoint_kernel(b->src_type, b->mode, C), b->block, C.a_smem, &per_sm);
       if (rc) return rc;
       if (per_sm < 1) return set_error(IACT_E_UNSUPPORTED, "batched adjoint kernel does not fit on an SM");
       C.a_grid = std::max(1, std::min(C.a_tiles, per_sm * di.sm_count));
     }
   }
-  b->afin_gx = (int)std::max<long long>(1, std::min<long long>((b->max_fs + 255) / 256, 1024));
+  b->afin_gx = (int)std::max<long long>(1, std::min<long long>((b->max_fs + 31) / 32, 1024));
   b->prep_gx = (int)std::max<long long>(1, std::min<long long>((b->max_fm + 7) / 8, 1024));  // 8 warps per block
   b->fin_gx = (int)std::max<long long>(1, std::min<long long>((b->max_out + 255) / 256, 1024));
   b->table = std::move(table);
@@ -587,11 +599,7 @@ int iact_batch_render(iact_batch* b, void* stream) {
   void* const* ev = b->opts.kernel_events;
   if (ev[0]) cudaEventRecord(static_cast<cudaEvent_t>(ev[0]), st);
   if (b->max_pairs > 0) {  // candidate words of the hard classes' jobs (inside the kernel events)
-    if (b->src_type == IACT_SRC_POINT)
-      k_batch_masks<IACT_SRC_POINT><<<dim3(b->mask_gx, n_jobs), 256, b->mask_smem, st>>>(jobs);
-    else
-      k_batch_masks<IACT_SRC_PARALLEL><<<dim3(b->mask_gx, n_jobs), 256, b->mask_smem, st>>>(jobs);
-    rc = check_cuda(cudaGetLastError(), "k_batch_masks launch");
+    rc = launch_batch_masks(b, jobs, n_jobs, st);
     if (rc) return rc;
   }
   for (int ci = 0; ci < (int)b->classes.size(); ++ci) {

@@ -100,9 +100,74 @@ __global__ void __launch_bounds__(256) k_batch_adjoint_finish(const BatchJob* __
   }
 }
 
+// k_batch_adjoint for a class whose jobs all take the hard-pixel adjoint
+// body (adjoint_tile_hard; the class renders with k_batch_render_hard and no
+// job asks for roughness-scale gradients): candidate words per pair from
+// k_batch_masks. Tiles end without a barrier, so the tile index is
+// double-buffered.
+template <int SRC, int MODE, bool HEX>
+__global__ void __launch_bounds__(256, 4) k_batch_adjoint_hard(const BatchK b) {
+  extern __shared__ __align__(16) float smem[];
+  __shared__ __align__(16) AdjK s_a;
+  __shared__ int s_tile[2], s_job[2], s_begin[2];
+  float* tab = smem;
+  short* htab = reinterpret_cast<short*>(smem + b.tab_floats);
+  const int nthr = blockDim.x;
+  int cur = -1;
+  for (int it = 0;; ++it) {
+    const int k = it & 1;
+    if (threadIdx.x == 0) {
+      const int t = atomicAdd(b.counter, 1);
+      s_tile[k] = t;
+      if (t < b.n_tiles) {
+        int lo = 0, hi = b.n_jobs - 1;  // last job whose first adjoint tile is <= t
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (b.jobs[mid].atile_begin <= t) lo = mid;
+          else hi = mid - 1;
+        }
+        s_job[k] = lo;
+        s_begin[k] = b.jobs[lo].atile_begin;
+      }
+    }
+    __syncthreads();  // every warp is past its previous tile
+    const int tile = s_tile[k];
+    if (tile >= b.n_tiles) break;
+    const int j = s_job[k];
+    if (j != cur) {
+      const int* src = reinterpret_cast<const int*>(&b.jobs[j].ak);
+      int* dst = reinterpret_cast<int*>(&s_a);
+      for (int i = threadIdx.x; i < (int)(sizeof(AdjK) / 4); i += nthr) dst[i] = src[i];
+      __syncthreads();
+      for (int i = threadIdx.x; i < s_a.n_table_floats; i += nthr) tab[i] = s_a.tables[i];
+      if (HEX) {
+        const int nq = s_a.sn.table_q * s_a.sn.table_r;
+        const int n8 = (nq + 7) & ~7;
+        for (int i = threadIdx.x; i < n8; i += nthr) htab[i] = (short)(i < nq ? s_a.hex_table[i] : -1);
+      }
+      __syncthreads();
+      cur = j;
+    }
+    const Obst ob = make_obst(tab, s_a.n_cyl, s_a.n_box, s_a.n_sph, s_a.n_obox, s_a.n_tri);
+    adjoint_tile_hard<SRC, MODE, HEX>(s_a, ob, htab, tile - s_begin[k]);
+  }
+}
+
 namespace {
 
 using AdjKernel = void (*)(BatchK);
+
+template <int SRC, int MODE>
+AdjKernel pick_a_hard_hex(bool hex) {
+  return hex ? k_batch_adjoint_hard<SRC, MODE, true> : k_batch_adjoint_hard<SRC, MODE, false>;
+}
+AdjKernel pick_adjoint_hard(int src_type, int mode, bool hex) {
+  if (src_type == IACT_SRC_POINT)
+    return mode == IACT_MODE_RESPONSE ? pick_a_hard_hex<IACT_SRC_POINT, IACT_MODE_RESPONSE>(hex)
+                                      : pick_a_hard_hex<IACT_SRC_POINT, IACT_MODE_IMAGE>(hex);
+  return mode == IACT_MODE_RESPONSE ? pick_a_hard_hex<IACT_SRC_PARALLEL, IACT_MODE_RESPONSE>(hex)
+                                    : pick_a_hard_hex<IACT_SRC_PARALLEL, IACT_MODE_IMAGE>(hex);
+}
 
 template <int SRC, bool SOFT, int MODE>
 AdjKernel pick_a_stages(bool stages) {
@@ -125,8 +190,9 @@ AdjKernel pick_adjoint(int src_type, bool soft, int mode, bool stages) {
 
 }  // namespace
 
-const void* batch_adjoint_kernel(int src_type, bool soft, int mode, bool stages) {
-  return reinterpret_cast<const void*>(pick_adjoint(src_type, soft, mode, stages));
+const void* batch_adjoint_kernel(int src_type, int mode, const iact_batch::Class& C) {
+  if (C.a_hard) return reinterpret_cast<const void*>(pick_adjoint_hard(src_type, mode, C.hard == 2));
+  return reinterpret_cast<const void*>(pick_adjoint(src_type, C.soft, mode, C.stages));
 }
 
 }  // namespace iact
@@ -149,6 +215,10 @@ extern "C" int iact_batch_backward(iact_batch* b, void* stream) {
   if (rc) return rc;
   void* const* ev = b->opts.kernel_events;
   if (ev[0]) cudaEventRecord(static_cast<cudaEvent_t>(ev[0]), st);
+  if (b->max_pairs > 0) {  // candidate words of the hard classes' jobs (the sources may have changed)
+    rc = launch_batch_masks(b, jobs, n_jobs, st);
+    if (rc) return rc;
+  }
   for (int ci = 0; ci < (int)b->classes.size(); ++ci) {
     const iact_batch::Class& C = b->classes[ci];
     if (C.a_tiles == 0) continue;
@@ -160,11 +230,12 @@ extern "C" int iact_batch_backward(iact_batch* b, void* stream) {
     k.tab_floats = C.a_tab_floats;
     k.htab_elems = C.a_htab_elems;
     k.hist_floats = C.a_mgrad_floats;
-    pick_adjoint(b->src_type, C.soft, b->mode, C.stages)<<<C.a_grid, b->block, C.a_smem, st>>>(k);
+    reinterpret_cast<AdjKernel>(const_cast<void*>(batch_adjoint_kernel(b->src_type, b->mode, C)))
+        <<<C.a_grid, b->block, C.a_smem, st>>>(k);
     rc = check_cuda(cudaGetLastError(), "k_batch_adjoint launch");
     if (rc) return rc;
   }
   if (ev[1]) cudaEventRecord(static_cast<cudaEvent_t>(ev[1]), st);
-  k_batch_adjoint_finish<<<dim3(b->afin_gx, n_jobs), 256, 0, st>>>(jobs);
+  k_batch_adjoint_finish<<<dim3(b->afin_gx, n_jobs), 32, 0, st>>>(jobs);  // one warp per block (FP64 trigonometry)
   return check_cuda(cudaGetLastError(), "k_batch_adjoint_finish launch");
 }
