@@ -90,7 +90,9 @@ def test_hard_adjoint_equals_generic(cuda, name, mode):
     for k in hard:
         a, b = hard[k].double(), generic[k].double()
         nb = float(b.norm())
-        assert nb > 0, k
+        if nb == 0:  # e.g. facet positions under parallel sources and hard pixels: no path carries gradient
+            assert float(a.abs().max()) == 0, k
+            continue
         err = float((a - b).norm()) / nb
         assert err <= 1e-5, f"{k}: relative L2 {err:.3g} between the hard and the generic adjoint"
     del keep
