@@ -44,8 +44,9 @@ constexpr int kMirGrad = 22;    // per stage mirror: dL/dR (9), dL/dpos (3), dL/
 // adjoint takes scenes of at most kAdjRing later stages.
 constexpr int kAdjRing = 2;
 WsLayout workspace_layout(const iact_scene_t* sc, size_t acc_elems, bool with_delta, size_t mask_words = 0);
-// candidate words a forward render of S sources keeps per (source, facet)
-// pair: S * F for scenes of 1..32 shadowing primitives, else 0
+// candidate words a render of S sources keeps per (source, facet) pair:
+// S * F for scenes of 1..32 shadowing primitives while that is at most 2^26,
+// else 0 (the render then keeps per-tile masks)
 size_t pair_mask_words(const iact_scene_t* sc, int S);
 size_t acc_elems(const iact_sensor_t* sn, int S, int mode);  // 0 for DEBUG
 WsLayout workspace_for(const iact_scene_t* sc, const iact_sensor_t* sn, int S, int mode);

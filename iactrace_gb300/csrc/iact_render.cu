@@ -402,7 +402,9 @@ int dispatch_soft(bool soft, int mode, bool stages, RenderK p, int block, size_t
 
 size_t pair_mask_words(const iact_scene_t* sc, int S) {
   const int np = n_primitives(sc);
-  return (np > 0 && np <= 32) ? (size_t)std::max(S, 0) * (size_t)std::max(sc->n_facets, 0) : 0;
+  const size_t n = (size_t)std::max(S, 0) * (size_t)std::max(sc->n_facets, 0);
+  // at most 2^26 words (256 MiB): larger renders keep per-tile masks (k_render)
+  return (np > 0 && np <= 32 && n <= ((size_t)1 << 26)) ? n : 0;
 }
 
 WsLayout workspace_layout(const iact_scene_t* sc, size_t acc_elems, bool with_delta, size_t mask_words) {
@@ -543,7 +545,8 @@ int launch_render(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type,
   // every (source, facet) pair from k_masks
   const bool hard = !soft && !stages && (src_type == IACT_SRC_POINT || src_type == IACT_SRC_PARALLEL) &&
                     p.sn.axes && (sn->type == IACT_SENSOR_SQUARE || sn->type == IACT_SENSOR_HEX) &&
-                    (p.n_words == 1 || n_primitives(sc) == 0) && !(opts && opts->hist_mode == 2);
+                    ((p.n_words == 1 && L.n_masks > 0) || n_primitives(sc) == 0) &&
+                    !(opts && opts->hist_mode == 2);
   // image renders of k_render_hard keep their FP32 row across tiles and need
   // no masks per tile, so their tiles are smaller (balance at the end of a
   // launch: 1000-sample plain forward 51.5 us at 12 tiles per SM vs 57.4 at

@@ -203,3 +203,28 @@ def test_size_limits_are_validated(built):
         assert ws(sc) == rc, n
     assert ws(_fake_scene(1 << 15, 1 << 15)) == N.IACT_OK
     assert ws(_fake_scene(1 << 15, (1 << 15) + 1)) == N.IACT_E_UNSUPPORTED
+
+
+def test_pair_mask_workspace_is_capped(built):
+    """Renders of scenes with 1..32 primitives keep one candidate word per
+    (source, facet) pair in the workspace, up to 2^26 words; beyond that they
+    need none (the generic kernel keeps per-tile masks)."""
+    from iactrace_gb300 import Telescope, workloads as W
+    from iactrace_gb300.core.scene import pack_scene
+    tel, _, _, _ = W.plain_forward(n_samples=8, n_sources=1)
+    bare = Telescope(tel.mirror_groups, [], tel.sensors)
+    F = 380
+
+    def size(t, S):
+        ps = pack_scene(t, "cpu")
+        sd, keep = t.sensors[0].pack("cpu")
+        sz = ctypes.c_size_t(0)
+        N.check(built.iact_workspace_size(ctypes.byref(ps.desc), ctypes.byref(sd), S, N.MODE_IMAGE,
+                                          ctypes.byref(sz)))
+        del keep
+        return sz.value
+
+    S = 1000
+    assert size(tel, S) - size(bare, S) >= S * F * 4  # facet bounds + the pair words
+    S = (1 << 26) // F + 1
+    assert size(tel, S) - size(bare, S) < 1000 * F * 4  # facet bounds only
