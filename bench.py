@@ -66,15 +66,17 @@ KERNEL = {"response": "k_masks + k_render_hard", "plain": "k_masks + k_render_ha
 # have changed since, the figures are reported as stale and not used as the
 # roofline's traffic.
 CAPTURES = {
-    "response": {"digest": "666267296bfba4c6", "profile": "profiles/k_render_response_matrix_dc380_hex2048.md",
-                 "dram_bytes": 7.337e6, "shared_atomic_frac": 0.124, "thread_inst_per_ray": 219,
-                 "fma_pipe": 0.247, "issue_active": 0.834},
-    "plain": {"digest": "666267296bfba4c6", "profile": "profiles/k_render_plain_forward_dc380_square960.md",
-              "dram_bytes": 12.24e6, "shared_atomic_frac": 0.060, "thread_inst_per_ray": 210,
-              "fma_pipe": 0.200, "issue_active": 0.653},
-    "cassegrain": {"digest": "666267296bfba4c6", "profile": "profiles/k_render_cassegrain_61seg_square1024.md",
-                   "dram_bytes": 1.049e6, "shared_atomic_frac": 0.026, "thread_inst_per_ray": 941,
-                   "fma_pipe": 0.390, "issue_active": 0.738},
+    "response": {"digest": "959f5d7ba4953a79", "profile": "profiles/k_render_hard_response_matrix_dc380_hex2048.md",
+                 "dram_bytes": 13.51e6, "shared_atomic_frac": 0.096, "thread_inst_per_ray": 175,
+                 "fma_pipe": 0.351, "issue_active": 0.850},
+    "plain": {"digest": "959f5d7ba4953a79", "profile": "profiles/k_render_hard_plain_forward_dc380_square960.md",
+              "dram_bytes": 12.21e6, "shared_atomic_frac": 0.090, "thread_inst_per_ray": 183,
+              "fma_pipe": 0.250, "issue_active": 0.679},
+    "cassegrain": {"digest": "959f5d7ba4953a79", "profile": "profiles/k_render_cassegrain_61seg_square1024.md",
+                   "dram_bytes": 1.050e6, "shared_atomic_frac": 0.026, "thread_inst_per_ray": 945,
+                   "fma_pipe": 0.392, "issue_active": 0.742},
+    "batched": {"digest": "959f5d7ba4953a79", "profile": "profiles/k_batch_render_hard_ragged_batch64_hex960_2048.md",
+                "dram_bytes": 384.9e6, "thread_inst_per_ray": 188, "fma_pipe": 0.309, "issue_active": 0.804},
 }
 
 
@@ -559,6 +561,7 @@ def run_batched(args, rank, world):
     achieved = F_RAY["batched"] * rays / kern_s / 1e12
     h2d = sum(s.numel() * 4 + v.numel() * 4 for s, v in zip(srcs_h, vals_h))
     d2h = sum(x.numel() * 4 for x in b.outs)
+    bcap, bcap_ok = capture_fields("batched")
     line = {
         "metric": METRIC + " [ragged batch: one persistent launch + CUDA graph]", "value": rays * world / batch_s,
         "unit": "rays/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -575,9 +578,16 @@ def run_batched(args, rank, world):
         "batched_vs_per_instance": inst_s / batch_s,
         "small_instances": small,
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-                     "traffic": None, "kernel": KERNEL["batched"], "kernel_ms": kern_s * 1e3,
+                     "traffic": bcap["dram_bytes"] if bcap_ok else None,
+                     "traffic_unit": "bytes per launch (ncu dram__bytes_read + write)",
+                     "kernel": KERNEL["batched"], "kernel_ms": kern_s * 1e3,
                      "flops_per_ray": F_RAY["batched"],
-                     "peak_source": "measured live: FP32 FMA-chain probe kernel (iact_probe_fma)"},
+                     "flops_note": "algorithmic: the reference's full evaluation per ray without early-out "
+                                   "(obstruction tests the bundle culling skips are counted)",
+                     "peak_source": "measured live: FP32 FMA-chain probe kernel (iact_probe_fma)",
+                     "executed": {k: bcap[k] for k in ("thread_inst_per_ray", "fma_pipe", "issue_active")
+                                  if k in bcap} if bcap_ok else None,
+                     "capture": bcap},
         "fwd_adjoint_per_instance": {"value": rays / fa_s, "unit": "rays/s", "ms_per_step": fa_s * 1e3,
                                      "time_ratio_vs_batched_fwd": fa_s / batch_s},
         "fwd_adjoint_batched": {"value": rays / fab_s, "unit": "rays/s", "ms_per_step": fab_s * 1e3,
@@ -806,30 +816,34 @@ def main():
     # K steps back to back, each: sources and values copied in from pinned
     # memory, render, result copied back into pinned memory on a second
     # stream (two buffers), so step k's copy-back overlaps step k+1's render;
-    # the time per step is the loop's span (first step's start to the last
-    # copy-back's end) less the L2-flush writes between steps, over K
-    cstream = torch.cuda.Stream(dev)
-    out_pins = [out_pin, torch.empty(out.shape, dtype=torch.float32).pin_memory()]
+    # the L2-flush write before each step stays in the loop, its time (the
+    # mean of K flushes timed alone) is subtracted: time per step = (the
+    # loop's span from the first step's start to the last copy-back's end -
+    # (K - 1) flushes) / K. No per-step events: on a short step their host
+    # cost would pace the loop
     ev = lambda: torch.cuda.Event(enable_timing=True)
     fill_ev = [(ev(), ev()) for _ in range(args.steps)]
-    start, done = ev(), [ev() for _ in range(args.steps)]
-    end = ev()
     for k in range(args.steps):
         fill_ev[k][0].record(stream)
         flush_buf.fill_(float(k))
         fill_ev[k][1].record(stream)
+    torch.cuda.synchronize(dev)
+    fill_s = sum(a.elapsed_time(b) for a, b in fill_ev) / 1e3 / args.steps
+    cstream = torch.cuda.Stream(dev)
+    out_pins = [out_pin, torch.empty(out.shape, dtype=torch.float32).pin_memory()]
+    start, end = ev(), ev()
+    for k in range(args.steps):
+        flush_buf.fill_(float(k))
         if k == 0:
             start.record(stream)
         o = fn(tel, src_pin.to(dev, non_blocking=True), val_pin.to(dev, non_blocking=True), stype)
-        done[k].record(stream)
-        cstream.wait_event(done[k])
+        cstream.wait_stream(stream)
         with torch.cuda.stream(cstream):
             out_pins[k % 2].copy_(o, non_blocking=True)
         o.record_stream(cstream)
     end.record(cstream)
     torch.cuda.synchronize(dev)
-    fills = sum(a.elapsed_time(b) for a, b in fill_ev[1:])
-    e2e_s = (start.elapsed_time(end) - fills) / 1e3 / args.steps
+    e2e_s = (start.elapsed_time(end) / 1e3 - (args.steps - 1) * fill_s) / args.steps
     # the same call timed by the host clock, one call at a time: each step
     # ends with a synchronize, so the host's own overhead (argument checks,
     # the cached packing, launches, copies) and the synchronisation latency
@@ -879,7 +893,7 @@ def main():
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3,
                 "timing": "K steps back to back (copy in, render, copy back on a second stream, so a "
                           "step's copy-back overlaps the next render); CUDA events around the loop, less "
-                          "the L2-flush writes between steps, over K",
+                          "the L2-flush writes between steps (their mean time alone), over K",
                 "host_wall": {"value": rays * world / wall_s, "unit": "rays/s", "ms_per_step": wall_s * 1e3,
                               "timing": "host clock around call + copies + synchronize, one step at a time "
                                         "(median)"},
