@@ -69,11 +69,11 @@ __global__ void __launch_bounds__(256, STAGES ? 2 : (SOFT ? 3 : 4)) k_adjoint(co
   }
 }
 
-// k_adjoint for the common hard-pixel case (adjoint_tile_hard): the host
-// picks it when the backward qualifies. Shared memory: tables and hexagon
-// table. Tiles end without a barrier, so the tile index is double-buffered.
-template <int SRC, int MODE, bool HEX>
-__global__ void __launch_bounds__(256, 4) k_adjoint_hard(const AdjK p) {
+// Shared-memory layout (tables, hexagon table) and persistent tile loop of
+// the specialised adjoints (k_adjoint_hard, k_adjoint_soft). Tiles end
+// without a barrier, so the tile index is double-buffered.
+template <bool HEX, typename Body>
+__device__ __forceinline__ void adj_tile_loop(const AdjK& p, Body body) {
   extern __shared__ __align__(16) float smem[];
   __shared__ int s_tile[2];
   const int tab_n = (p.n_table_floats + 3) & ~3;
@@ -91,8 +91,25 @@ __global__ void __launch_bounds__(256, 4) k_adjoint_hard(const AdjK p) {
     __syncthreads();
     const int tile = s_tile[it & 1];
     if (tile >= p.n_tiles) break;
-    adjoint_tile_hard<SRC, MODE, HEX>(p, ob, htab, tile);
+    body(ob, htab, tile);
   }
+}
+
+// k_adjoint for the common hard-pixel case (adjoint_tile_hard): the host
+// picks it when the backward qualifies.
+template <int SRC, int MODE, bool HEX>
+__global__ void __launch_bounds__(256, 4) k_adjoint_hard(const AdjK p) {
+  adj_tile_loop<HEX>(p, [&](const Obst& ob, const short* htab, int tile) {
+    adjoint_tile_hard<SRC, MODE, HEX>(p, ob, htab, tile);
+  });
+}
+
+// k_adjoint for the common soft-pixel case (adjoint_tile_soft).
+template <int SRC, int MODE, bool HEX>
+__global__ void __launch_bounds__(256, 3) k_adjoint_soft(const AdjK p) {
+  adj_tile_loop<HEX>(p, [&](const Obst& ob, const short* htab, int tile) {
+    adjoint_tile_soft<SRC, MODE, HEX>(p, ob, htab, tile);
+  });
 }
 
 __global__ void k_adjoint_mirrors(const double* gmir, const iact_mirror_t* mirrors, int n_mir, float* g_rot,
@@ -162,6 +179,28 @@ int run_adjoint_hard(int src_type, int mode, bool hex, const AdjK& p, int block,
   const int grid = std::max(1, std::min(p.n_tiles, per_sm * device_info().sm_count));
   kern<<<grid, block, smem, st>>>(p);
   return check_cuda(cudaGetLastError(), "k_adjoint launch");
+}
+
+// the common soft-pixel case (k_adjoint_soft)
+template <int SRC>
+int run_adjoint_soft_src(int mode, bool hex, const AdjK& p, int block, size_t smem, cudaStream_t st) {
+  void (*kern)(const AdjK);
+  if (mode == IACT_MODE_RESPONSE)
+    kern = hex ? k_adjoint_soft<SRC, IACT_MODE_RESPONSE, true> : k_adjoint_soft<SRC, IACT_MODE_RESPONSE, false>;
+  else
+    kern = hex ? k_adjoint_soft<SRC, IACT_MODE_IMAGE, true> : k_adjoint_soft<SRC, IACT_MODE_IMAGE, false>;
+  int per_sm = 0;
+  const int rc = resident_ctas(reinterpret_cast<const void*>(kern), block, smem, &per_sm);
+  if (rc) return rc;
+  if (per_sm < 1) return set_error(IACT_E_UNSUPPORTED, "adjoint kernel does not fit on an SM");
+  const int grid = std::max(1, std::min(p.n_tiles, per_sm * device_info().sm_count));
+  kern<<<grid, block, smem, st>>>(p);
+  return check_cuda(cudaGetLastError(), "k_adjoint launch");
+}
+int run_adjoint_soft(int src_type, int mode, bool hex, const AdjK& p, int block, size_t smem, cudaStream_t st) {
+  if (src_type == IACT_SRC_POINT) return run_adjoint_soft_src<IACT_SRC_POINT>(mode, hex, p, block, smem, st);
+  if (src_type == IACT_SRC_EXTENDED) return run_adjoint_soft_src<IACT_SRC_EXTENDED>(mode, hex, p, block, smem, st);
+  return run_adjoint_soft_src<IACT_SRC_PARALLEL>(mode, hex, p, block, smem, st);
 }
 
 // the render parameters k_masks reads, from the adjoint's
@@ -283,9 +322,10 @@ int launch_backward(const iact_scene_t* sc, const iact_sensor_t* sn, int src_typ
     const int stages = n_mir > 0 ? std::max(sc->n_stages, 1) : 0;
     // the common hard-pixel case: k_adjoint_hard with the candidate word of
     // every (source, facet) pair from k_masks (inside the kernel events)
-    const bool hard = !soft && n_mir == 0 && (src_type == IACT_SRC_POINT || src_type == IACT_SRC_PARALLEL) &&
-                      p.sn.axes && !g_scale && !g_samples &&
-                      (sn->type == IACT_SENSOR_SQUARE || (sn->type == IACT_SENSOR_HEX && p.hex_in_smem)) &&
+    // (soft pixels: k_adjoint_soft, also for extended sources)
+    const bool hex_kind = sn->type == IACT_SENSOR_HEX || sn->type == IACT_SENSOR_SOFT_HEX;
+    const bool hard = n_mir == 0 && (soft || src_type == IACT_SRC_POINT || src_type == IACT_SRC_PARALLEL) &&
+                      p.sn.axes && !g_scale && !g_samples && (!hex_kind || p.hex_in_smem) &&
                       ((p.n_words == 1 && L.n_masks > 0) || n_primitives(sc) == 0);
     if (hard) {
       if (p.n_words) {
@@ -294,10 +334,9 @@ int launch_backward(const iact_scene_t* sc, const iact_sensor_t* sn, int src_typ
         if (rc) return rc;
       }
       const size_t hsmem = sizeof(float) * (size_t)((p.n_table_floats + 3) & ~3) +
-                           (sn->type == IACT_SENSOR_HEX
-                                ? sizeof(short) * (((size_t)sn->table_q * sn->table_r + 7) & ~(size_t)7)
-                                : 0);
-      rc = run_adjoint_hard(src_type, mode, sn->type == IACT_SENSOR_HEX, p, block, hsmem, st);
+                           (hex_kind ? sizeof(short) * (((size_t)sn->table_q * sn->table_r + 7) & ~(size_t)7) : 0);
+      if (soft) rc = run_adjoint_soft(src_type, mode, hex_kind, p, block, hsmem, st);
+      else rc = run_adjoint_hard(src_type, mode, hex_kind, p, block, hsmem, st);
     } else if (src_type == IACT_SRC_POINT)
       rc = soft ? adj_stages<IACT_SRC_POINT, true>(stages, mode, p, block, smem, st)
                 : adj_stages<IACT_SRC_POINT, false>(stages, mode, p, block, smem, st);

@@ -747,7 +747,133 @@ __device__ __forceinline__ void adjoint_tile_hard(const AdjK& p, const Obst& ob,
   if (cur_f >= 0) flush_facet_hard(acc, p.gfacet, cur_f);
 }
 
-// Per facet: dL/dR = H R, then dL/d(tip, tilt, rot) in degrees with
+// Soft-pixel adjoint tile of the common case: a single-stage scene, point,
+// parallel or extended sources, a sensor whose rotation is the identity,
+// the hexagon table in shared memory, candidate words per (source, facet)
+// pair from k_masks, and no roughness-scale or per-sample gradients. The
+// arithmetic is adjoint_tile<SRC, true, MODE, false, true>'s: the reverse of
+// the soft deposit (soft_square_bwd / soft_hex_bwd), of the sensor-plane hit
+// and of the reflection; the sensor kind is compile-time, per-pair values
+// (source, jitter basis, value, facet position, candidate word) are loaded
+// once per pair, and a warp's tasks run facet by facet (source next, chunk
+// fastest) as in adjoint_tile_hard.
+template <int SRC, int MODE, bool HEX>
+__device__ __forceinline__ void adjoint_tile_soft(const AdjK& p, const Obst& ob, const short* htab, int tile) {
+  const SensorK& sn = p.sn;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  const int nch = (p.M + 31) >> 5;
+  Acc acc;
+  acc_zero_facet(acc);
+  acc_zero_src(acc);
+  const int per_s = p.n_fchunk * p.n_cchunk;
+  const int sblk = tile / per_s;
+  const int fc = (tile - sblk * per_s) / p.n_cchunk;
+  const int cc = tile - sblk * per_s - fc * p.n_cchunk;
+  const int s0 = sblk * p.SB, f0 = fc * p.FC, c0 = cc * p.CC;
+  const int SBc = min(p.SB, p.S - s0), FCc = min(p.FC, p.F - f0), CCc = min(p.CC, nch - c0);
+  const int T = SBc * FCc * CCc;
+  const int tb = (warp * T) / nw, te = ((warp + 1) * T) / nw;
+  constexpr int SS = (SRC == IACT_SRC_EXTENDED) ? 4 : 3;
+  // tasks t = (facet fl, source sl, chunk cl), chunk fastest
+  int q = tb / CCc;  // pair index fl * SBc + sl
+  int fl = q / SBc, sl = q - fl * SBc;
+  int cl = tb - q * CCc;
+  int cur_f = -1;
+  const int mlast = p.M - 1;
+  for (int t = tb; t < te;) {
+    const int s = s0 + sl, f = f0 + fl;
+    const int ce = min(CCc, cl + (te - t));
+    t += ce - cl;
+    if (f != cur_f) {
+      if (cur_f >= 0) flush_facet_hard(acc, p.gfacet, cur_f);
+      cur_f = f;
+    }
+    const V3 src = mk(__ldg(p.sources + SS * s), __ldg(p.sources + SS * s + 1), __ldg(p.sources + SS * s + 2));
+    const float sig = (SRC == IACT_SRC_EXTENDED) ? __ldg(p.sources + SS * s + 3) : 0.f;
+    const float v = __ldg(p.values + s);
+    const V3 fpos = mk(__ldg(p.facet_pos + 3 * f), __ldg(p.facet_pos + 3 * f + 1), __ldg(p.facet_pos + 3 * f + 2));
+    const uint32_t word = p.gmask ? __ldg(p.gmask + (size_t)s * p.F + f) : 0u;
+    const int rowbase = (MODE == IACT_MODE_RESPONSE) ? s * p.P : 0;
+    const int fbase = f * p.M;
+    JBasis jb;
+    if (SRC == IACT_SRC_EXTENDED) jb = jitter_basis(src);
+    for (; cl < ce; ++cl) {
+      const int m = (c0 + cl) * 32 + lane;
+      const bool ok = m < p.M;
+      const int mc = ok ? m : mlast;
+      const float4 P4 = __ldg(p.P4 + fbase + mc), N4 = __ldg(p.N4 + fbase + mc);
+      const V3 tp = mk(P4.x, P4.y, P4.z), nn = mk(N4.x, N4.y, N4.z);
+      const float iw = P4.w;
+      // ---- forward re-trace
+      V3 d, w;
+      float inv_len = 0.f;
+      if (SRC == IACT_SRC_POINT) {
+        w = tp - src;
+        inv_len = rsqrtf(dot(w, w));
+        d = inv_len * w;
+      } else if (SRC == IACT_SRC_EXTENDED) {  // jitter regenerated from its counter
+        float z0, z1;
+        ray_normals(p.seed, s, f, mc, z0, z1);
+        d = jitter_dir(jb, sig, z0, z1);
+      } else {
+        d = src;
+      }
+      bool shadowed = false;
+      if (word) shadowed = shadow_word(ob, word, tp, mk(-d.x, -d.y, -d.z));  // warp-uniform
+      const float c = dot(d, nn);
+      const V3 r = d - (2.f * c) * nn;
+      const float val = v * -c * iw;
+      const bool parallel = fabsf(r.z) < 1e-10f;
+      const float inv_nd = rcp_a(parallel ? 1.f : r.z);
+      const float tpl = (sn.pos[2] - tp.z) * inv_nd;
+      const bool hit_plane = !parallel && (tpl > 0.f);
+      const float x = hit_plane ? (tp.x + tpl * r.x) - sn.pos[0] : kBig;
+      const float y = hit_plane ? (tp.y + tpl * r.y) - sn.pos[1] : kBig;
+      // ---- reverse of the soft deposit
+      float gval = 0.f, gx = 0.f, gy = 0.f;
+      if (ok && !shadowed) {
+        if (HEX) soft_hex_bwd(sn, htab, p.grad_out, rowbase, x, y, val, gval, gx, gy);
+        else soft_square_bwd(sn, p.grad_out, rowbase, x, y, val, gval, gx, gy);
+      }
+      if ((gval == 0.f) & (gx == 0.f) & (gy == 0.f)) continue;
+      // plane (intersections.py:23-35): p = o + t r, t = ns.(C - o) / ns.r, ns = z
+      const V3 gpl = mk(gx, gy, 0.f);  // dL/dp
+      const float dLdt = dot(gpl, r);
+      V3 a = mk(gpl.x, gpl.y, -(dLdt * inv_nd));                   // dL/do through the plane
+      const V3 gr = mk(tpl * gpl.x, tpl * gpl.y, -(dLdt * tpl * inv_nd));  // dL/dr through the plane
+      // val = v (-c) iw ; r = d - 2 c n'
+      const float dLdc = -gval * v * iw - 2.f * dot(gr, nn);
+      const V3 b = (-2.f * c) * gr + dLdc * d;  // dL/dn'
+      const V3 gd = gr + dLdc * nn;             // dL/dd
+      V3 gs;
+      if (SRC == IACT_SRC_POINT) {
+        const V3 gw = inv_len * (gd - dot(d, gd) * d);  // d = w/|w|
+        a = a + gw;
+        gs = mk(-gw.x, -gw.y, -gw.z);
+      } else {
+        gs = gd;
+      }
+      // facet buckets: H += a (tp - pos)^T + b n'^T ; dL/dpos = a
+      const V3 pr = tp - fpos;
+      acc.H[0] += a.x * pr.x + b.x * nn.x; acc.H[1] += a.x * pr.y + b.x * nn.y; acc.H[2] += a.x * pr.z + b.x * nn.z;
+      acc.H[3] += a.y * pr.x + b.y * nn.x; acc.H[4] += a.y * pr.y + b.y * nn.y; acc.H[5] += a.y * pr.z + b.y * nn.z;
+      acc.H[6] += a.z * pr.x + b.z * nn.x; acc.H[7] += a.z * pr.y + b.z * nn.y; acc.H[8] += a.z * pr.z + b.z * nn.z;
+      acc.gp[0] += a.x; acc.gp[1] += a.y; acc.gp[2] += a.z;
+      acc.gsrc[0] += gs.x; acc.gsrc[1] += gs.y; acc.gsrc[2] += gs.z;
+      acc.gv += gval * -c * iw;
+    }
+    flush_src(acc, p.gsrc, s);  // the next pair has another source (or this warp ends)
+    cl = 0;
+    ++q;
+    if (++sl == SBc) {
+      sl = 0;
+      ++fl;
+    }
+  }
+  if (cur_f >= 0) flush_facet_hard(acc, p.gfacet, cur_f);
+}
+
+// Per facet: dL/dR = H R, then dL/d(tip, tilt, rot) in degrees with// Per facet: dL/dR = H R, then dL/d(tip, tilt, rot) in degrees with
 // R = Rz(rot) Ry(tilt) Rx(tip) (core/transforms.py:72-107); per source the
 // FP64 sums to float.
 // cs = (cos, sin) of tip, tilt and rot in radians

@@ -91,18 +91,15 @@ __global__ void __launch_bounds__(256) k_masks(const RenderK p, uint32_t* out) {
   pair_masks<SRC>(p, ob, (long long)blockIdx.x * blockDim.x + threadIdx.x, (long long)gridDim.x * blockDim.x, out);
 }
 
-// k_render for the common hard-pixel case (render_tile_hard): the host picks
-// it when the launch qualifies (single stage, point or parallel sources,
-// axis-aligned sensor, rows and hexagon table in shared memory, candidate
-// words per pair from k_masks). Shared memory: tables, hexagon table, rows.
-// A response tile flushes its rows; an image's one row is flushed every
-// p.flush_tiles tiles and when the CTA runs out of tiles, so small image
-// tiles (balance) cost no flush each.
-template <int SRC, int MODE, bool HEX>
-__global__ void __launch_bounds__(256, IACT_RENDER_MIN_CTAS) k_render_hard(const RenderK p) {
+// Shared-memory layout and persistent tile loop of the specialised kernels
+// (k_render_hard, k_render_soft): tables, hexagon table, FP32 rows. A
+// response tile flushes its rows itself; an image's one row is flushed
+// every p.flush_tiles tiles and when the CTA runs out of tiles. The tile
+// index is double-buffered: an image tile ends without a barrier, so thread
+// 0 may fetch the next index while a slow warp still reads this one.
+template <int MODE, bool HEX, typename Body>
+__device__ __forceinline__ void rows_tile_loop(const RenderK& p, Body body) {
   extern __shared__ __align__(16) float smem[];
-  // tile index, double-buffered: an image tile ends without a barrier, so
-  // thread 0 may fetch the next index while a slow warp still reads this one
   __shared__ int s_tile[2];
   const int tab_n = (p.n_table_floats + 3) & ~3;
   const int htab_n = HEX ? ((p.sn.table_q * p.sn.table_r + 7) & ~7) : 0;  // int16 entries
@@ -127,8 +124,28 @@ __global__ void __launch_bounds__(256, IACT_RENDER_MIN_CTAS) k_render_hard(const
       __syncthreads();
     }
     if (tile >= p.n_tiles) break;
-    render_tile_hard<SRC, MODE, HEX>(p, ob, htab, sh_hist, tile);
+    body(ob, htab, sh_hist, tile);
   }
+}
+
+// k_render for the common hard-pixel case (render_tile_hard): the host picks
+// it when the launch qualifies (single stage, point or parallel sources,
+// axis-aligned sensor, rows and hexagon table in shared memory, candidate
+// words per pair from k_masks).
+template <int SRC, int MODE, bool HEX>
+__global__ void __launch_bounds__(256, IACT_RENDER_MIN_CTAS) k_render_hard(const RenderK p) {
+  rows_tile_loop<MODE, HEX>(p, [&](const Obst& ob, const short* htab, float* rows, int tile) {
+    render_tile_hard<SRC, MODE, HEX>(p, ob, htab, rows, tile);
+  });
+}
+
+// k_render for the common soft-pixel case (render_tile_soft): as
+// k_render_hard, also for extended sources.
+template <int SRC, int MODE, bool HEX>
+__global__ void __launch_bounds__(256, IACT_RENDER_MIN_CTAS) k_render_soft(const RenderK p) {
+  rows_tile_loop<MODE, HEX>(p, [&](const Obst& ob, const short* htab, float* rows, int tile) {
+    render_tile_soft<SRC, MODE, HEX>(p, ob, htab, rows, tile);
+  });
 }
 
 // FP64 accumulator -> FP32 output
@@ -333,7 +350,9 @@ int launch_masks(int src_type, const RenderK& p, uint32_t* out, cudaStream_t st)
   if (n <= 0) return IACT_OK;
   const size_t smem = sizeof(float) * (size_t)std::max(p.n_table_floats, 1);
   void (*kern)(const RenderK, uint32_t*) =
-      src_type == IACT_SRC_POINT ? k_masks<IACT_SRC_POINT> : k_masks<IACT_SRC_PARALLEL>;
+      src_type == IACT_SRC_POINT      ? k_masks<IACT_SRC_POINT>
+      : src_type == IACT_SRC_EXTENDED ? k_masks<IACT_SRC_EXTENDED>
+                                      : k_masks<IACT_SRC_PARALLEL>;
   int per_sm = 0;
   int rc = resident_ctas(reinterpret_cast<const void*>(kern), 256, smem, &per_sm);
   if (rc) return rc;
@@ -381,6 +400,23 @@ int run_render_hard(int src_type, int mode, bool hex, RenderK p, int block, size
       kern = hex ? k_render_hard<IACT_SRC_PARALLEL, IACT_MODE_IMAGE, true> : k_render_hard<IACT_SRC_PARALLEL, IACT_MODE_IMAGE, false>;
   }
   return run_persistent(kern, p, block, smem, st, ev);
+}
+
+// the common soft-pixel case (k_render_soft)
+template <int SRC>
+int run_render_soft_src(int mode, bool hex, RenderK p, int block, size_t smem, cudaStream_t st, void* const* ev) {
+  void (*kern)(const RenderK);
+  if (mode == IACT_MODE_RESPONSE)
+    kern = hex ? k_render_soft<SRC, IACT_MODE_RESPONSE, true> : k_render_soft<SRC, IACT_MODE_RESPONSE, false>;
+  else
+    kern = hex ? k_render_soft<SRC, IACT_MODE_IMAGE, true> : k_render_soft<SRC, IACT_MODE_IMAGE, false>;
+  return run_persistent(kern, p, block, smem, st, ev);
+}
+int run_render_soft(int src_type, int mode, bool hex, RenderK p, int block, size_t smem, cudaStream_t st,
+                    void* const* ev) {
+  if (src_type == IACT_SRC_POINT) return run_render_soft_src<IACT_SRC_POINT>(mode, hex, p, block, smem, st, ev);
+  if (src_type == IACT_SRC_EXTENDED) return run_render_soft_src<IACT_SRC_EXTENDED>(mode, hex, p, block, smem, st, ev);
+  return run_render_soft_src<IACT_SRC_PARALLEL>(mode, hex, p, block, smem, st, ev);
 }
 
 template <int SRC, bool SOFT, int MODE>
@@ -541,10 +577,11 @@ int launch_render(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type,
   // at 5 tiles per SM, 256 us at 10)
   const bool soft = (sn->type == IACT_SENSOR_SOFT_SQUARE || sn->type == IACT_SENSOR_SOFT_HEX);
   const bool stages = sc->n_mirrors > 0;
-  // the common hard-pixel case runs k_render_hard, with the candidate word of
-  // every (source, facet) pair from k_masks
-  const bool hard = !soft && !stages && (src_type == IACT_SRC_POINT || src_type == IACT_SRC_PARALLEL) &&
-                    p.sn.axes && (sn->type == IACT_SENSOR_SQUARE || sn->type == IACT_SENSOR_HEX) &&
+  // the common cases run k_render_hard (hard pixels, point or parallel
+  // sources) or k_render_soft (soft pixels, also extended sources), with the
+  // candidate word of every (source, facet) pair from k_masks
+  const bool hard = !stages && p.sn.axes &&
+                    (soft || src_type == IACT_SRC_POINT || src_type == IACT_SRC_PARALLEL) &&
                     ((p.n_words == 1 && L.n_masks > 0) || n_primitives(sc) == 0) &&
                     !(opts && opts->hist_mode == 2);
   // image renders of k_render_hard keep their FP32 row across tiles and need
@@ -552,7 +589,7 @@ int launch_render(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type,
   // launch: 1000-sample plain forward 51.5 us at 12 tiles per SM vs 57.4 at
   // 16 and 56.2 at 4)
   const long long tiles_per_sm =
-      (hard && mode == IACT_MODE_IMAGE) ? 12 : (sc->n_mirrors > 0 ? 8 : (n_primitives(sc) > 32 ? 10 : 4));
+      (hard && !soft && mode == IACT_MODE_IMAGE) ? 12 : (sc->n_mirrors > 0 ? 8 : (n_primitives(sc) > 32 ? 10 : 4));
   rc = plan_tiles(p, mode, block, opts, tiles_per_sm * std::max(di.sm_count, 1));
   if (rc) return rc;
   const size_t smem_max = (size_t)std::min(di.smem_optin > 0 ? di.smem_optin : 49152, 200 * 1024);
@@ -562,7 +599,8 @@ int launch_render(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type,
   if (hard) {
     rc = plan_smem(sn, L.n_table_floats, p.SB, mode, opts ? opts->hist_mode : 0, smem_max, 0, 0, sp);
     if (rc) return rc;
-    use_hard = sp.rows_in_smem > 0 && (sn->type == IACT_SENSOR_SQUARE || sp.hex_in_smem);
+    use_hard = sp.rows_in_smem > 0 &&
+               (sn->type == IACT_SENSOR_SQUARE || sn->type == IACT_SENSOR_SOFT_SQUARE || sp.hex_in_smem);
     smem = sp.tab_bytes + sp.htab_bytes + sp.hist_bytes;
   }
   if (!use_hard) {  // k_render: candidate masks of a tile's tasks in shared memory
@@ -584,11 +622,14 @@ int launch_render(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type,
       rc = launch_masks(src_type, p, reinterpret_cast<uint32_t*>(w + L.masks), st);
       if (rc) return rc;
     }
-    // an image row sums about 16k rays between flushes to the FP64 accumulator
+    // an image row sums about 16k rays (hard pixels) or 12k rays of taps
+    // (soft pixels, as many as a tile of the generic kernel) between flushes
+    // to the FP64 accumulator
     const int tile_tasks = p.SB * p.FC * p.CC;
-    p.flush_tiles = std::max(1, 512 / std::max(tile_tasks, 1));
+    p.flush_tiles = std::max(1, (soft ? 384 : 512) / std::max(tile_tasks, 1));
     void* const ev_end[2] = {nullptr, ev ? ev[1] : nullptr};
-    rc = run_render_hard(src_type, mode, sn->type == IACT_SENSOR_HEX, p, block, smem, st, ev_end);
+    if (soft) rc = run_render_soft(src_type, mode, sn->type == IACT_SENSOR_SOFT_HEX, p, block, smem, st, ev_end);
+    else rc = run_render_hard(src_type, mode, sn->type == IACT_SENSOR_HEX, p, block, smem, st, ev_end);
   } else if (src_type == IACT_SRC_POINT) {
     rc = dispatch_soft<IACT_SRC_POINT>(soft, mode, stages, p, block, smem, st, ev);
   } else if (src_type == IACT_SRC_EXTENDED) {

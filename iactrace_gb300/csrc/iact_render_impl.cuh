@@ -212,8 +212,15 @@ struct Sink {
   }
 };
 
+// Hits into FP32 shared-memory rows only (the soft-pixel kernel's sink).
+struct RowSink {
+  float* sh;
+  __device__ __forceinline__ void add(int key, float v) const { atomicAdd(sh + key, v); }
+};
+
 // all 32 lanes call; key < 0 or v == 0 means nothing to add for this lane
-__device__ __forceinline__ void warp_add(const Sink& sink, int key, float v) {
+template <typename SK>
+__device__ __forceinline__ void warp_add(const SK& sink, int key, float v) {
   const int k0 = __shfl_sync(kFull, key, 0);
   if (__all_sync(kFull, key == k0)) {
 #pragma unroll
@@ -227,7 +234,8 @@ __device__ __forceinline__ void warp_add(const Sink& sink, int key, float v) {
 // sensors/square.py:144-172 DifferentiableSquareSensor.accumulate, one ray
 // (all lanes call; inactive lanes pass ok = false). Rays whose plane hit is
 // the 1e10 sentinel deposit nothing.
-__device__ __forceinline__ void splat_square(const SensorK& s, const Sink& sink, int rowbase, bool ok,
+template <typename SK>
+__device__ __forceinline__ void splat_square(const SensorK& s, const SK& sink, int rowbase, bool ok,
                                              float x, float y, float v) {
   ok = ok && (x < 1e9f) && (y < 1e9f);
   float xp = (x - s.x0) * s.inv_dx, yp = (y - s.y0) * s.inv_dy;
@@ -257,8 +265,8 @@ __device__ __forceinline__ void splat_square(const SensorK& s, const Sink& sink,
 // (all lanes call; inactive lanes pass ok = false). The tap weights of the
 // one-ring kernel (kernel_size 1, the reference default) stay in registers
 // between the normalisation and the deposit; larger kernels recompute them.
-template <typename TT>
-__device__ __forceinline__ void splat_hex(const SensorK& s, const TT* table, const Sink& sink,
+template <typename TT, typename SK>
+__device__ __forceinline__ void splat_hex(const SensorK& s, const TT* table, const SK& sink,
                                           int rowbase, bool ok, float x, float y, float v) {
   ok = ok && (x < 1e9f) && (y < 1e9f);
   float xg, yg, qi, ri;
@@ -588,6 +596,87 @@ __device__ __forceinline__ bool shadow_word(const Obst& ob, uint32_t m, V3 o, V3
     sh |= tri_shadows(ob.tri + k * kTriF, o, d);
   }
   return sh;
+}
+
+// Soft-pixel tile body of the common case (sensors/square.py:144-172,
+// sensors/hexagonal.py:264-315 deposits): a single-stage scene, point,
+// parallel or extended sources, a sensor whose rotation is the identity,
+// the rows and (hexagons) the lookup table in shared memory, candidate
+// words per (source, facet) pair from k_masks (or no primitives). The per-ray
+// arithmetic is render_tile<SRC, true, MODE, false, AX>'s (the same trace,
+// splat and warp-aggregated adds); the sensor kind and the row sink are
+// compile-time, per-pair values (source, its jitter basis, value, candidate
+// word) are loaded once per pair, and lanes past a facet's last sample
+// trace its last sample with value 0. Response rows are flushed per tile,
+// an image row as render_tile_hard's.
+template <int SRC, int MODE, bool HEX>
+__device__ __forceinline__ void render_tile_soft(const RenderK& p, const Obst& ob, const short* htab,
+                                                 float* sh_hist, int tile) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  const int nch = (p.M + 31) >> 5;
+  const int per_s = p.n_fchunk * p.n_cchunk;
+  const int sblk = tile / per_s;
+  const int fc = (tile - sblk * per_s) / p.n_cchunk;
+  const int cc = tile - sblk * per_s - fc * p.n_cchunk;
+  const int s0 = sblk * p.SB, f0 = fc * p.FC, c0 = cc * p.CC;
+  const int SBc = min(p.SB, p.S - s0), FCc = min(p.FC, p.F - f0), CCc = min(p.CC, nch - c0);
+  const RowSink sink{sh_hist};
+  constexpr int SS = (SRC == IACT_SRC_EXTENDED) ? 4 : 3;
+  const int T = SBc * FCc * CCc;
+  const int tb = (warp * T) / nw, te = ((warp + 1) * T) / nw;
+  int q = tb / CCc;  // pair index sl * FCc + fl
+  int sl = q / FCc, fl = q - sl * FCc;
+  int cl = tb - q * CCc;
+  const int mlast = p.M - 1;
+  for (int t = tb; t < te;) {
+    const int s = s0 + sl, f = f0 + fl;
+    const int ce = min(CCc, cl + (te - t));
+    t += ce - cl;
+    const V3 src = mk(__ldg(p.sources + SS * s), __ldg(p.sources + SS * s + 1), __ldg(p.sources + SS * s + 2));
+    const float sig = (SRC == IACT_SRC_EXTENDED) ? __ldg(p.sources + SS * s + 3) : 0.f;
+    const float v = __ldg(p.values + s);
+    const uint32_t word = p.gmask ? __ldg(p.gmask + (size_t)s * p.F + f) : 0u;  // pair's candidates (k_masks)
+    const int rowbase = (MODE == IACT_MODE_RESPONSE) ? sl * p.P : 0;
+    const int fbase = f * p.M;
+    JBasis jb;
+    if (SRC == IACT_SRC_EXTENDED) jb = jitter_basis(src);
+    for (; cl < ce; ++cl) {
+      const int m = (c0 + cl) * 32 + lane;
+      const bool act = m < p.M;
+      const float4 P = __ldg(p.P4 + fbase + (act ? m : mlast)), N = __ldg(p.N4 + fbase + (act ? m : mlast));
+      const V3 tp = mk(P.x, P.y, P.z), tn = mk(N.x, N.y, N.z);
+      V3 d;
+      if (SRC == IACT_SRC_POINT) {
+        V3 dd = tp - src;  // dirs = normalize(tp - src)
+        d = rsqrtf(dot(dd, dd)) * dd;
+      } else if (SRC == IACT_SRC_EXTENDED) {
+        float z0, z1;
+        ray_normals(p.seed, s, f, act ? m : mlast, z0, z1);
+        d = jitter_dir(jb, sig, z0, z1);
+      } else {
+        d = src;
+      }
+      bool sh = false;
+      if (word) sh = shadow_word(ob, word, tp, mk(-d.x, -d.y, -d.z));  // warp-uniform
+      const float c = dot(d, tn);                                       // core/reflection.py:5-20
+      const V3 r = d - (2.f * c) * tn;
+      const float val = (v * -c * P.w) * (sh ? 0.f : 1.f);  // values * cos / tw * shadow
+      float x, y;
+      plane_hit<true>(p.sn, tp, r, x, y);
+      if (HEX) splat_hex(p.sn, htab, sink, rowbase, act, x, y, val);
+      else splat_square(p.sn, sink, rowbase, act, x, y, val);
+    }
+    cl = 0;
+    ++q;
+    if (++fl == FCc) {
+      fl = 0;
+      ++sl;
+    }
+  }
+  if (MODE == IACT_MODE_RESPONSE) {
+    __syncthreads();
+    flush_rows(p, sh_hist, s0, SBc);
+  }
 }
 
 // Hard-pixel tile body of the common case: a single-stage scene, point or
