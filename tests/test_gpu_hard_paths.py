@@ -1,9 +1,10 @@
-"""The hard-pixel kernels equal the generic ones.
+"""The specialised kernels equal the generic ones.
 
-Hard-pixel renders of single-stage scenes with at most 32 shadowing
-primitives run k_render_hard (candidate words per (source, facet) pair from
-k_masks), their adjoints k_adjoint_hard, and batch classes whose jobs all
-qualify the batched forms of both. Everything else runs the generic
+Renders of single-stage scenes with at most 32 shadowing primitives and an
+axis-aligned sensor run k_render_hard (hard pixels) or k_render_soft (soft
+pixels, also extended sources), with candidate words per (source, facet)
+pair from k_masks; their adjoints k_adjoint_hard / k_adjoint_soft; batch
+classes whose jobs all qualify the batched hard-pixel forms. Everything else runs the generic
 kernels. Both evaluate the same per-ray arithmetic, so on the same scene
 they must give the same outputs up to the order of the sums: the generic
 kernel is forced here by options the hard path does not take (histogram
@@ -18,8 +19,11 @@ import ctypes
 import pytest
 import torch
 
+import numpy as np
+
 import iactrace_gb300 as it
-from iactrace_gb300 import _native as N, Telescope, workloads as W
+from iactrace_gb300 import _native as N, Telescope, alignment as A, workloads as W
+from iactrace_gb300.sensors import DifferentiableHexagonalSensor, DifferentiableSquareSensor
 from iactrace_gb300.core.render import source_code
 from iactrace_gb300.core.scene import pack_scene
 
@@ -40,23 +44,35 @@ def _scenes():
     tel, src, val, _ = resp
     bare = (Telescope(tel.mirror_groups, [], tel.sensors), src, val, "point")  # no primitives
     par = (tel, -src / src.norm(dim=1, keepdim=True), val, "parallel")
-    return {"plain": plain, "response_hex": resp, "no_obstructions": bare, "parallel": par}
+    soft_sq = DifferentiableSquareSensor([0.0, 0.0, 15.0], [0.0, 0.0, 0.0], 32, 30, (-0.672, 0.672, -0.63, 0.63),
+                                         sigma=0.5, kernel_size=2)
+    soft_hx = DifferentiableHexagonalSensor([0.0, 0.0, 15.0], [0.0, 0.0, 0.0],
+                                            W.hex_grid(2048, 0.042).astype(np.float32), sigma=0.5, kernel_size=1)
+    ptel, psrc, pval, _ = plain
+    ext = A.extended_sources(8, max_deg=2.0, seed=7)
+    return {"plain": plain, "response_hex": resp, "no_obstructions": bare, "parallel": par,
+            "soft_square": (Telescope(ptel.mirror_groups, ptel.obstruction_groups, [soft_sq]), psrc, pval, "point"),
+            "soft_hex_extended": (Telescope(tel.mirror_groups, tel.obstruction_groups, [soft_hx]), ext,
+                                  torch.ones(8), "extended")}
 
 
-@pytest.mark.parametrize("name", ["plain", "response_hex", "no_obstructions", "parallel"])
+SCENES = ["plain", "response_hex", "no_obstructions", "parallel", "soft_square", "soft_hex_extended"]
+
+
+@pytest.mark.parametrize("name", SCENES)
 @pytest.mark.parametrize("mode", ["image", "response"])
 def test_hard_render_equals_generic(cuda, name, mode):
     tel, src, val, st = _scenes()[name]
     src, val = src.to(cuda), val.to(cuda)
     fn = it.render_response_matrix if mode == "response" else it.render
-    a = fn(tel, src, val, st).double()
-    b = fn(tel, src, val, st, opts=_generic_opts()).double()
+    a = fn(tel, src, val, st, seed=11).double()
+    b = fn(tel, src, val, st, opts=_generic_opts(), seed=11).double()
     assert float(b.abs().sum()) > 0
     bad = (a - b).abs() > SUM_TOL * b.abs() + 1e-12 * float(b.abs().max())
     assert int(bad.sum()) == 0, f"{int(bad.sum())} of {b.numel()} entries differ beyond {SUM_TOL}"
 
 
-def _backward(lib, ps, sd, code, src, val, mode, gout, scale):
+def _backward(lib, ps, sd, code, src, val, mode, gout, scale, seed=0):
     """iact_render_backward through the C ABI: facet rotations and positions,
     sources, values; with `scale` also the roughness scales (which the hard
     adjoint does not take, so the generic kernel runs)."""
@@ -65,15 +81,21 @@ def _backward(lib, ps, sd, code, src, val, mode, gout, scale):
     ws = torch.empty(ps.workspace_bytes(sd, S, N.MODE_BACKWARD), dtype=torch.uint8, device=dev)
     g = [torch.zeros((ps.F, 3), device=dev), torch.zeros((ps.F, 3), device=dev), torch.zeros(ps.F, device=dev),
          torch.zeros((S, 3), device=dev), torch.zeros(S, device=dev)]
+    ext = code == N.SRC_EXTENDED  # no source gradients for extended sources
+    opts = N.IactOpts()
+    opts.seed = seed
     N.check(lib.iact_render_backward(ctypes.byref(ps.desc), ctypes.byref(sd), code, src.data_ptr(), val.data_ptr(),
                                      S, mode, gout.data_ptr(), g[0].data_ptr(), g[1].data_ptr(),
-                                     g[2].data_ptr() if scale else None, g[3].data_ptr(), g[4].data_ptr(), None,
-                                     None, None, None, ws.data_ptr(), ws.numel(), None,
-                                     torch.cuda.current_stream(dev).cuda_stream))
-    return {"rot": g[0], "pos": g[1], "src": g[3], "val": g[4]}
+                                     g[2].data_ptr() if scale else None, None if ext else g[3].data_ptr(),
+                                     g[4].data_ptr(), None, None, None, None, ws.data_ptr(), ws.numel(),
+                                     ctypes.byref(opts), torch.cuda.current_stream(dev).cuda_stream))
+    out = {"rot": g[0], "pos": g[1], "val": g[4]}
+    if not ext:
+        out["src"] = g[3]
+    return out
 
 
-@pytest.mark.parametrize("name", ["plain", "response_hex", "no_obstructions", "parallel"])
+@pytest.mark.parametrize("name", SCENES)
 @pytest.mark.parametrize("mode", ["image", "response"])
 def test_hard_adjoint_equals_generic(cuda, name, mode):
     tel, src, val, st = _scenes()[name]
@@ -82,11 +104,11 @@ def test_hard_adjoint_equals_generic(cuda, name, mode):
     ps = pack_scene(tel, cuda)
     sd, keep = tel.sensors[0].pack(cuda)
     fn = it.render_response_matrix if mode == "response" else it.render
-    out = fn(tel, src, val, st)
+    out = fn(tel, src, val, st, seed=11)
     gout = torch.randn(out.shape, device=cuda, generator=torch.Generator(device=cuda).manual_seed(3)).contiguous()
     nm = N.MODE_RESPONSE if mode == "response" else N.MODE_IMAGE
-    hard = _backward(lib, ps, sd, source_code(st), src, val, nm, gout, scale=False)
-    generic = _backward(lib, ps, sd, source_code(st), src, val, nm, gout, scale=True)
+    hard = _backward(lib, ps, sd, source_code(st), src, val, nm, gout, scale=False, seed=11)
+    generic = _backward(lib, ps, sd, source_code(st), src, val, nm, gout, scale=True, seed=11)
     for k in hard:
         a, b = hard[k].double(), generic[k].double()
         nb = float(b.norm())
