@@ -9,6 +9,7 @@ from __future__ import annotations
 
 import ctypes
 import math
+import operator
 
 import torch
 
@@ -278,6 +279,10 @@ def _object_ids(tel, sensor):
             tuple(map(id, tel.obstruction_groups or ())), tuple(map(id, sensor.__dict__.values())))
 
 
+_VERSION = operator.attrgetter("_version")
+_REQUIRES_GRAD = operator.attrgetter("requires_grad")
+
+
 def _tensor_fields(tel, sensor):
     """The tensors among the mirror groups' and the sensor's fields."""
     return tuple(v for g in tel.mirror_groups for v in g.__dict__.values() if isinstance(v, torch.Tensor)) + \
@@ -298,9 +303,9 @@ def _fast_forward(tel, sensor, sensor_idx, src, val, code, mode, shape, opts, de
     hit = cache.get(ck)
     if hit is not None and hit[0] == _object_ids(tel, sensor):
         tens = hit[1]
-        if any(t.requires_grad for t in tens):
+        if any(map(_REQUIRES_GRAD, tens)):
             return None
-        if tuple(t._version for t in tens) != hit[2]:
+        if tuple(map(_VERSION, tens)) != hit[2]:
             hit = None
     else:
         hit = None
@@ -312,7 +317,7 @@ def _fast_forward(tel, sensor, sensor_idx, src, val, code, mode, shape, opts, de
         ws_bytes = max(ps.workspace_bytes(sdesc, int(src.shape[0]), mode), 256)
         # after packing: the packing caches stored on the sensor are part of its fields
         tens = _tensor_fields(tel, sensor)
-        hit = (_object_ids(tel, sensor), tens, tuple(t._version for t in tens), ps,
+        hit = (_object_ids(tel, sensor), tens, tuple(map(_VERSION, tens)), ps,
                (ps.facet_rot, ps.facet_pos, ps.facet_scale), sdesc, keep, ws_bytes)
         cache[ck] = hit
     ps, facets, sdesc, keep, ws_bytes = hit[3:]
