@@ -150,3 +150,20 @@ def test_batched_hard_classes_equal_generic(cuda):
                 continue
             err = float((da[k].double() - db[k].double()).norm()) / nb
             assert err <= 1e-5, f"{k}: relative L2 {err:.3g}"
+
+
+def test_render_beyond_the_pair_word_cap(cuda):
+    """An image render of more than 2^26 (source, facet) pairs keeps per-tile
+    masks (generic kernel); it equals the sum of the same render split into
+    two halves of the sources, each of which takes the pair words."""
+    tel, _, _, st = W.plain_forward(n_samples=1, n_sources=1)
+    F = 380
+    S = (1 << 26) // F + 64
+    src = W.point_sources_disk(S, 2.5, 9).to(cuda)
+    val = (0.5 + torch.rand(S, generator=torch.Generator().manual_seed(10))).to(cuda)
+    whole = it.render(tel, src, val, st).double()
+    h = S // 2
+    halves = (it.render(tel, src[:h], val[:h], st).double() + it.render(tel, src[h:], val[h:], st).double())
+    assert float(whole.abs().sum()) > 0
+    err = float((whole - halves).norm() / halves.norm())
+    assert err <= 1e-6, f"relative L2 {err:.3g} between the capped render and its halves"
