@@ -40,7 +40,7 @@ from test_gpu_forward import IMG_TOL, RAW_TOL, check_image, check_rays, cont_val
 
 SAME_TOL = 1e-6  # same rays and bins, other summation order (tiles, batch)
 GRAD_TOL = 1e-4  # gradients against their linear identity
-SOFT_TOL = 1e-5  # soft-sensor images against the FP64 oracle (the benchmark spec's image gate)
+SOFT_TOL = 1e-5  # soft-sensor images against the FP64 oracle (the image gate: 1e-5 against FP64)
 
 pytestmark = pytest.mark.gpu
 

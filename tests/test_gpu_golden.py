@@ -10,7 +10,7 @@ float64 runs on the same sampled arrays), through the C ABI.
   - per ray, the GPU's hard pixel id equals the pixel id the reference's own
     accumulate gave its float32 hit, except for rays whose FP64 hit lies
     within EDGE_BAND = 4e-6 m of a pixel edge; the count of mismatches with
-    an edge margin between 1e-6 m and 4e-6 m is printed. The benchmark spec's
+    an edge margin between 1e-6 m and 4e-6 m is printed. The stated parity
     band is 1e-6 m; the float32 reference chain itself moves hits by up to
     ~3e-6 m against FP64 (one-ulp sin/cos differences of a facet rotation
     tilt the normal by ~6e-8 rad, ~2e-6 m after reflection over 15 m), so
