@@ -40,6 +40,8 @@ template <int SRC, bool SOFT, int MODE, bool STAGES, bool AX = false, bool DEEP 
 __global__ void __launch_bounds__(256, STAGES ? 2 : (SOFT ? 3 : 4)) k_adjoint(const AdjK p) {
   extern __shared__ __align__(16) float smem[];
   __shared__ int s_tile;
+  grid_dep_wait();  // the prep launch's tables, samples and zeroed buckets
+  grid_dep_launch();
   const int tab_n = (p.n_table_floats + 3) & ~3;
   const int htab_n = p.hex_in_smem ? ((p.sn.table_q * p.sn.table_r + 7) & ~7) : 0;
   float* tab = smem;
@@ -81,6 +83,8 @@ __device__ __forceinline__ void adj_tile_loop(const AdjK& p, Body body) {
   float* tab = smem;
   short* htab = reinterpret_cast<short*>(smem + tab_n);
   const int nthr = blockDim.x;
+  grid_dep_wait();  // the prep and mask launches' results
+  grid_dep_launch();
   for (int i = threadIdx.x; i < p.n_table_floats; i += nthr) tab[i] = p.tables[i];
   for (int i = threadIdx.x; i < htab_n; i += nthr)
     htab[i] = (short)(i < p.sn.table_q * p.sn.table_r ? p.hex_table[i] : -1);
@@ -114,12 +118,15 @@ __global__ void __launch_bounds__(256, 3) k_adjoint_soft(const AdjK p) {
 
 __global__ void k_adjoint_mirrors(const double* gmir, const iact_mirror_t* mirrors, int n_mir, float* g_rot,
                                   float* g_pos, float* g_surf) {
+  grid_dep_wait();  // the adjoint's buckets
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n_mir) adjoint_mirror_item(i, gmir, mirrors, g_rot, g_pos, g_surf);
 }
 
 __global__ void k_adjoint_finish(const double* gfacet, const double* gsrc, const float* facet_rot, int F, int S,
                                  float* g_rot, float* g_pos, float* g_scale, float* g_src, float* g_val) {
+  grid_dep_wait();  // the adjoint's buckets
+  grid_dep_launch();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   adjoint_finish_item(i, gfacet, gsrc, facet_rot, F, S, g_rot, g_pos, g_scale, g_src, g_val);
 }
@@ -138,8 +145,7 @@ int run_adjoint(const AdjK& p, int block, size_t smem, cudaStream_t st) {
   if (rc) return rc;
   if (per_sm < 1) return set_error(IACT_E_UNSUPPORTED, "adjoint kernel does not fit on an SM");
   const int grid = std::max(1, std::min(p.n_tiles, per_sm * device_info().sm_count));
-  kern<<<grid, block, smem, st>>>(p);
-  return check_cuda(cudaGetLastError(), "k_adjoint launch");
+  return check_cuda(launch_after(kern, dim3(grid), dim3(block), smem, st, p), "k_adjoint launch");
 }
 
 template <int SRC, bool SOFT, bool STAGES, bool DEEP = false>
@@ -177,8 +183,7 @@ int run_adjoint_hard(int src_type, int mode, bool hex, const AdjK& p, int block,
   if (rc) return rc;
   if (per_sm < 1) return set_error(IACT_E_UNSUPPORTED, "adjoint kernel does not fit on an SM");
   const int grid = std::max(1, std::min(p.n_tiles, per_sm * device_info().sm_count));
-  kern<<<grid, block, smem, st>>>(p);
-  return check_cuda(cudaGetLastError(), "k_adjoint launch");
+  return check_cuda(launch_after(kern, dim3(grid), dim3(block), smem, st, p), "k_adjoint launch");
 }
 
 // the common soft-pixel case (k_adjoint_soft)
@@ -194,8 +199,7 @@ int run_adjoint_soft_src(int mode, bool hex, const AdjK& p, int block, size_t sm
   if (rc) return rc;
   if (per_sm < 1) return set_error(IACT_E_UNSUPPORTED, "adjoint kernel does not fit on an SM");
   const int grid = std::max(1, std::min(p.n_tiles, per_sm * device_info().sm_count));
-  kern<<<grid, block, smem, st>>>(p);
-  return check_cuda(cudaGetLastError(), "k_adjoint launch");
+  return check_cuda(launch_after(kern, dim3(grid), dim3(block), smem, st, p), "k_adjoint launch");
 }
 int run_adjoint_soft(int src_type, int mode, bool hex, const AdjK& p, int block, size_t smem, cudaStream_t st) {
   if (src_type == IACT_SRC_POINT) return run_adjoint_soft_src<IACT_SRC_POINT>(mode, hex, p, block, smem, st);
@@ -353,14 +357,15 @@ int launch_backward(const iact_scene_t* sc, const iact_sensor_t* sn, int src_typ
   if (n > 0) {
     // FP64 trigonometry per facet (GB300: 2 FP64 FMAs per clock per SM):
     // one warp per block spreads the facets over the SMs
-    k_adjoint_finish<<<(n + 31) / 32, 32, 0, st>>>(gfacet, gsrc, sc->facet_rot, F, S, g_rot, g_pos, g_scale,
-                                                      g_src, g_val);
-    rc = check_cuda(cudaGetLastError(), "k_adjoint_finish launch");
+    rc = check_cuda(launch_after(k_adjoint_finish, dim3((n + 31) / 32), dim3(32), 0, st, gfacet, gsrc,
+                                 sc->facet_rot, F, S, g_rot, g_pos, g_scale, g_src, g_val),
+                    "k_adjoint_finish launch");
     if (rc) return rc;
   }
   if (n_mir > 0 && (g_mrot || g_mpos || g_msurf)) {
-    k_adjoint_mirrors<<<(n_mir + 63) / 64, 64, 0, st>>>(gmir, sc->mirrors, n_mir, g_mrot, g_mpos, g_msurf);
-    rc = check_cuda(cudaGetLastError(), "k_adjoint_mirrors launch");
+    rc = check_cuda(launch_after(k_adjoint_mirrors, dim3((n_mir + 63) / 64), dim3(64), 0, st, gmir, sc->mirrors,
+                                 n_mir, g_mrot, g_mpos, g_msurf),
+                    "k_adjoint_mirrors launch");
   }
   return rc;
 }

@@ -18,6 +18,18 @@ constexpr float kBig = 1e10f;  // the reference's miss / shadow sentinel
 constexpr float kEps = 1e-8f;
 constexpr unsigned kFull = 0xffffffffu;
 
+// ------------------------------------------- programmatic dependent launch
+// A kernel launched with the programmatic stream serialization attribute
+// (launch_after below) may be scheduled while its predecessor on the stream
+// still runs; grid_dep_wait, before its first read of the predecessor's
+// results, waits until that grid has completed and its writes are visible.
+// For a kernel launched without the attribute both are no-ops.
+__device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+// lets the stream's next kernel (launched with the attribute) be scheduled
+// once every CTA of this grid has started; its grid_dep_wait still waits for
+// this grid to complete
+__device__ __forceinline__ void grid_dep_launch() { asm volatile("griddepcontrol.launch_dependents;" :::); }
+
 // ------------------------------------------------------------ table records
 // Sizes in floats; records are packed back to back in shared memory.
 constexpr int kCylF = 8;    // p1(3) axis(3) height r*r

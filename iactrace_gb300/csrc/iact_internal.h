@@ -17,6 +17,27 @@ namespace iact {
 int set_error(int code, const std::string& msg);
 int check_cuda(cudaError_t e, const char* what);
 
+// Launch of a kernel that follows another kernel of the same chain on
+// `st` (prep -> masks -> render -> finish; prep -> masks -> adjoint ->
+// finish) with programmatic stream serialization: it may be scheduled while
+// its predecessor runs and waits in grid_dep_wait for the predecessor's
+// results, so the launch gap between the two overlaps the predecessor.
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_after(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                                Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kern, static_cast<Args&&>(args)...);
+}
+
 // validation of the descriptors shared by every entry point
 int validate_scene(const iact_scene_t* sc);
 int validate_sensor(const iact_sensor_t* sn);

@@ -32,6 +32,7 @@
 namespace iact {
 
 __global__ void __launch_bounds__(256) k_prep(const PrepK p) {
+  grid_dep_launch();
   if (blockIdx.x == 0) prep_tables(p);
   if (p.counter && blockIdx.x == 0 && threadIdx.x < 16) p.counter[threadIdx.x] = 0;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < p.n_zero;
@@ -45,6 +46,8 @@ template <int SRC, bool SOFT, int MODE, bool STAGES>
 __global__ void __launch_bounds__(256, STAGES ? 3 : IACT_RENDER_MIN_CTAS) k_render(const RenderK p) {
   extern __shared__ __align__(16) float smem[];
   __shared__ int s_tile;
+  grid_dep_wait();  // the prep launch's tables, samples and zeroed accumulator
+  grid_dep_launch();
   const int tab_n = (p.n_table_floats + 3) & ~3;
   const int htab_n = p.hex_in_smem ? ((p.sn.table_q * p.sn.table_r + 7) & ~7) : 0;  // int16 entries
   float* tab = smem;
@@ -85,6 +88,8 @@ __global__ void __launch_bounds__(256, STAGES ? 3 : IACT_RENDER_MIN_CTAS) k_rend
 template <int SRC>
 __global__ void __launch_bounds__(256) k_masks(const RenderK p, uint32_t* out) {
   extern __shared__ __align__(16) float smem[];
+  grid_dep_wait();  // the prep launch's facet bounds and tables
+  grid_dep_launch();
   for (int i = threadIdx.x; i < p.n_table_floats; i += blockDim.x) smem[i] = p.tables[i];
   __syncthreads();
   const Obst ob = make_obst(smem, p.n_cyl, p.n_box, p.n_sph, p.n_obox, p.n_tri);
@@ -108,6 +113,8 @@ __device__ __forceinline__ void rows_tile_loop(const RenderK& p, Body body) {
   float* sh_hist = smem + tab_n + htab_n / 2;
   const int hist_n = p.rows_in_smem * p.P;
   const int nthr = blockDim.x;
+  grid_dep_wait();  // the prep and mask launches' results
+  grid_dep_launch();
 
   for (int i = threadIdx.x; i < p.n_table_floats; i += nthr) tab[i] = p.tables[i];
   for (int i = threadIdx.x; i < htab_n; i += nthr)
@@ -150,6 +157,7 @@ __global__ void __launch_bounds__(256, IACT_RENDER_MIN_CTAS) k_render_soft(const
 
 // FP64 accumulator -> FP32 output
 __global__ void __launch_bounds__(256) k_finish(const double* __restrict__ acc, float* __restrict__ out, size_t n) {
+  grid_dep_wait();  // the render's accumulator
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
     out[i] = (float)acc[i];
 }
@@ -357,8 +365,7 @@ int launch_masks(int src_type, const RenderK& p, uint32_t* out, cudaStream_t st)
   int rc = resident_ctas(reinterpret_cast<const void*>(kern), 256, smem, &per_sm);
   if (rc) return rc;
   const int grid = (int)std::min<long long>((n + 255) / 256, 65535);
-  kern<<<grid, 256, smem, st>>>(p, out);
-  return check_cuda(cudaGetLastError(), "k_masks launch");
+  return check_cuda(launch_after(kern, dim3(grid), dim3(256), smem, st, p, out), "k_masks launch");
 }
 
 // one persistent launch of a render kernel: as many CTAs as are resident
@@ -372,8 +379,7 @@ int run_persistent(void (*kern)(const RenderK), RenderK p, int block, size_t sme
   int grid = std::min(p.n_tiles, per_sm * di.sm_count);
   grid = std::max(grid, 1);
   if (ev && ev[0]) cudaEventRecord(static_cast<cudaEvent_t>(ev[0]), st);
-  kern<<<grid, block, smem, st>>>(p);
-  rc = check_cuda(cudaGetLastError(), "k_render launch");
+  rc = check_cuda(launch_after(kern, dim3(grid), dim3(block), smem, st, p), "k_render launch");
   if (ev && ev[1]) cudaEventRecord(static_cast<cudaEvent_t>(ev[1]), st);
   return rc;
 }
@@ -639,8 +645,8 @@ int launch_render(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type,
   }
   if (rc) return rc;
   const int fb = (int)std::min<size_t>((n_acc + 255) / 256, 4096);
-  k_finish<<<std::max(fb, 1), 256, 0, st>>>(p.acc, out, n_acc);
-  return check_cuda(cudaGetLastError(), "k_finish launch");
+  return check_cuda(launch_after(k_finish, dim3(std::max(fb, 1)), dim3(256), 0, st, p.acc, out, n_acc),
+                    "k_finish launch");
 }
 
 int launch_debug(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type, const float* sources,
