@@ -415,6 +415,9 @@ def run_alignment(args, rank, world):
             "alignment": {"loss_first": hist["loss"][0], "loss_last": hist["loss"][-1],
                           "rms_tilt_error_mrad_first": hist["rms_mrad"][0],
                           "rms_tilt_error_mrad_last": hist["rms_mrad"][-1], "adam_steps": steps},
+            # the library's kernels per Adam step (counted by the library around the
+            # captured step) times the timed steps
+            "gpu_launches": hist["launches_per_step"] * steps,
             "clocks": clk,
         }), flush=True)
 
@@ -685,6 +688,8 @@ def main():
         tdist.barrier()
     torch.cuda.synchronize(dev)
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    lib = N.load()
+    n_launch0 = lib.iact_kernel_launches()
     for k in range(args.steps):
         flush_buf.fill_(float(k))
         opts.kernel_events[0] = kev[k][0].cuda_event
@@ -692,6 +697,7 @@ def main():
         ev[k][0].record(stream)
         out = fn(tel, src, val, stype, opts=opts)
         ev[k][1].record(stream)
+    n_launch = lib.iact_kernel_launches() - n_launch0  # the library's kernels in the timed steps
     torch.cuda.synchronize(dev)
     if dist:
         tdist.barrier()
@@ -918,7 +924,7 @@ def main():
                      "capture": ({"profile": cap["profile"], "digest": cap["digest"], "current": cap_ok}
                                  if cap else None)},
         "fwd_adjoint": fwdadj,
-        "gpu_launches": 3 * args.steps,  # k_prep, k_render, k_finish per step
+        "gpu_launches": n_launch,
         **({"culling": culling} if culling else {}),
         "clocks": clk,
     }

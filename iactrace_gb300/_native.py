@@ -127,6 +127,7 @@ _SIGS = {
                      _i, _i, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(IactOpts),
                      ctypes.c_void_p], ctypes.c_int),
     "iact_probe_fma": ([ctypes.c_void_p, _i, _i, ctypes.c_void_p], ctypes.c_int),
+    "iact_kernel_launches": ([], ctypes.c_int64),
     "iact_render_backward": ([ctypes.POINTER(IactScene), ctypes.POINTER(IactSensor), _i, ctypes.c_void_p,
                               ctypes.c_void_p, _i, _i, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                               ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,

@@ -29,6 +29,7 @@ import time
 import numpy as np
 import torch
 
+from . import _native as N
 from .core.apertures import PolygonAperture
 from .core.integrators import MCIntegrator
 from .core.render import render
@@ -116,7 +117,9 @@ def run(prob, steps: int = 200, lr: float = 2e-3, log_every: int = 0, checkpoint
     Adam moments, step count, history) and continues up to `steps` in
     total; the state is saved there every `checkpoint_every` steps and at
     the end. graph: after three eager steps, the whole Adam step (render,
-    loss, adjoint, optimiser) is captured in a CUDA graph and replayed."""
+    loss, adjoint, optimiser) is captured in a CUDA graph and replayed.
+    hist["launches_per_step"]: the library's kernels in one step (counted
+    around an eager step, or around the capture of the replayed step)."""
     tel, src, val, target = prob["telescope"], prob["sources"], prob["values"], prob["target"]
     base = prob["nominal"]
     # the facet positions and roughness scales stay fixed: keep them on the
@@ -145,6 +148,7 @@ def run(prob, steps: int = 200, lr: float = 2e-3, log_every: int = 0, checkpoint
             os.replace(tmp, checkpoint)
 
     scale = float(target.pow(2).sum())
+    lib = N.load()
 
     def body():
         rot = base + torch.cat([delta, pad], 1)
@@ -172,16 +176,20 @@ def run(prob, steps: int = 200, lr: float = 2e-3, log_every: int = 0, checkpoint
     with torch.cuda.stream(side) if graph else _nullctx():
         while it < n_eager:
             t0 = time.perf_counter()
+            n0 = lib.iact_kernel_launches()
             opt.zero_grad(set_to_none=True)
             loss, rot = body()
+            hist["launches_per_step"] = lib.iact_kernel_launches() - n0
             record(it, t0, loss, rot)
             it += 1
     if graph and it < steps:
         torch.cuda.current_stream(base.device).wait_stream(side)
         g = torch.cuda.CUDAGraph()
         opt.zero_grad(set_to_none=True)
+        n0 = lib.iact_kernel_launches()
         with torch.cuda.graph(g):
             s_loss, s_rot = body()
+        hist["launches_per_step"] = lib.iact_kernel_launches() - n0
         while it < steps:
             t0 = time.perf_counter()
             g.replay()

@@ -46,7 +46,7 @@ __global__ void __launch_bounds__(256) k_batch_prep(const BatchJob* __restrict__
 
 int launch_batch_prep(const BatchJob* jobs, int n_jobs, int gx, int backward, cudaStream_t st) {
   k_batch_prep<<<dim3(gx, n_jobs), 256, 0, st>>>(jobs, backward);
-  return check_cuda(cudaGetLastError(), "k_batch_prep launch");
+  return launched("k_batch_prep launch");
 }
 
 // AX: every job of the launch has an axis-aligned sensor (plane hit without
@@ -249,7 +249,7 @@ int iact::launch_batch_masks(const iact_batch* b, const BatchJob* jobs, int n_jo
     k_batch_masks<IACT_SRC_POINT><<<dim3(b->mask_gx, n_jobs), 256, b->mask_smem, st>>>(jobs);
   else
     k_batch_masks<IACT_SRC_PARALLEL><<<dim3(b->mask_gx, n_jobs), 256, b->mask_smem, st>>>(jobs);
-  return check_cuda(cudaGetLastError(), "k_batch_masks launch");
+  return launched("k_batch_masks launch");
 }
 
 extern "C" {
@@ -614,13 +614,13 @@ int iact_batch_render(iact_batch* b, void* stream) {
     k.htab_elems = C.htab_elems;
     k.hist_floats = C.hist_floats;
     class_kernel(b->src_type, b->mode, C)<<<C.grid, b->block, C.smem, st>>>(k);
-    rc = check_cuda(cudaGetLastError(), "k_batch_render launch");
+    rc = launched("k_batch_render launch");
     if (rc) return rc;
   }
   if (ev[1]) cudaEventRecord(static_cast<cudaEvent_t>(ev[1]), st);
   if (b->max_out > 0) {
     k_batch_finish<<<dim3(b->fin_gx, n_jobs), 256, 0, st>>>(jobs);
-    rc = check_cuda(cudaGetLastError(), "k_batch_finish launch");
+    rc = launched("k_batch_finish launch");
   }
   return rc;
 }

@@ -232,10 +232,10 @@ extern "C" int iact_batch_backward(iact_batch* b, void* stream) {
     k.hist_floats = C.a_mgrad_floats;
     reinterpret_cast<AdjKernel>(const_cast<void*>(batch_adjoint_kernel(b->src_type, b->mode, C)))
         <<<C.a_grid, b->block, C.a_smem, st>>>(k);
-    rc = check_cuda(cudaGetLastError(), "k_batch_adjoint launch");
+    rc = launched("k_batch_adjoint launch");
     if (rc) return rc;
   }
   if (ev[1]) cudaEventRecord(static_cast<cudaEvent_t>(ev[1]), st);
   k_batch_adjoint_finish<<<dim3(b->afin_gx, n_jobs), 32, 0, st>>>(jobs);  // one warp per block (FP64 trigonometry)
-  return check_cuda(cudaGetLastError(), "k_batch_adjoint_finish launch");
+  return launched("k_batch_adjoint_finish launch");
 }

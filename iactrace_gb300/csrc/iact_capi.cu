@@ -2,6 +2,7 @@
 // thread-local error messages, workspace sizing and dispatch.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cmath>
 #include <cstdint>
 #include <string>
@@ -13,7 +14,10 @@ namespace iact {
 
 namespace {
 thread_local std::string g_last_error;
+std::atomic<int64_t> g_launches{0};
 }
+
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 int set_error(int code, const std::string& msg) {
   g_last_error = msg;
@@ -106,6 +110,8 @@ extern "C" {
 int iact_abi_version(void) { return IACT_ABI_VERSION; }
 
 const char* iact_last_error(void) { return g_last_error.c_str(); }
+
+int64_t iact_kernel_launches(void) { return g_launches.load(std::memory_order_relaxed); }
 
 // sizes of the ABI structs as this library sees them (bindings check theirs);
 // a fifth slot receives sizeof(iact_job_t), a sixth sizeof(iact_sampler_t)

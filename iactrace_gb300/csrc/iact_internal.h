@@ -17,6 +17,18 @@ namespace iact {
 int set_error(int code, const std::string& msg);
 int check_cuda(cudaError_t e, const char* what);
 
+// one more kernel queued by the library (process-wide count behind
+// iact_kernel_launches); every launch site calls it after its launch
+void count_launch();
+
+// status of the `<<<...>>>` launch just made on this thread: counted when it
+// was queued, IACT_E_CUDA with `what` in the message when it was not
+inline int launched(const char* what) {
+  const cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) count_launch();
+  return check_cuda(e, what);
+}
+
 // Launch of a kernel that follows another kernel of the same chain on
 // `st` (prep -> masks -> render -> finish; prep -> masks -> adjoint ->
 // finish) with programmatic stream serialization: it may be scheduled while
@@ -35,7 +47,9 @@ inline cudaError_t launch_after(void (*kern)(KArgs...), dim3 grid, dim3 block, s
   attr[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, kern, static_cast<Args&&>(args)...);
+  const cudaError_t e = cudaLaunchKernelEx(&cfg, kern, static_cast<Args&&>(args)...);
+  if (e == cudaSuccess) count_launch();
+  return e;
 }
 
 // validation of the descriptors shared by every entry point

@@ -303,7 +303,7 @@ int launch_prep(const iact_scene_t* sc, const WsLayout& L, char* ws, cudaStream_
   const long long zb = (p.n_zero + 256LL * 8 - 1) / (256LL * 8);  // about 8 words per thread
   const int blocks = (int)std::min<long long>(std::max<long long>({1LL, (units + 7) / 8, zb}), 65535);
   k_prep<<<blocks, 256, 0, st>>>(p);
-  return check_cuda(cudaGetLastError(), "k_prep launch");
+  return launched("k_prep launch");
 }
 
 RenderK base_params(const iact_scene_t* sc, const iact_sensor_t* sn, const WsLayout& L, char* ws,
@@ -680,7 +680,7 @@ int launch_debug(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type, 
   if (rc) return rc;
   if (per_sm < 1) return set_error(IACT_E_UNSUPPORTED, "debug kernel does not fit on an SM with these tables");
   kern<<<grid, block, smem, st>>>(p, pts, vals, pix, hit_mirror);
-  return check_cuda(cudaGetLastError(), "k_debug launch");
+  return launched("k_debug launch");
 }
 
 __global__ void __launch_bounds__(256) k_probe_fma(float* out, int iters) {
@@ -701,7 +701,7 @@ __global__ void __launch_bounds__(256) k_probe_fma(float* out, int iters) {
 
 int launch_probe_fma(float* out, int blocks, int iters, cudaStream_t st) {
   k_probe_fma<<<blocks, 256, 0, st>>>(out, iters);
-  return check_cuda(cudaGetLastError(), "k_probe_fma launch");
+  return launched("k_probe_fma launch");
 }
 
 }  // namespace iact

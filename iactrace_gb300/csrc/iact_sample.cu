@@ -299,7 +299,7 @@ extern "C" int iact_sample_facets(const iact_sampler_t* s, float* points, float*
   if (n == 0) return IACT_OK;
   if (!points || !normals || !delta || !weights) return set_error(IACT_E_INVALID, "iact_sample_facets: NULL array");
   k_sample<<<(int)((n + 255) / 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(k, points, normals, delta, weights);
-  return check_cuda(cudaGetLastError(), "k_sample launch");
+  return launched("k_sample launch");
 }
 
 extern "C" int iact_sample_facets_backward(const iact_sampler_t* s, const float* g_points, const float* g_normals,
@@ -315,5 +315,5 @@ extern "C" int iact_sample_facets_backward(const iact_sampler_t* s, const float*
   const long long n = (long long)k.F * k.M;
   if (n == 0 || (!g_points && !g_normals && !g_delta && !g_weights)) return IACT_OK;
   k_sample_bwd<<<(int)((n + 255) / 256), 256, 0, st>>>(k, g_points, g_normals, g_delta, g_weights, g_surface);
-  return check_cuda(cudaGetLastError(), "k_sample_bwd launch");
+  return launched("k_sample_bwd launch");
 }

@@ -175,6 +175,11 @@ int iact_abi_layout(size_t* out, int n);
  * one float per thread to out[blocks*256]. */
 int iact_probe_fma(float* out, int32_t blocks, int32_t iters, void* stream);
 
+/* Diagnostics: kernels this library has queued, on any stream and thread,
+ * since it was loaded. Launches made while a stream is being captured into
+ * a CUDA graph are counted once, at capture; the graph's replays are not. */
+int64_t iact_kernel_launches(void);
+
 /* Bytes of scratch needed by a call of the given mode (IMAGE / RESPONSE:
  * iact_render, DEBUG: iact_render_debug) on this scene, sensor and source
  * count. Holds the world-space samples, the per-launch tables and the FP64

@@ -15,7 +15,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def declared_symbols():
     src = open(os.path.join(ROOT, "include", "iactrace_gb300.h")).read()
-    return sorted(set(re.findall(r"^\s*(?:int|void|const char\*)\s+(iact_\w+)\s*\(", src, re.M)))
+    return sorted(set(re.findall(r"^\s*(?:int|int64_t|void|const char\*)\s+(iact_\w+)\s*\(", src, re.M)))
 
 
 def test_exports_every_declared_symbol(built):
@@ -66,6 +66,19 @@ def test_render_rejects_bad_arguments_before_any_cuda_call(built):
     sn.type = N.SENSOR_HEX
     rc = built.iact_render(ctypes.byref(sc), ctypes.byref(sn), 0, None, None, 0, 0, None, None, 0, None, None)
     assert rc == N.IACT_E_INVALID and b"lookup table" in built.iact_last_error()
+
+
+def test_refused_calls_launch_nothing(built):
+    """The launch counter moves only for kernels actually queued: calls
+    refused by validation (and, without a GPU, launches that fail) leave
+    it where it was."""
+    n0 = built.iact_kernel_launches()
+    assert n0 >= 0
+    sc, sn = N.IactScene(), _square()
+    assert built.iact_render(ctypes.byref(sc), ctypes.byref(sn), 7, None, None, 0, 0, None, None, 0, None,
+                             None) == N.IACT_E_INVALID
+    assert built.iact_probe_fma(None, 1, 1, None) == N.IACT_E_INVALID
+    assert built.iact_kernel_launches() == n0
 
 
 def test_render_without_device_fails_loudly(built):
