@@ -872,7 +872,7 @@ def main():
     # the same call through a RenderPlan (copies in, render, copy out as one
     # CUDA graph per call), host clock, one call at a time; the result lands
     # in the plan's pinned buffer
-    plan = it.RenderPlan(tel, S, stype, mode=mode)
+    plan = it.RenderPlan(tel, S, stype, mode=mode, depth=2)
     for _ in range(2):
         plan(src_h, val_h, copy=False)
     pw = []
@@ -883,7 +883,30 @@ def main():
         plan(src_h, val_h, copy=False)
         pw.append(time.perf_counter() - t0)
     plan_s = sorted(pw)[len(pw) // 2]
-    del plan
+    # pipelined through RenderPlan.submit: each step copies the sources and
+    # values into the next of two slots, replays its graph (copies in,
+    # render, copy out) and takes the previous step's result, so the host
+    # prepares step k + 1 while the GPU runs step k; the L2-flush write
+    # before each step is on the plan's stream, its mean time subtracted as
+    # above; CUDA events on the plan's stream from the first step's start to
+    # the last copy-back's end
+    n_pipe = max(args.steps, 50)
+    pstart, pend = ev(), ev()
+    prev = None
+    for k in range(n_pipe):
+        with torch.cuda.stream(plan.stream):
+            flush_buf.fill_(float(k))
+            if k == 0:
+                pstart.record(plan.stream)
+        tk = plan.submit(src_h, val_h)
+        if prev is not None:
+            prev.result(copy=False)
+        prev = tk
+    pend.record(plan.stream)
+    prev.result(copy=False)
+    torch.cuda.synchronize(dev)
+    pipe_s = (pstart.elapsed_time(pend) / 1e3 - (n_pipe - 1) * fill_s) / n_pipe
+    del plan, prev, tk
     clk = clocks.stop()
 
     t = torch.tensor([step_s, kern_s, e2e_s], device=dev, dtype=torch.float64)
@@ -910,7 +933,12 @@ def main():
                                         "(median)"},
                 "plan_host_wall": {"value": rays * world / plan_s, "unit": "rays/s", "ms_per_step": plan_s * 1e3,
                                    "timing": "RenderPlan: copies in, render, copy out replayed as one CUDA graph "
-                                             "per call; host clock, one call at a time (median)"}},
+                                             "per call; host clock, one call at a time (median)"},
+                "plan_pipelined": {"value": rays * world / pipe_s, "unit": "rays/s", "ms_per_step": pipe_s * 1e3,
+                                   "steps": n_pipe,
+                                   "timing": "RenderPlan.submit with two slots, each step's result taken after "
+                                             "the next step is queued; CUDA events on the plan's stream, less the "
+                                             "L2-flush writes between steps"}},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                      "traffic": cap["dram_bytes"] if cap_ok else None,
                      "traffic_unit": "bytes per launch (ncu dram__bytes_read + write)",
