@@ -414,7 +414,11 @@ def run_alignment(args, rank, world):
                         "kernel_time_ratio_vs_fwd": (sorted(fw)[2] + adj_s * 1e3) / sorted(fw)[2]},
             "alignment": {"loss_first": hist["loss"][0], "loss_last": hist["loss"][-1],
                           "rms_tilt_error_mrad_first": hist["rms_mrad"][0],
-                          "rms_tilt_error_mrad_last": hist["rms_mrad"][-1], "adam_steps": steps},
+                          "rms_tilt_error_mrad_last": hist["rms_mrad"][-1], "adam_steps": steps,
+                          "note": "camera at the focus, where every facet's spot of a source falls on the "
+                                  "same place: the image loss falls, the per-facet tilts are not identifiable "
+                                  "from the summed image; with a defocused camera the same run recovers them "
+                                  "(tests/test_gpu_extended.py)"},
             # the library's kernels per Adam step (counted by the library around the
             # captured step) times the timed steps
             "gpu_launches": hist["launches_per_step"] * steps,
