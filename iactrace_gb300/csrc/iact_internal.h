@@ -104,7 +104,9 @@ SensorK make_sensor(const iact_sensor_t* s);
 // `block` threads: fills p.SB, FC, CC, n_fchunk, n_cchunk, n_tiles from
 // p.F, p.M, p.S and the opts knobs; without explicit knobs the tile shrinks
 // (down to one task per warp) until there are at least `min_tiles`.
-int plan_tiles(RenderK& p, int mode, int block, const iact_opts_t* opts, long long min_tiles);
+// sb_fixed > 0 fixes the sources per tile (32 for the source-per-lane body).
+int plan_tiles(RenderK& p, int mode, int block, const iact_opts_t* opts, long long min_tiles,
+               int sb_fixed = 0);
 // Shared-memory plan of one render: tables, int16 hex lookup table (if it
 // fits in half the budget) and FP32 histogram rows (if they fit). Floors let
 // a batch reserve the largest table sizes of all its jobs.

@@ -155,6 +155,15 @@ __global__ void __launch_bounds__(256, IACT_RENDER_MIN_CTAS) k_render_soft(const
   });
 }
 
+// k_render_soft for image renders of at least 32 sources, one source per
+// lane (render_tile_soft_spread).
+template <int SRC, bool HEX>
+__global__ void __launch_bounds__(256, IACT_RENDER_MIN_CTAS) k_render_soft_spread(const RenderK p) {
+  rows_tile_loop<IACT_MODE_IMAGE, HEX>(p, [&](const Obst& ob, const short* htab, float* rows, int tile) {
+    render_tile_soft_spread<SRC, HEX>(p, ob, htab, rows, tile);
+  });
+}
+
 // FP64 accumulator -> FP32 output
 __global__ void __launch_bounds__(256) k_finish(const double* __restrict__ acc, float* __restrict__ out, size_t n) {
   grid_dep_wait();  // the render's accumulator
@@ -424,6 +433,18 @@ int run_render_soft(int src_type, int mode, bool hex, RenderK p, int block, size
   if (src_type == IACT_SRC_EXTENDED) return run_render_soft_src<IACT_SRC_EXTENDED>(mode, hex, p, block, smem, st, ev);
   return run_render_soft_src<IACT_SRC_PARALLEL>(mode, hex, p, block, smem, st, ev);
 }
+// image renders of at least 32 sources (k_render_soft_spread)
+int run_render_soft_spread(int src_type, bool hex, RenderK p, int block, size_t smem, cudaStream_t st,
+                           void* const* ev) {
+  void (*kern)(const RenderK);
+  if (src_type == IACT_SRC_POINT)
+    kern = hex ? k_render_soft_spread<IACT_SRC_POINT, true> : k_render_soft_spread<IACT_SRC_POINT, false>;
+  else if (src_type == IACT_SRC_EXTENDED)
+    kern = hex ? k_render_soft_spread<IACT_SRC_EXTENDED, true> : k_render_soft_spread<IACT_SRC_EXTENDED, false>;
+  else
+    kern = hex ? k_render_soft_spread<IACT_SRC_PARALLEL, true> : k_render_soft_spread<IACT_SRC_PARALLEL, false>;
+  return run_persistent(kern, p, block, smem, st, ev);
+}
 
 template <int SRC, bool SOFT, int MODE>
 int dispatch_stages(bool stages, RenderK p, int block, size_t smem, cudaStream_t st, void* const* ev) {
@@ -490,7 +511,7 @@ WsLayout workspace_for(const iact_scene_t* sc, const iact_sensor_t* sn, int S, i
   return workspace_layout(sc, acc_elems(sn, S, mode), false, pair_mask_words(sc, S));
 }
 
-int plan_tiles(RenderK& p, int mode, int block, const iact_opts_t* opts, long long min_tiles) {
+int plan_tiles(RenderK& p, int mode, int block, const iact_opts_t* opts, long long min_tiles, int sb_fixed) {
   const int nw = block / 32;
   const int nch = (p.M + 31) / 32;
   const int S = p.S;
@@ -498,7 +519,7 @@ int plan_tiles(RenderK& p, int mode, int block, const iact_opts_t* opts, long lo
   // source halves that footprint and doubles the CTAs an SM holds
   int SB = (opts && opts->sources_per_cta > 0) ? opts->sources_per_cta
                                                : std::min(S, mode == IACT_MODE_RESPONSE ? std::max(1, nw / 2) : nw);
-  SB = std::max(1, std::min(SB, S));
+  SB = sb_fixed > 0 ? sb_fixed : std::max(1, std::min(SB, S));
   const bool fixed = opts && (opts->tasks_per_warp > 0 || opts->facets_per_tile > 0);
   // response tiles flush SB full rows each: larger tiles flush less often
   // (4096-source hard-hexagon response: 192 tasks per warp 3.23 ms, 96: 3.27,
@@ -596,7 +617,14 @@ int launch_render(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type,
   // 16 and 56.2 at 4)
   const long long tiles_per_sm =
       (hard && !soft && mode == IACT_MODE_IMAGE) ? 12 : (sc->n_mirrors > 0 ? 8 : (n_primitives(sc) > 32 ? 10 : 4));
-  rc = plan_tiles(p, mode, block, opts, tiles_per_sm * std::max(di.sm_count, 1));
+  const long long min_tiles = tiles_per_sm * std::max(di.sm_count, 1);
+  // soft-pixel images of at least 32 sources trace one source per lane
+  // (k_render_soft_spread) when full 32-source blocks fill at least 3/4 of
+  // the lanes (alignment render, 256 extended sources: the taps of one
+  // add instruction then seldom share an address)
+  bool spread = hard && soft && mode == IACT_MODE_IMAGE && S >= 32 && 4LL * S >= 3LL * 32 * ((S + 31) / 32) &&
+                !(opts && opts->sources_per_cta > 0);
+  rc = plan_tiles(p, mode, block, opts, min_tiles, spread ? 32 : 0);
   if (rc) return rc;
   const size_t smem_max = (size_t)std::min(di.smem_optin > 0 ? di.smem_optin : 49152, 200 * 1024);
   SmemPlan sp;
@@ -608,6 +636,11 @@ int launch_render(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type,
     use_hard = sp.rows_in_smem > 0 &&
                (sn->type == IACT_SENSOR_SQUARE || sn->type == IACT_SENSOR_SOFT_SQUARE || sp.hex_in_smem);
     smem = sp.tab_bytes + sp.htab_bytes + sp.hist_bytes;
+  }
+  if (spread && !use_hard) {  // the generic kernel keeps its own tile shape
+    spread = false;
+    rc = plan_tiles(p, mode, block, opts, min_tiles, 0);
+    if (rc) return rc;
   }
   if (!use_hard) {  // k_render: candidate masks of a tile's tasks in shared memory
     const size_t mask_bytes = sizeof(uint32_t) * (size_t)p.n_words * p.SB * p.FC;
@@ -634,7 +667,8 @@ int launch_render(const iact_scene_t* sc, const iact_sensor_t* sn, int src_type,
     const int tile_tasks = p.SB * p.FC * p.CC;
     p.flush_tiles = std::max(1, (soft ? 384 : 512) / std::max(tile_tasks, 1));
     void* const ev_end[2] = {nullptr, ev ? ev[1] : nullptr};
-    if (soft) rc = run_render_soft(src_type, mode, sn->type == IACT_SENSOR_SOFT_HEX, p, block, smem, st, ev_end);
+    if (spread) rc = run_render_soft_spread(src_type, sn->type == IACT_SENSOR_SOFT_HEX, p, block, smem, st, ev_end);
+    else if (soft) rc = run_render_soft(src_type, mode, sn->type == IACT_SENSOR_SOFT_HEX, p, block, smem, st, ev_end);
     else rc = run_render_hard(src_type, mode, sn->type == IACT_SENSOR_HEX, p, block, smem, st, ev_end);
   } else if (src_type == IACT_SRC_POINT) {
     rc = dispatch_soft<IACT_SRC_POINT>(soft, mode, stages, p, block, smem, st, ev);

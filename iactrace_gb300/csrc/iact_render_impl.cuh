@@ -231,6 +231,16 @@ __device__ __forceinline__ void warp_add(const SK& sink, int key, float v) {
   }
 }
 
+// Rows whose adds come from lanes on different sources' spots (the
+// source-per-lane tile body): a lane's address rarely equals another
+// lane's, so each lane adds on its own, without warp_add's vote.
+struct SpreadSink {
+  float* sh;
+};
+__device__ __forceinline__ void warp_add(const SpreadSink& sink, int key, float v) {
+  if (key >= 0 && v != 0.f) atomicAdd(sink.sh + key, v);
+}
+
 // sensors/square.py:144-172 DifferentiableSquareSensor.accumulate, one ray
 // (all lanes call; inactive lanes pass ok = false). Rays whose plane hit is
 // the 1e10 sentinel deposit nothing.
@@ -676,6 +686,81 @@ __device__ __forceinline__ void render_tile_soft(const RenderK& p, const Obst& o
   if (MODE == IACT_MODE_RESPONSE) {
     __syncthreads();
     flush_rows(p, sh_hist, s0, SBc);
+  }
+}
+
+// Soft-pixel image tile body with one source per lane (image renders of at
+// least 32 sources, p.SB == 32). A warp task is one (facet, sample) traced
+// towards the tile's 32 sources, so the 32 lanes' hits fall on 32 sources'
+// spots instead of on one source's spot. A shared-memory float add is a
+// compare-and-swap loop that runs once more for every lane sharing its
+// address, and the taps of one source's rays pile onto a few pixels; the
+// taps of different sources seldom meet. The sample point and normal are
+// warp-uniform loads; a lane's source, value and jitter basis stay in
+// registers for the whole tile; the candidate word of a facet is the OR of
+// the lanes' pair words (a superset, so the shadow tests stay exact). Each
+// ray runs the same floating-point operations as in render_tile_soft (the
+// same Philox stream per (source, facet, sample)); only the order of the
+// sums differs.
+template <int SRC, bool HEX>
+__device__ __forceinline__ void render_tile_soft_spread(const RenderK& p, const Obst& ob, const short* htab,
+                                                        float* sh_hist, int tile) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  const int per_s = p.n_fchunk * p.n_cchunk;
+  const int sblk = tile / per_s;
+  const int fc = (tile - sblk * per_s) / p.n_cchunk;
+  const int cc = tile - sblk * per_s - fc * p.n_cchunk;
+  const int f0 = fc * p.FC, m0 = cc * p.CC * 32;
+  const int FCc = min(p.FC, p.F - f0);
+  const int msz = min(p.CC * 32, p.M - m0);  // samples of each facet in this tile
+  const int s_lane = sblk * 32 + lane;
+  const bool sact = s_lane < p.S;
+  const int s = sact ? s_lane : p.S - 1;
+  constexpr int SS = (SRC == IACT_SRC_EXTENDED) ? 4 : 3;
+  const V3 src = mk(__ldg(p.sources + SS * s), __ldg(p.sources + SS * s + 1), __ldg(p.sources + SS * s + 2));
+  const float sig = (SRC == IACT_SRC_EXTENDED) ? __ldg(p.sources + SS * s + 3) : 0.f;
+  const float v = __ldg(p.values + s);
+  JBasis jb;
+  if (SRC == IACT_SRC_EXTENDED) jb = jitter_basis(src);
+  const SpreadSink sink{sh_hist};
+  const int T = FCc * msz;
+  const int tb = (warp * T) / nw, te = ((warp + 1) * T) / nw;
+  int fl = tb / msz, ml = tb - fl * msz;
+  int wf = -1;
+  uint32_t word = 0u;
+  for (int t = tb; t < te; ++t) {
+    const int f = f0 + fl, m = m0 + ml;
+    if (p.gmask && f != wf) {  // the facet's candidates for any of the lanes' sources (k_masks)
+      word = __reduce_or_sync(kFull, sact ? __ldg(p.gmask + (size_t)s * p.F + f) : 0u);
+      wf = f;
+    }
+    const int mi = f * p.M + m;  // F * M < 2^30
+    const float4 P = __ldg(p.P4 + mi), N = __ldg(p.N4 + mi);
+    const V3 tp = mk(P.x, P.y, P.z), tn = mk(N.x, N.y, N.z);
+    V3 d;
+    if (SRC == IACT_SRC_POINT) {
+      V3 dd = tp - src;  // dirs = normalize(tp - src)
+      d = rsqrtf(dot(dd, dd)) * dd;
+    } else if (SRC == IACT_SRC_EXTENDED) {
+      float z0, z1;
+      ray_normals(p.seed, s, f, m, z0, z1);
+      d = jitter_dir(jb, sig, z0, z1);
+    } else {
+      d = src;
+    }
+    bool sh = false;
+    if (word) sh = shadow_word(ob, word, tp, mk(-d.x, -d.y, -d.z));  // warp-uniform word
+    const float c = dot(d, tn);                                       // core/reflection.py:5-20
+    const V3 r = d - (2.f * c) * tn;
+    const float val = (v * -c * P.w) * (sh ? 0.f : 1.f);  // values * cos / tw * shadow
+    float x, y;
+    plane_hit<true>(p.sn, tp, r, x, y);
+    if (HEX) splat_hex(p.sn, htab, sink, 0, sact, x, y, val);
+    else splat_square(p.sn, sink, 0, sact, x, y, val);
+    if (++ml == msz) {
+      ml = 0;
+      ++fl;
+    }
   }
 }
 

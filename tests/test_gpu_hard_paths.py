@@ -4,9 +4,11 @@ Renders of single-stage scenes with at most 32 shadowing primitives and an
 axis-aligned sensor run k_render_hard (hard pixels) or k_render_soft (soft
 pixels, also extended sources), with candidate words per (source, facet)
 pair from k_masks; their adjoints k_adjoint_hard / k_adjoint_soft; batch
-classes whose jobs all qualify the batched hard-pixel forms. Everything else runs the generic
-kernels. Both evaluate the same per-ray arithmetic, so on the same scene
-they must give the same outputs up to the order of the sums: the generic
+classes whose jobs all qualify the batched hard-pixel forms; soft-pixel
+images of at least 32 sources k_render_soft_spread (one source per lane).
+Everything else runs the generic kernels. Both evaluate the same per-ray
+arithmetic, so on the same scene they must give the same outputs up to the
+order of the sums: the generic
 kernel is forced here by options the hard path does not take (histogram
 rows in the FP64 accumulator; roughness-scale gradients), and images,
 response matrices and gradients are compared at SUM_TOL (relative, per
@@ -50,13 +52,23 @@ def _scenes():
                                             W.hex_grid(2048, 0.042).astype(np.float32), sigma=0.5, kernel_size=1)
     ptel, psrc, pval, _ = plain
     ext = A.extended_sources(8, max_deg=2.0, seed=7)
+    # image renders of >= 32 sources take the source-per-lane soft body:
+    # 48 sources (a second, half-filled 32-source block) under the masts, 64
+    # extended sources
+    _, src48, val48, _ = W.plain_forward(n_samples=96, n_sources=48)
+    ext64 = A.extended_sources(64, max_deg=2.0, seed=9)
     return {"plain": plain, "response_hex": resp, "no_obstructions": bare, "parallel": par,
             "soft_square": (Telescope(ptel.mirror_groups, ptel.obstruction_groups, [soft_sq]), psrc, pval, "point"),
             "soft_hex_extended": (Telescope(tel.mirror_groups, tel.obstruction_groups, [soft_hx]), ext,
-                                  torch.ones(8), "extended")}
+                                  torch.ones(8), "extended"),
+            "soft_square_48": (Telescope(ptel.mirror_groups, ptel.obstruction_groups, [soft_sq]), src48, val48,
+                               "point"),
+            "soft_hex_extended_64": (Telescope(tel.mirror_groups, tel.obstruction_groups, [soft_hx]), ext64,
+                                     torch.rand(64, generator=torch.Generator().manual_seed(4)) + 0.5, "extended")}
 
 
-SCENES = ["plain", "response_hex", "no_obstructions", "parallel", "soft_square", "soft_hex_extended"]
+SCENES = ["plain", "response_hex", "no_obstructions", "parallel", "soft_square", "soft_hex_extended",
+          "soft_square_48", "soft_hex_extended_64"]
 
 
 @pytest.mark.parametrize("name", SCENES)
