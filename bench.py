@@ -66,17 +66,17 @@ KERNEL = {"response": "k_masks + k_render_hard", "plain": "k_masks + k_render_ha
 # have changed since, the figures are reported as stale and not used as the
 # roofline's traffic.
 CAPTURES = {
-    "response": {"digest": "00e8023f96eb6901", "profile": "profiles/k_render_hard_response_matrix_dc380_hex2048.md",
-                 "dram_bytes": 13.50e6, "shared_atomic_frac": 0.097, "thread_inst_per_ray": 175,
+    "response": {"digest": "8f1912f64f179566", "profile": "profiles/k_render_hard_response_matrix_dc380_hex2048.md",
+                 "dram_bytes": 13.51e6, "shared_atomic_frac": 0.097, "thread_inst_per_ray": 175,
                  "fma_pipe": 0.351, "issue_active": 0.850},
-    "plain": {"digest": "00e8023f96eb6901", "profile": "profiles/k_render_hard_plain_forward_dc380_square960.md",
+    "plain": {"digest": "8f1912f64f179566", "profile": "profiles/k_render_hard_plain_forward_dc380_square960.md",
               "dram_bytes": 12.21e6, "shared_atomic_frac": 0.082, "thread_inst_per_ray": 183,
-              "fma_pipe": 0.252, "issue_active": 0.673},
-    "cassegrain": {"digest": "00e8023f96eb6901", "profile": "profiles/k_render_cassegrain_61seg_square1024.md",
+              "fma_pipe": 0.249, "issue_active": 0.672},
+    "cassegrain": {"digest": "8f1912f64f179566", "profile": "profiles/k_render_cassegrain_61seg_square1024.md",
                    "dram_bytes": 1.050e6, "shared_atomic_frac": 0.025, "thread_inst_per_ray": 945,
-                   "fma_pipe": 0.390, "issue_active": 0.739},
-    "batched": {"digest": "00e8023f96eb6901", "profile": "profiles/k_batch_render_hard_ragged_batch64_hex960_2048.md",
-                "dram_bytes": 382.8e6, "thread_inst_per_ray": 188, "fma_pipe": 0.309, "issue_active": 0.804},
+                   "fma_pipe": 0.389, "issue_active": 0.740},
+    "batched": {"digest": "8f1912f64f179566", "profile": "profiles/k_batch_render_hard_ragged_batch64_hex960_2048.md",
+                "dram_bytes": 383.5e6, "thread_inst_per_ray": 188, "fma_pipe": 0.309, "issue_active": 0.804},
 }
 
 
